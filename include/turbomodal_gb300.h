@@ -1,0 +1,140 @@
+/*
+ * turbomodal_gb300 C ABI: GB300 (sm_103a) cyclic-symmetry modal solve.
+ *
+ * Plain C: opaque context, POD descriptors, caller-owned output buffers, int status
+ * codes (TMG_OK == 0) and a per-context last-error string.  No exception crosses the ABI.
+ * A context drives one CUDA device; its calls are not thread-safe with each other
+ * (one host thread per context).
+ *
+ * Each entry point names the reference interface it replaces (file:line in the
+ * turbomodal project).
+ */
+#ifndef TURBOMODAL_GB300_H
+#define TURBOMODAL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TMG_OK 0
+#define TMG_ERR_ARG 1      /* invalid argument / size */
+#define TMG_ERR_CUDA 2     /* CUDA runtime error (message in tmg_last_error) */
+#define TMG_ERR_STATE 3    /* call out of order (e.g. no sector uploaded) */
+#define TMG_ERR_NUMERIC 4  /* zero pivot, singular Jacobian, breakdown */
+#define TMG_ERR_NOMEM 5    /* device memory budget exceeded */
+#define TMG_ERR_TIMEOUT 6  /* a bounded device wait gave up */
+
+/* Matrix selectors for tmg_assemble / tmg_projection. */
+#define TMG_MAT_K 0        /* sector stiffness            assembler.cpp:11-69   */
+#define TMG_MAT_M 1        /* sector consistent mass      assembler.cpp:11-69   */
+#define TMG_MAT_KOMEGA 2   /* spin softening at rpm       assembler.cpp:157-218 */
+#define TMG_MAT_G 3        /* gyroscopic (no 2*omega)     assembler.cpp:157-218 */
+#define TMG_MAT_KSIGMA 4   /* stress stiffening at rpm    assembler.cpp:71-155  */
+#define TMG_MAT_KEFF 5     /* K - Komega + Ksigma         cyclic_solver.cpp:744-773 */
+#define TMG_MAT_KCF 10     /* free-space projections      cyclic_solver.cpp:560-671 */
+#define TMG_MAT_KPF 11
+#define TMG_MAT_MCF 12
+#define TMG_MAT_MPF 13
+#define TMG_MAT_GCF 14
+#define TMG_MAT_GPF 15
+#define TMG_MAT_K0R 20     /* real k=0 / k=N/2 matrices   cyclic_solver.cpp:673-723 */
+#define TMG_MAT_M0R 21
+#define TMG_MAT_KHR 22
+#define TMG_MAT_MHR 23
+#define TMG_MAT_KK 30      /* per-harmonic K_k, M_k       cyclic_solver.cpp:942-947 */
+#define TMG_MAT_MK 31
+
+/* Arithmetic of the shift-invert factorisation and triangular solves. */
+#define TMG_PREC_FP64 0    /* plain FP64 supernodal LDL^H */
+#define TMG_PREC_MIXED 1   /* FP32 LDL^H + FP64 iterative refinement of every solve */
+
+typedef struct tmg_context tmg_context;
+
+/* Sector mesh + material + cyclic boundary data.
+ * Replaces the state the reference CyclicSymmetrySolver constructor captures
+ * (cyclic_solver.cpp:88-105, mesh.hpp:40-53, material.cpp:5-13). */
+typedef struct {
+    int32_t num_nodes;
+    const double* coords;            /* num_nodes x 3, row-major */
+    int32_t num_elements;
+    const int32_t* connectivity;     /* num_elements x 10, TET10 node order of element.cpp:71-85 */
+    double E, nu, rho;
+    int32_t num_sectors;
+    int32_t rotation_axis;           /* 0 = X, 1 = Y, 2 = Z */
+    int32_t num_left;
+    const int32_t* left_nodes;       /* matched left boundary nodes  */
+    int32_t num_right;
+    const int32_t* right_nodes;      /* matched right boundary nodes */
+    int32_t num_pairs;
+    const int32_t* pairs;            /* (left, right) x num_pairs    */
+    int32_t num_constrained;
+    const int32_t* constrained_nodes;/* FIXED hub nodes (empty = free hub) */
+} tmg_sector_desc;
+
+/* Per-result metadata of a ModalResult (modal_solver.hpp:8-15). */
+typedef struct {
+    int32_t harmonic_index;
+    int32_t num_modes;
+    int32_t converged;
+    int32_t iterations;              /* Lanczos restarts used */
+    int32_t status;                  /* TMG_OK or the per-problem error code */
+    double rpm;
+    double max_residual;             /* max ||K x - lambda M x|| / ||K x|| over modes */
+    double refine_residual;          /* worst relative residual of a refined solve (mixed) */
+} tmg_result_meta;
+
+/* Context on one device with a device-memory budget (0 = 90% of free memory).
+ * Replaces the per-solver thread pool + memory cap (cyclic_solver.cpp:1226-1273). */
+int tmg_create(int device, size_t mem_budget_bytes, tmg_context** out);
+int tmg_destroy(tmg_context* ctx);
+const char* tmg_last_error(const tmg_context* ctx);
+
+/* Upload a sector; replaces CyclicSymmetrySolver(mesh, material, fluid, apply_hub)
+ * (python_bindings.cpp:321-331, cyclic_solver.cpp:88-105). */
+int tmg_upload_sector(tmg_context* ctx, const tmg_sector_desc* desc);
+
+/* Assemble one sector matrix on the device and copy it out as CSC (column pointers,
+ * sorted row indices, FP64 values).  Pass NULL arrays to query *nnz first.
+ * Replaces GlobalAssembler::assemble / K() / M() / K_omega() / G() / K_sigma()
+ * (assembler.cpp:11-218, python_bindings.cpp:162-197). */
+int tmg_assemble(tmg_context* ctx, int which, double rpm, int64_t* nnz,
+                 int32_t* colptr, int32_t* rowidx, double* values);
+
+/* Build the rotating-effect operators and the cyclic projections at one speed
+ * (cyclic_solver.cpp:735-899). */
+int tmg_prepare(tmg_context* ctx, double rpm, int coriolis);
+
+/* Copy a projected matrix (complex interleaved values) after tmg_prepare.
+ * k selects the harmonic for TMG_MAT_KK / TMG_MAT_MK.  Pass NULL arrays to query. */
+int tmg_projection(tmg_context* ctx, int which, int k, int64_t* nnz, int32_t* n,
+                   int32_t* colptr, int32_t* rowidx, double* values);
+
+/* Fill-reducing order, elimination tree and L column counts of the shift-invert operator
+ * K_k - sigma M_k (kind 0: complex harmonics; 1: k = 0; 2: k = N/2), as the reference's
+ * SimplicialLDLT<..., Lower>::analyzePattern computes them (hermitian_lanczos.cpp:20).
+ * perm[j] = original index of pivot j.  Pass NULL arrays to query *n. */
+int tmg_symbolic(tmg_context* ctx, int kind, int32_t* n, int32_t* perm, int32_t* parent,
+                 int32_t* colcount);
+
+/* Full modal solve at one speed; replaces CyclicSymmetrySolver::solve_at_rpm
+ * (cyclic_solver.cpp:725-1357, python_bindings.cpp:332-361).  harmonics == NULL or
+ * nh == 0 solves k = 0..N/2.  Results stay in the context until the next solve. */
+int tmg_solve_at_rpm(tmg_context* ctx, double rpm, int num_modes, const int32_t* harmonics, int nh,
+                     int coriolis, double min_frequency, int precision, int32_t* num_results);
+
+/* Result access (ModalResult fields, modal_solver.hpp:8-15).  shapes: num_dof x num_modes
+ * complex interleaved, column-major; NULL skips the copy. */
+int tmg_result_info(tmg_context* ctx, int idx, tmg_result_meta* info);
+int tmg_result_copy(tmg_context* ctx, int idx, double* freqs, double* shapes, int32_t* whirl);
+
+/* Device time (ms) spent in each phase of the last solve, and launch count of this
+ * library's kernels in it. */
+int tmg_last_timing(tmg_context* ctx, double* phase_ms, int nphase, int64_t* kernel_launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TURBOMODAL_GB300_H */

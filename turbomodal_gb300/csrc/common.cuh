@@ -1,0 +1,84 @@
+// Shared device/host helpers: complex types, error handling, launch accounting.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+namespace tmg {
+
+struct cuda_error : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct numeric_error : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+#define TMG_CUDA(call)                                                                        \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            throw ::tmg::cuda_error(std::string(#call) + ": " + cudaGetErrorString(e_) +      \
+                                    " (" __FILE__ ":" + std::to_string(__LINE__) + ")");      \
+    } while (0)
+
+// Every kernel launch of this library goes through TMG_LAUNCH so the host can report
+// how many of its kernels ran in a timed region.
+extern int64_t g_kernel_launches;
+#define TMG_LAUNCH(kernel, grid, block, smem, stream, ...)                                    \
+    do {                                                                                      \
+        kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);                            \
+        ::tmg::g_kernel_launches++;                                                           \
+    } while (0)
+#define TMG_CHECK_LAUNCH() TMG_CUDA(cudaGetLastError())
+
+// Minimal complex types (interleaved re/im), usable on host and device.
+template <typename R>
+struct cpx {
+    R x, y;
+};
+using zd = cpx<double>;
+using zf = cpx<float>;
+
+template <typename T> struct real_of { using type = T; };
+template <typename R> struct real_of<cpx<R>> { using type = R; };
+
+#define HD __host__ __device__ __forceinline__
+template <typename R> HD cpx<R> mk(R a, R b) { return cpx<R>{a, b}; }
+template <typename R> HD cpx<R> operator+(cpx<R> a, cpx<R> b) { return {a.x + b.x, a.y + b.y}; }
+template <typename R> HD cpx<R> operator-(cpx<R> a, cpx<R> b) { return {a.x - b.x, a.y - b.y}; }
+template <typename R> HD cpx<R> operator*(cpx<R> a, cpx<R> b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+template <typename R> HD cpx<R> operator*(R s, cpx<R> a) { return {s * a.x, s * a.y}; }
+template <typename R> HD cpx<R> operator*(cpx<R> a, R s) { return {s * a.x, s * a.y}; }
+template <typename R> HD cpx<R> operator/(cpx<R> a, R s) { return {a.x / s, a.y / s}; }
+template <typename R> HD cpx<R>& operator+=(cpx<R>& a, cpx<R> b) { a.x += b.x; a.y += b.y; return a; }
+template <typename R> HD cpx<R>& operator-=(cpx<R>& a, cpx<R> b) { a.x -= b.x; a.y -= b.y; return a; }
+template <typename R> HD cpx<R> conj(cpx<R> a) { return {a.x, -a.y}; }
+template <typename R> HD R re(cpx<R> a) { return a.x; }
+template <typename R> HD R abs2(cpx<R> a) { return a.x * a.x + a.y * a.y; }
+HD double conj(double a) { return a; }
+HD float conj(float a) { return a; }
+HD double re(double a) { return a; }
+HD float re(float a) { return a; }
+HD double abs2(double a) { return a * a; }
+HD float abs2(float a) { return a * a; }
+
+template <typename T> HD T zero_of();
+template <> HD double zero_of<double>() { return 0.0; }
+template <> HD float zero_of<float>() { return 0.0f; }
+template <> HD zd zero_of<zd>() { return zd{0.0, 0.0}; }
+template <> HD zf zero_of<zf>() { return zf{0.0f, 0.0f}; }
+
+// conversion between precisions (used at the mixed-precision boundary)
+template <typename To, typename From> HD To conv(From a);
+template <> HD double conv<double, double>(double a) { return a; }
+template <> HD float conv<float, double>(double a) { return (float)a; }
+template <> HD double conv<double, float>(float a) { return (double)a; }
+template <> HD zd conv<zd, zd>(zd a) { return a; }
+template <> HD zf conv<zf, zd>(zd a) { return zf{(float)a.x, (float)a.y}; }
+template <> HD zd conv<zd, zf>(zf a) { return zd{(double)a.x, (double)a.y}; }
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace tmg

@@ -1,0 +1,1518 @@
+// Host runtime + C ABI of the GB300 cyclic-symmetry modal solve.
+//
+// Data flow for one speed (reference: src/cyclic_solver.cpp:725-1357):
+//   element kernels -> candidate-pattern gathers (K, M, Komega, G, Ksigma)      [device]
+//   static prestress: (Tr^T K Tr) projection, supernodal LDL^T, solve            [device]
+//   cyclic projections Kc/Kp/Mc/Mp (+Gc/Gp): two-stage gathers with pruning      [device]
+//   per harmonic: operator K_k - sigma M_k formed on the union pattern, scattered
+//   into fronts, multifrontal LDL^H (FP64, or FP32 + FP64 refinement), Lanczos    [device]
+// Host work is pattern-only (symbolic analysis, cached per pattern) plus the small
+// per-restart control decisions.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <set>
+
+#include "../../include/turbomodal_gb300.h"
+#include "engine.hpp"
+#include "fe.cuh"
+
+namespace tmg {
+
+constexpr double PI = 3.14159265358979323846;
+
+// ------------------------------------------------------------------------------------
+// small device kernels of the runtime
+// ------------------------------------------------------------------------------------
+__global__ void k_proj1(int64_t n, const int64_t* __restrict__ p, const int64_t* __restrict__ src,
+                        const double* __restrict__ coef, const double* __restrict__ A, double* __restrict__ out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    double acc = 0.0;
+    for (int64_t q = p[e]; q < p[e + 1]; q++) {
+        const double t = coef[q] * A[src[q]];
+        acc = (q == p[e]) ? t : acc + t;
+    }
+    out[e] = acc;
+}
+
+__global__ void k_proj2(int64_t n, const int64_t* __restrict__ p, const int64_t* __restrict__ src,
+                        const double* __restrict__ coef, const double* __restrict__ I, double tol,
+                        double* __restrict__ out, uint8_t* __restrict__ flag) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    double acc = 0.0;
+    for (int64_t q = p[e]; q < p[e + 1]; q++) {
+        const double t = I[src[q]] * coef[q];
+        acc = (q == p[e]) ? t : acc + t;
+    }
+    out[e] = acc;
+    flag[e] = fabs(acc) > tol ? 1 : 0;
+}
+
+__global__ void k_gather(int64_t n, const int64_t* __restrict__ idx, const double* __restrict__ src,
+                         double* __restrict__ out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e < n) out[e] = idx[e] >= 0 ? src[idx[e]] : 0.0;
+}
+
+template <typename T>
+__global__ void k_gather_t(int64_t n, const int64_t* __restrict__ idx, const T* __restrict__ src, T* __restrict__ out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e < n) out[e] = src[idx[e]];
+}
+
+template <typename T, typename U>
+__global__ void k_gather_conv(int64_t n, const int64_t* __restrict__ idx, const U* __restrict__ src, T* __restrict__ out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e < n) out[e] = conv<T, U>(src[idx[e]]);
+}
+
+// Complex harmonic operator on the union pattern:
+//   ((kc + P kp) + conj(P) kph) - sigma ((mc + P mp) + conj(P) mph)
+// with missing constituents read as exact zeros (the reference's sparse-sum semantics,
+// src/cyclic_solver.cpp:946-947, src/hermitian_lanczos.cpp:15).
+__global__ void k_form_complex(int64_t n, const int64_t* __restrict__ ikc, const int64_t* __restrict__ ikp,
+                               const int64_t* __restrict__ ikh, const int64_t* __restrict__ imc,
+                               const int64_t* __restrict__ imp, const int64_t* __restrict__ imh,
+                               const double* __restrict__ kc, const double* __restrict__ kp,
+                               const double* __restrict__ mc, const double* __restrict__ mp, double Pr, double Pi,
+                               double sigma, double kscale, zd* __restrict__ out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const double a = ikc[e] >= 0 ? kc[ikc[e]] : 0.0;
+    const double b = ikp[e] >= 0 ? kp[ikp[e]] : 0.0;
+    const double c = ikh[e] >= 0 ? kp[ikh[e]] : 0.0;
+    const double am = imc[e] >= 0 ? mc[imc[e]] : 0.0;
+    const double bm = imp[e] >= 0 ? mp[imp[e]] : 0.0;
+    const double cm = imh[e] >= 0 ? mp[imh[e]] : 0.0;
+    const zd P{Pr, Pi}, Pc{Pr, -Pi};
+    const zd kk = (zd{a, 0.0} + P * zd{b, 0.0}) + Pc * zd{c, 0.0};
+    const zd mm = (zd{am, 0.0} + P * zd{bm, 0.0}) + Pc * zd{cm, 0.0};
+    out[e] = kscale * kk - sigma * mm;
+}
+
+// Real (k = 0 or N/2) sums (kc + s kp) + s kph and their |v| > 1e-15 flags.
+__global__ void k_form_real_sum(int64_t n, const int64_t* __restrict__ ic, const int64_t* __restrict__ ip,
+                                const int64_t* __restrict__ ih, const double* __restrict__ c,
+                                const double* __restrict__ p, double s, double* __restrict__ out,
+                                uint8_t* __restrict__ flag) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const double a = ic[e] >= 0 ? c[ic[e]] : 0.0;
+    const double b = ip[e] >= 0 ? p[ip[e]] : 0.0;
+    const double h = ih[e] >= 0 ? p[ih[e]] : 0.0;
+    const double v = (a + s * b) + s * h;
+    out[e] = v;
+    flag[e] = fabs(v) > 1e-15 ? 1 : 0;
+}
+
+__global__ void k_form_real_op(int64_t n, const int64_t* __restrict__ ik, const int64_t* __restrict__ im,
+                               const double* __restrict__ kv, const double* __restrict__ mv, double sigma,
+                               double kscale, double* __restrict__ out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const double a = ik[e] >= 0 ? kv[ik[e]] : 0.0;
+    const double b = im[e] >= 0 ? mv[im[e]] : 0.0;
+    out[e] = kscale * a - sigma * b;
+}
+
+// u_red (reduced numbering) = scatter of x_free; out_full = T0 u_red with right rows * P
+__global__ void k_expand(int32_t nfull, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                         const double* __restrict__ tv, const uint8_t* __restrict__ isr, const int32_t* __restrict__ r2f,
+                         const zd* __restrict__ x, int64_t ldx, zd P, zd* __restrict__ out, int64_t ldo) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nfull) return;
+    const int64_t v = blockIdx.y;
+    zd s{0.0, 0.0};
+    for (int64_t q = rp[i]; q < rp[i + 1]; q++) {
+        const int32_t f = r2f[ci[q]];
+        if (f >= 0) s += tv[q] * x[v * ldx + f];
+    }
+    out[v * ldo + i] = isr[i] ? s * P : s;
+}
+
+__global__ void k_real_to_complex(int64_t n, const double* __restrict__ a, zd* __restrict__ b) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = zd{a[i], 0.0};
+}
+
+// F_cyc = Tr^T F (gather over the transposed transformation), and u = Tr u_cyc
+__global__ void k_csr_real(int32_t nrows, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                           const double* __restrict__ v, const double* __restrict__ x, double* __restrict__ y) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nrows) return;
+    double s = 0.0;
+    for (int64_t q = rp[i]; q < rp[i + 1]; q++) s += v[q] * x[ci[q]];
+    y[i] = s;
+}
+
+template <typename T>
+__global__ void k_restart_norm(int64_t n, int nev, const T* __restrict__ dot, const T* __restrict__ f,
+                               const T* __restrict__ Mf, T* __restrict__ V, T* __restrict__ MV,
+                               double* __restrict__ beta) {
+    const double b = sqrt(fabs(re(dot[0])));
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b > 1e-14) {
+        if (i == 0) beta[nev - 1] = b;
+        if (i < n) {
+            V[(int64_t)nev * n + i] = f[i] / b;
+            MV[(int64_t)nev * n + i] = Mf[i] / b;
+        }
+    } else if (i == 0) {
+        beta[nev - 1] = 0.0;
+    }
+}
+
+template <typename T, typename U>
+__global__ void k_conv_copy(int64_t n, const U* __restrict__ a, T* __restrict__ b) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = conv<T, U>(a[i]);
+}
+
+template <typename T>
+__global__ void k_gather_i32(int64_t n, const int32_t* __restrict__ idx, const T* __restrict__ src, T* __restrict__ dst) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[idx[i]];
+}
+
+template <typename T>
+__global__ void k_scatter_vec(int64_t n, const int32_t* __restrict__ idx, const T* __restrict__ src, T* __restrict__ dst) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) dst[idx[i]] = src[i];
+}
+
+// ------------------------------------------------------------------------------------
+// host helpers
+// ------------------------------------------------------------------------------------
+inline unsigned nblk(int64_t n, int b = 256) { return (unsigned)std::max<int64_t>(1, ceil_div(n, b)); }
+
+Pattern transpose_map(const Pattern& A, std::vector<int64_t>& map) {
+    Pattern B;
+    B.nrows = A.ncols; B.ncols = A.nrows;
+    B.p.assign(B.ncols + 1, 0);
+    for (int32_t r : A.i) B.p[r + 1]++;
+    for (int32_t c = 0; c < B.ncols; c++) B.p[c + 1] += B.p[c];
+    B.i.resize(A.i.size());
+    map.assign(A.i.size(), -1);
+    std::vector<int64_t> pos(B.p.begin(), B.p.end() - 1);
+    for (int32_t j = 0; j < A.ncols; j++)
+        for (int64_t q = A.p[j]; q < A.p[j + 1]; q++) {
+            const int64_t d = pos[A.i[q]]++;
+            B.i[d] = j;
+            map[d] = q;
+        }
+    return B;
+}
+
+Flagged flagged(const Pattern& cand, const std::vector<uint8_t>& f) {
+    Flagged F;
+    F.pat.nrows = cand.nrows; F.pat.ncols = cand.ncols;
+    F.pat.p.assign(cand.ncols + 1, 0);
+    for (int32_t j = 0; j < cand.ncols; j++) {
+        for (int64_t q = cand.p[j]; q < cand.p[j + 1]; q++)
+            if (f[q]) { F.pat.i.push_back(cand.i[q]); F.cand.push_back(q); }
+        F.pat.p[j + 1] = (int64_t)F.pat.i.size();
+    }
+    return F;
+}
+
+// Sub-pattern selection by a predicate on (row, col), keeping the source slot index.
+template <typename Pred>
+Flagged select(const Pattern& A, const std::vector<int64_t>& src, Pred pred) {
+    Flagged F;
+    F.pat.nrows = A.nrows; F.pat.ncols = A.ncols;
+    F.pat.p.assign(A.ncols + 1, 0);
+    for (int32_t j = 0; j < A.ncols; j++) {
+        for (int64_t q = A.p[j]; q < A.p[j + 1]; q++)
+            if (pred(A.i[q], j)) { F.pat.i.push_back(A.i[q]); F.cand.push_back(src.empty() ? q : src[q]); }
+        F.pat.p[j + 1] = (int64_t)F.pat.i.size();
+    }
+    return F;
+}
+
+// Build the projection chain for C = (Tt * A) * T where A's entries live at `asrc`
+// positions of a device value array.
+void build_chain(ProjChain& ch, const Pattern& Tt, const std::vector<double>& Ttv, const Flagged& A,
+                 const Pattern& T, const std::vector<double>& Tv) {
+    Product P1 = product(Tt, A.pat);
+    Product P2 = product(P1.C, T);
+    ch.C = P2.C;
+    ch.n1 = P1.C.nnz();
+    ch.n2 = P2.C.nnz();
+    std::vector<int64_t> src1(P1.a_slot.size()), src2(P2.a_slot.size());
+    std::vector<double> c1(P1.a_slot.size()), c2(P2.a_slot.size());
+    for (size_t q = 0; q < P1.a_slot.size(); q++) { c1[q] = Ttv[P1.a_slot[q]]; src1[q] = A.cand[P1.b_slot[q]]; }
+    for (size_t q = 0; q < P2.a_slot.size(); q++) { src2[q] = P2.a_slot[q]; c2[q] = Tv[P2.b_slot[q]]; }
+    ch.p1.upload(P1.cptr); ch.src1.upload(src1); ch.coef1.upload(c1);
+    ch.p2.upload(P2.cptr); ch.src2.upload(src2); ch.coef2.upload(c2);
+    ch.I.alloc(ch.n1); ch.Cv.alloc(ch.n2); ch.Cf.alloc(ch.n2);
+}
+
+void run_chain(cudaStream_t st, ProjChain& ch, const double* A, double tol) {
+    if (ch.n1) TMG_LAUNCH(k_proj1, nblk(ch.n1), 256, 0, st, ch.n1, ch.p1.p, ch.src1.p, ch.coef1.p, A, ch.I.p);
+    if (ch.n2) TMG_LAUNCH(k_proj2, nblk(ch.n2), 256, 0, st, ch.n2, ch.p2.p, ch.src2.p, ch.coef2.p, ch.I.p, tol, ch.Cv.p, ch.Cf.p);
+    TMG_CHECK_LAUNCH();
+}
+
+// Free-space extraction of the pruned projection (src/cyclic_solver.cpp:644-658).
+void extract_free(cudaStream_t st, const ProjChain& ch, const std::vector<int32_t>& r2free, int32_t nfree,
+                  FreeMat& out) {
+    std::vector<uint8_t> f = ch.Cf.download();
+    out.pat.nrows = out.pat.ncols = nfree;
+    out.pat.p.assign(nfree + 1, 0);
+    out.pat.i.clear();
+    std::vector<int64_t> idx;
+    for (int32_t j = 0; j < ch.C.ncols; j++) {
+        const int32_t fj = r2free[j];
+        if (fj < 0) continue;
+        for (int64_t q = ch.C.p[j]; q < ch.C.p[j + 1]; q++) {
+            const int32_t fi = r2free[ch.C.i[q]];
+            if (fi >= 0 && f[q]) { out.pat.i.push_back(fi); idx.push_back(q); }
+        }
+        out.pat.p[fj + 1] = (int64_t)out.pat.i.size();
+    }
+    for (int32_t j = 0; j < nfree; j++) out.pat.p[j + 1] = std::max(out.pat.p[j + 1], out.pat.p[j]);
+    out.idx.upload(idx);
+    out.v.alloc(idx.size());
+    if (!idx.empty()) TMG_LAUNCH(k_gather, nblk(idx.size()), 256, 0, st, (int64_t)idx.size(), out.idx.p, ch.Cv.p, out.v.p);
+    TMG_CHECK_LAUNCH();
+}
+
+// Union of patterns with per-constituent index maps, CSR view and lower triangle.
+void build_union(UnionMaps& um, const std::vector<const Pattern*>& parts) {
+    um.U = pattern_union(parts);
+    um.maps.clear();
+    for (const Pattern* P : parts) {
+        std::vector<int64_t> loc = locate(um.U, *P);
+        std::vector<int64_t> m(um.U.nnz(), -1);
+        for (size_t q = 0; q < loc.size(); q++) m[loc[q]] = (int64_t)q;
+        DVec<int64_t> d;
+        d.upload(m);
+        um.maps.push_back(std::move(d));
+    }
+    std::vector<int64_t> tmap;
+    Pattern Ut = transpose_map(um.U, tmap);   // CSC of U^T == CSR of U
+    um.csr2csc.upload(tmap);
+    um.csr_rowptr.upload(Ut.p);
+    um.csr_col.upload(Ut.i);
+    um.lower = lower_triangle(um.U);
+    std::vector<int64_t> l2c;
+    for (int32_t j = 0; j < um.U.ncols; j++)
+        for (int64_t q = um.U.p[j]; q < um.U.p[j + 1]; q++)
+            if (um.U.i[q] >= j) l2c.push_back(q);
+    um.lower2csc.upload(l2c);
+}
+
+}  // namespace tmg
+
+// =====================================================================================
+// Context
+// =====================================================================================
+using namespace tmg;
+
+struct ResultHost {
+    int32_t k = 0;
+    double rpm = 0.0;
+    std::vector<double> freqs;
+    std::vector<int32_t> whirl;
+    std::vector<zd> shapes;          // ndof x m
+    int32_t converged = 0, iterations = 0, status = 0;
+    double max_residual = 0.0, refine_residual = 0.0;
+};
+
+struct tmg_context {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    size_t budget = 0;
+    std::string err;
+    std::unique_ptr<Sector> sec;
+    // candidate-pattern matrices
+    CandMat K, M, Kw, G, Ks, Keff;
+    bool have_KM = false;
+    double kw_omega = -1.0;
+    // static prestress operator (k = 0 reduced stiffness without hub DOFs)
+    bool static_ready = false;
+    ProjChain stat_chain;
+    FreeMat stat_free;
+    OpSymbolic stat_sym;
+    UnionMaps stat_union;
+    DVec<double> stat_F, stat_t, stat_x, stat_vals;
+    std::vector<int32_t> stat_free_idx;     // free position -> reduced index
+    DVec<int32_t> dstat_free_idx;
+    DVec<double> u_static;
+    // prepared speed
+    bool prepared = false;
+    double rpm = 0.0;
+    bool coriolis = false;
+    ProjChain chK[2], chM[2], chG[2];
+    Flagged fK, fM, fG;
+    FreeMat Kcf, Kpf, Mcf, Mpf, Gcf, Gpf;
+    std::vector<int64_t> kpT, mpT;
+    Pattern KpfH, MpfH;
+    // operators
+    UnionMaps opC, opMC;                 // complex harmonic operator and its mass part
+    OpSymbolic symC;
+    std::string symC_key;
+    UnionMaps W0, WM0;                   // real-sum domains (Kc + s Kp + s Kp^H)
+    struct RealOp {
+        FreeMat Kr, Mr;
+        UnionMaps op;
+        OpSymbolic sym;
+        std::string key;
+        bool valid = false;
+    } real[2];                            // 0: k = 0, 1: k = N/2
+    std::vector<ResultHost> results;
+    double phase_ms[8] = {0};
+    int64_t launches = 0;
+};
+
+namespace {
+
+int set_err(tmg_context* c, int code, const std::string& m) {
+    if (c) c->err = m;
+    return code;
+}
+
+template <typename F>
+int guarded(tmg_context* c, F&& fn) {
+    try {
+        cudaSetDevice(c->device);
+        return fn();
+    } catch (const cuda_error& e) {
+        return set_err(c, TMG_ERR_CUDA, e.what());
+    } catch (const numeric_error& e) {
+        return set_err(c, TMG_ERR_NUMERIC, e.what());
+    } catch (const std::bad_alloc&) {
+        return set_err(c, TMG_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return set_err(c, TMG_ERR_ARG, e.what());
+    }
+}
+
+// ---- sector set-up -------------------------------------------------------------------
+void setup_sector(tmg_context* c, const tmg_sector_desc* d) {
+    auto S = std::make_unique<Sector>();
+    S->nn = d->num_nodes; S->ne = d->num_elements; S->ns = d->num_sectors; S->axis = d->rotation_axis;
+    S->E = d->E; S->nu = d->nu; S->rho = d->rho;
+    if (S->nn <= 0 || S->ne <= 0) throw std::invalid_argument("empty mesh");
+    if (S->ns <= 0) throw std::invalid_argument("num_sectors must be positive");
+    if (S->axis < 0 || S->axis > 2) throw std::invalid_argument("rotation_axis must be 0, 1 or 2");
+    if (S->E <= 0.0) throw std::invalid_argument("Young's modulus E must be positive");
+    if (S->nu <= 0.0 || S->nu >= 0.5) throw std::invalid_argument("Poisson's ratio nu must be in (0, 0.5)");
+    if (S->rho <= 0.0) throw std::invalid_argument("Density rho must be positive");
+    S->X.assign(d->coords, d->coords + (size_t)3 * S->nn);
+    S->conn.assign(d->connectivity, d->connectivity + (size_t)10 * S->ne);
+    for (int32_t v : S->conn)
+        if (v < 0 || v >= S->nn) throw std::invalid_argument("connectivity references an unknown node");
+    S->left.assign(d->left_nodes, d->left_nodes + d->num_left);
+    S->right.assign(d->right_nodes, d->right_nodes + d->num_right);
+    for (int k = 0; k < d->num_pairs; k++) S->pairs.push_back({d->pairs[2 * k], d->pairs[2 * k + 1]});
+    S->hub.assign(d->constrained_nodes, d->constrained_nodes + d->num_constrained);
+    const int32_t nn = S->nn, ndof = 3 * nn;
+    // DOF classes (src/cyclic_solver.cpp:214-238)
+    std::vector<uint8_t> isl(nn, 0), isr(nn, 0);
+    for (int32_t v : S->left) isl.at(v) = 1;
+    for (int32_t v : S->right) isr.at(v) = 1;
+    S->is_right.assign(ndof, 0);
+    for (int32_t i = 0; i < nn; i++)
+        for (int dd = 0; dd < 3; dd++) {
+            const int32_t dof = 3 * i + dd;
+            if (isr[i]) { S->right_dofs.push_back(dof); S->is_right[dof] = 1; }
+            else if (isl[i]) S->left_dofs.push_back(dof);
+            else S->interior_dofs.push_back(dof);
+        }
+    S->f2r.assign(ndof, -1);
+    int32_t idx = 0;
+    for (int32_t dof : S->interior_dofs) S->f2r[dof] = idx++;
+    for (int32_t dof : S->left_dofs) S->f2r[dof] = idx++;
+    S->n_reduced = idx;
+    std::set<int32_t> cons;
+    for (int32_t nid : S->hub) { cons.insert(3 * nid); cons.insert(3 * nid + 1); cons.insert(3 * nid + 2); }
+    std::vector<int32_t> r2full;
+    r2full.insert(r2full.end(), S->interior_dofs.begin(), S->interior_dofs.end());
+    r2full.insert(r2full.end(), S->left_dofs.begin(), S->left_dofs.end());
+    S->r2free.assign(S->n_reduced, -1);
+    for (int32_t r = 0; r < S->n_reduced; r++)
+        if (!cons.count(r2full[r])) { S->r2free[r] = (int32_t)S->free_reduced_map.size(); S->free_reduced_map.push_back(r); }
+    S->n_free = (int32_t)S->free_reduced_map.size();
+    // T(0): identity on interior + left, rotation on right rows (src/cyclic_solver.cpp:240-330)
+    {
+        const double alpha = 2.0 * PI / S->ns;
+        const double ca = std::cos(alpha), sa = std::sin(alpha);
+        int c1, c2, cax;
+        if (S->axis == 0) { c1 = 1; c2 = 2; cax = 0; }
+        else if (S->axis == 1) { c1 = 0; c2 = 2; cax = 1; }
+        else { c1 = 0; c2 = 1; cax = 2; }
+        std::vector<int32_t> r2l(nn, -1);
+        for (auto& pr : S->pairs) r2l.at(pr.second) = pr.first;
+        // (row, col, value) triplets, unique positions
+        std::vector<std::vector<std::pair<int32_t, double>>> rows(ndof);
+        for (int32_t dof : S->interior_dofs) rows[dof].push_back({S->f2r[dof], 1.0});
+        for (int32_t dof : S->left_dofs) rows[dof].push_back({S->f2r[dof], 1.0});
+        std::vector<uint8_t> done(nn, 0);
+        for (int32_t rd : S->right_dofs) {
+            const int32_t rn = rd / 3;
+            if (done[rn]) continue;
+            done[rn] = 1;
+            const int32_t ln = r2l[rn];
+            if (ln < 0) throw std::invalid_argument("Right boundary node " + std::to_string(rn) + " has no matched left partner");
+            const int32_t l1 = S->f2r[3 * ln + c1], l2 = S->f2r[3 * ln + c2], lax = S->f2r[3 * ln + cax];
+            if (l1 < 0 || l2 < 0 || lax < 0) throw std::invalid_argument("matched left node is on the right boundary");
+            const int32_t rb = 3 * rn;
+            rows[rb + c1].push_back({l1, ca}); rows[rb + c1].push_back({l2, -sa});
+            rows[rb + c2].push_back({l1, sa}); rows[rb + c2].push_back({l2, ca});
+            rows[rb + cax].push_back({lax, 1.0});
+        }
+        // CSC of T (full x reduced) and of its real filtered copy (|v| > 1e-15)
+        auto build = [&](bool filt, Pattern& T, std::vector<double>& Tv) {
+            T.nrows = ndof; T.ncols = S->n_reduced;
+            T.p.assign(S->n_reduced + 1, 0);
+            std::vector<std::vector<std::pair<int32_t, double>>> cols(S->n_reduced);
+            for (int32_t r = 0; r < ndof; r++)
+                for (auto& e : rows[r])
+                    if (!filt || std::fabs(e.second) > 1e-15) cols[e.first].push_back({r, e.second});
+            T.i.clear(); Tv.clear();
+            for (int32_t cc = 0; cc < S->n_reduced; cc++) {
+                std::sort(cols[cc].begin(), cols[cc].end());
+                for (auto& e : cols[cc]) { T.i.push_back(e.first); Tv.push_back(e.second); }
+                T.p[cc + 1] = (int64_t)T.i.size();
+            }
+        };
+        build(false, S->T0, S->T0v);
+        build(true, S->Tr, S->Trv);
+        std::vector<int64_t> mp;
+        S->T0t = transpose_map(S->T0, mp);
+        S->T0tv.resize(mp.size());
+        for (size_t q = 0; q < mp.size(); q++) S->T0tv[q] = S->T0v[mp[q]];
+        S->Trt = transpose_map(S->Tr, mp);
+        S->Trtv.resize(mp.size());
+        for (size_t q = 0; q < mp.size(); q++) S->Trtv[q] = S->Trv[mp[q]];
+    }
+    // node adjacency -> candidate pattern
+    {
+        std::vector<std::vector<int32_t>> adj(nn);
+        for (int32_t e = 0; e < S->ne; e++)
+            for (int a = 0; a < 10; a++)
+                for (int b = 0; b < 10; b++) adj[S->conn[(size_t)e * 10 + b]].push_back(S->conn[(size_t)e * 10 + a]);
+        S->nadj_p.assign(nn + 1, 0);
+        for (int32_t v = 0; v < nn; v++) {
+            auto& L = adj[v];
+            std::sort(L.begin(), L.end());
+            L.erase(std::unique(L.begin(), L.end()), L.end());
+            S->nadj_p[v + 1] = S->nadj_p[v] + (int64_t)L.size();
+        }
+        S->nadj_i.resize(S->nadj_p[nn]);
+        for (int32_t v = 0; v < nn; v++) std::copy(adj[v].begin(), adj[v].end(), S->nadj_i.begin() + S->nadj_p[v]);
+        S->npairs = S->nadj_p[nn];
+        Pattern& C = S->cand;
+        C.nrows = C.ncols = ndof;
+        C.p.assign(ndof + 1, 0);
+        C.i.resize(9 * S->npairs);
+        std::vector<int64_t> candp(ndof + 1, 0);
+        for (int32_t nb = 0; nb < nn; nb++) {
+            const int64_t deg = S->nadj_p[nb + 1] - S->nadj_p[nb];
+            for (int dd = 0; dd < 3; dd++) {
+                const int64_t base = 9 * S->nadj_p[nb] + 3 * deg * dd;
+                C.p[3 * nb + dd] = base;
+                for (int64_t t = 0; t < deg; t++)
+                    for (int cc = 0; cc < 3; cc++) C.i[base + 3 * t + cc] = 3 * S->nadj_i[S->nadj_p[nb] + t] + cc;
+            }
+        }
+        C.p[ndof] = 9 * S->npairs;
+        std::vector<int32_t> pcol(S->npairs), ppos(S->npairs);
+        for (int32_t nb = 0; nb < nn; nb++)
+            for (int64_t q = S->nadj_p[nb]; q < S->nadj_p[nb + 1]; q++) { pcol[q] = nb; ppos[q] = (int32_t)(q - S->nadj_p[nb]); }
+        // contributions per node pair in element order
+        std::vector<int64_t> cnt(S->npairs + 1, 0);
+        auto pair_of = [&](int32_t na, int32_t nb) -> int64_t {
+            const int32_t* b = S->nadj_i.data() + S->nadj_p[nb];
+            const int32_t* e = S->nadj_i.data() + S->nadj_p[nb + 1];
+            return S->nadj_p[nb] + (std::lower_bound(b, e, na) - b);
+        };
+        for (int32_t e = 0; e < S->ne; e++)
+            for (int a = 0; a < 10; a++)
+                for (int b = 0; b < 10; b++) cnt[pair_of(S->conn[(size_t)e * 10 + a], S->conn[(size_t)e * 10 + b]) + 1]++;
+        for (int64_t q = 0; q < S->npairs; q++) cnt[q + 1] += cnt[q];
+        std::vector<int32_t> cl(cnt[S->npairs]);
+        std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
+        for (int32_t e = 0; e < S->ne; e++)
+            for (int a = 0; a < 10; a++)
+                for (int b = 0; b < 10; b++)
+                    cl[pos[pair_of(S->conn[(size_t)e * 10 + a], S->conn[(size_t)e * 10 + b])]++] = e * 100 + a * 10 + b;
+        // node -> (element, local node) in element order, for load vectors
+        std::vector<int64_t> np(nn + 1, 0);
+        for (int32_t v : S->conn) np[v + 1]++;
+        for (int32_t v = 0; v < nn; v++) np[v + 1] += np[v];
+        std::vector<int32_t> nl(np[nn]);
+        std::vector<int64_t> npos(np.begin(), np.end() - 1);
+        for (int32_t e = 0; e < S->ne; e++)
+            for (int a = 0; a < 10; a++) nl[npos[S->conn[(size_t)e * 10 + a]]++] = e * 10 + a;
+        S->dX.upload(S->X);
+        S->dconn.upload(S->conn);
+        S->pair_col.upload(pcol);
+        S->pair_pos.upload(ppos);
+        S->clist.upload(cl);
+        S->cptr.upload(cnt);
+        S->dnadj_p.upload(S->nadj_p);
+        std::vector<int64_t> cp(C.p.begin(), C.p.end());
+        S->dcand_p.upload(cp);
+        S->nptr.upload(np);
+        S->nlist.upload(nl);
+    }
+    c->sec = std::move(S);
+    c->have_KM = false;
+    c->static_ready = false;
+    c->prepared = false;
+    c->kw_omega = -1.0;
+    c->symC.valid = false;
+    c->symC_key.clear();
+    c->real[0].valid = c->real[1].valid = false;
+    c->results.clear();
+}
+
+void ensure_elem_buffers(Sector& S) {
+    S.Kel.alloc((size_t)S.ne * 900);
+    S.Mel.alloc((size_t)S.ne * 900);
+}
+
+void gather_into(tmg_context* c, const double* Kel, CandMat& out) {
+    Sector& S = *c->sec;
+    out.v.alloc(S.cand.nnz());
+    out.f.alloc(S.cand.nnz());
+    launch_gather_blocks(c->st, S.npairs, S.pair_col.p, S.pair_pos.p, S.dnadj_p.p, S.cptr.p, S.clist.p, S.dcand_p.p,
+                         Kel, out.v.p, out.f.p);
+}
+
+void assemble_KM(tmg_context* c) {
+    if (c->have_KM) return;
+    Sector& S = *c->sec;
+    ensure_elem_buffers(S);
+    DVec<int> neg;
+    neg.alloc(1);
+    neg.zero(c->st);
+    launch_elem_KM(c->st, S.ne, S.dX.p, S.dconn.p, S.E, S.nu, S.rho, S.Kel.p, S.Mel.p, neg.p);
+    gather_into(c, S.Kel.p, c->K);
+    gather_into(c, S.Mel.p, c->M);
+    c->have_KM = true;
+}
+
+void assemble_rot(tmg_context* c, double omega) {
+    if (c->kw_omega == omega) return;
+    Sector& S = *c->sec;
+    ensure_elem_buffers(S);
+    launch_elem_rot(c->st, S.ne, S.dX.p, S.dconn.p, S.rho, omega, S.axis, S.Kel.p, S.Mel.p);
+    gather_into(c, S.Kel.p, c->Kw);
+    gather_into(c, S.Mel.p, c->G);
+    c->kw_omega = omega;
+}
+
+// ---- factorisation + solve helpers ---------------------------------------------------
+void analyze_op(OpSymbolic& os, const UnionMaps& um) {
+    os.S = analyze(um.lower, 0.0, 0);
+    std::vector<int64_t> dest;
+    std::vector<uint8_t> cj;
+    scatter_map(os.S, um.lower, dest, cj);
+    os.D.upload(os.S, dest, cj);
+    os.valid = true;
+}
+
+std::string pattern_key(const Pattern& P) {
+    // cheap fingerprint of a pattern (size + rolling hash)
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) { h ^= v; h *= 1099511628211ull; };
+    mix((uint64_t)P.nrows); mix((uint64_t)P.nnz());
+    for (int64_t v : P.p) mix((uint64_t)v);
+    for (int32_t v : P.i) mix((uint64_t)v);
+    return std::to_string(h);
+}
+
+// Static prestress operator: (Tr^T K Tr).pruned, hub DOFs removed (cyclic_solver.cpp:456-541)
+void ensure_static(tmg_context* c) {
+    if (c->static_ready) return;
+    Sector& S = *c->sec;
+    assemble_KM(c);
+    Flagged fk = flagged(S.cand, c->K.f.download());
+    build_chain(c->stat_chain, S.Trt, S.Trtv, fk, S.Tr, S.Trv);
+    run_chain(c->st, c->stat_chain, c->K.v.p, 1e-15 * 1e-12);
+    // free DOFs of the static solve: hub-constrained reduced DOFs removed
+    extract_free(c->st, c->stat_chain, S.r2free, S.n_free, c->stat_free);
+    build_union(c->stat_union, {&c->stat_free.pat});
+    analyze_op(c->stat_sym, c->stat_union);
+    // values -> fronts, factor (FP64 real)
+    const DevSymbolic& D = c->stat_sym.D;
+    c->stat_F.alloc(D.front_entries);
+    c->stat_F.zero(c->st);
+    c->stat_vals.alloc(c->stat_union.lower2csc.n);
+    DVec<double> full;
+    full.alloc(c->stat_union.U.nnz());
+    if (full.n)
+        TMG_LAUNCH(k_gather, nblk(full.n), 256, 0, c->st, (int64_t)full.n, c->stat_union.maps[0].p, c->stat_free.v.p, full.p);
+    if (c->stat_vals.n)
+        TMG_LAUNCH(k_gather_t<double>, nblk(c->stat_vals.n), 256, 0, c->st, (int64_t)c->stat_vals.n,
+                   c->stat_union.lower2csc.p, full.p, c->stat_vals.p);
+    mf_scatter<double>(c->st, D, c->stat_vals.p, c->stat_F.p);
+    DVec<int> status;
+    status.alloc(1);
+    status.zero(c->st);
+    mf_factor<double>(c->st, D, c->stat_F.p, status.p);
+    int hs = 0;
+    TMG_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    TMG_CUDA(cudaStreamSynchronize(c->st));
+    if (hs) throw numeric_error("static prestress factorisation hit a zero pivot");
+    c->stat_t.alloc(std::max<int64_t>(1, D.ns ? (int64_t)c->stat_sym.S.sn_row_ptr.back() : 1));
+    c->stat_x.alloc(S.n_free);
+    std::vector<int32_t> fr(S.free_reduced_map.begin(), S.free_reduced_map.end());
+    c->dstat_free_idx.upload(fr);
+    c->static_ready = true;
+}
+
+// u(omega) = Tr u_cyc with K_cyc,free u_free = (Tr^T F)_free (cyclic_solver.cpp:461-557)
+void static_solve(tmg_context* c, double omega) {
+    Sector& S = *c->sec;
+    ensure_static(c);
+    const DevSymbolic& D = c->stat_sym.D;
+    DVec<double> Fe, F, Fc, uc;
+    Fe.alloc((size_t)S.ne * 30);
+    F.alloc(3 * (size_t)S.nn);
+    launch_elem_fc(c->st, S.ne, S.dX.p, S.dconn.p, S.rho, omega, S.axis, Fe.p);
+    launch_gather_load(c->st, S.nn, S.nptr.p, S.nlist.p, Fe.p, F.p);
+    DVec<int64_t> trp, trtp;
+    DVec<int32_t> tri, trti;
+    DVec<double> trv, trtv;
+    trp.upload(S.Tr.p); tri.upload(S.Tr.i); trv.upload(S.Trv);       // CSC of Tr == CSR of Tr^T
+    trtp.upload(S.Trt.p); trti.upload(S.Trt.i); trtv.upload(S.Trtv); // CSC of Tr^T == CSR of Tr
+    Fc.alloc(S.n_reduced);
+    TMG_LAUNCH(k_csr_real, nblk(S.n_reduced), 256, 0, c->st, S.n_reduced, trp.p, tri.p, trv.p, F.p, Fc.p);
+    DVec<double> ff;
+    ff.alloc(S.n_free);
+    TMG_LAUNCH(k_gather_i32<double>, nblk(S.n_free), 256, 0, c->st, (int64_t)S.n_free, c->dstat_free_idx.p, Fc.p, ff.p);
+    mf_permute_in<double, double>(c->st, D, ff.p, c->stat_x.p, 1, S.n_free);
+    mf_solve<double>(c->st, D, c->stat_F.p, c->stat_x.p, c->stat_t.p);
+    mf_permute_out<double, double>(c->st, D, c->stat_x.p, ff.p, 1, S.n_free);
+    uc.alloc(S.n_reduced);
+    uc.zero(c->st);
+    TMG_LAUNCH(k_scatter_vec<double>, nblk(S.n_free), 256, 0, c->st, (int64_t)S.n_free, c->dstat_free_idx.p, ff.p, uc.p);
+    c->u_static.alloc(3 * (size_t)S.nn);
+    TMG_LAUNCH(k_csr_real, nblk(3 * (int64_t)S.nn), 256, 0, c->st, 3 * S.nn, trtp.p, trti.p, trtv.p, uc.p, c->u_static.p);
+    TMG_CHECK_LAUNCH();
+    TMG_CUDA(cudaStreamSynchronize(c->st));
+}
+
+}  // namespace
+
+namespace {
+
+// ---- cyclic projections ----------------------------------------------------------------
+struct ChainCache {
+    std::string key;
+};
+
+void project(tmg_context* c, const CandMat& A, ProjChain* ch, Flagged& fl, FreeMat& cf, FreeMat& pf, double tol) {
+    Sector& S = *c->sec;
+    Flagged f = flagged(S.cand, A.f.download());
+    const bool same_pat = (f.pat.p == fl.pat.p) && (f.pat.i == fl.pat.i) && ch[0].n2 > 0;
+    if (!same_pat) {
+        fl = f;
+        const std::vector<uint8_t>& isr = S.is_right;
+        Flagged as = select(fl.pat, fl.cand, [&](int32_t r, int32_t cc) { return isr[r] == isr[cc]; });
+        Flagged an = select(fl.pat, fl.cand, [&](int32_t r, int32_t cc) { return !isr[r] && isr[cc]; });
+        build_chain(ch[0], S.T0t, S.T0tv, as, S.T0, S.T0v);
+        build_chain(ch[1], S.T0t, S.T0tv, an, S.T0, S.T0v);
+    }
+    run_chain(c->st, ch[0], A.v.p, tol);
+    run_chain(c->st, ch[1], A.v.p, tol);
+    extract_free(c->st, ch[0], S.r2free, S.n_free, cf);
+    extract_free(c->st, ch[1], S.r2free, S.n_free, pf);
+}
+
+bool same_pattern(const Pattern& a, const Pattern& b) { return a.p == b.p && a.i == b.i && a.nrows == b.nrows; }
+
+void prepare(tmg_context* c, double rpm, bool coriolis) {
+    Sector& S = *c->sec;
+    const double omega = rpm * 2.0 * PI / 60.0;
+    auto t0 = std::chrono::steady_clock::now();
+    assemble_KM(c);
+    const int64_t nc = S.cand.nnz();
+    c->Keff.v.alloc(nc);
+    c->Keff.f.alloc(nc);
+    if (std::fabs(omega) > 0.0) {
+        assemble_rot(c, omega);
+        if (!S.hub.empty()) {
+            static_solve(c, omega);
+            ensure_elem_buffers(S);
+            DVec<int> bad;
+            bad.alloc(1);
+            bad.zero(c->st);
+            launch_elem_ksig(c->st, S.ne, S.dX.p, S.dconn.p, S.E, S.nu, c->u_static.p, S.Kel.p, bad.p);
+            gather_into(c, S.Kel.p, c->Ks);
+            int hb = 0;
+            TMG_CUDA(cudaMemcpy(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost));
+            if (hb) throw numeric_error("TET10::B_matrix: singular Jacobian (degenerate element)");
+            launch_cand_axpy3(c->st, nc, 1.0, c->K.v.p, c->K.f.p, -1.0, c->Kw.v.p, c->Kw.f.p, 1.0, c->Ks.v.p,
+                              c->Ks.f.p, c->Keff.v.p, c->Keff.f.p);
+        } else {
+            launch_cand_axpy3(c->st, nc, 1.0, c->K.v.p, c->K.f.p, -1.0, c->Kw.v.p, c->Kw.f.p, 0.0, nullptr, nullptr,
+                              c->Keff.v.p, c->Keff.f.p);
+        }
+    } else {
+        launch_cand_axpy3(c->st, nc, 1.0, c->K.v.p, c->K.f.p, 0.0, nullptr, nullptr, 0.0, nullptr, nullptr,
+                          c->Keff.v.p, c->Keff.f.p);
+    }
+    project(c, c->Keff, c->chK, c->fK, c->Kcf, c->Kpf, 1e-27);
+    project(c, c->M, c->chM, c->fM, c->Mcf, c->Mpf, 1e-27);
+    c->coriolis = coriolis && std::fabs(omega) > 0.0;
+    if (c->coriolis) project(c, c->G, c->chG, c->fG, c->Gcf, c->Gpf, 1e-27);
+    // complex harmonic operator: union of Kc, Kp, Kp^H, Mc, Mp, Mp^H
+    c->KpfH = transpose_map(c->Kpf.pat, c->kpT);
+    c->MpfH = transpose_map(c->Mpf.pat, c->mpT);
+    Pattern U = pattern_union({&c->Kcf.pat, &c->Kpf.pat, &c->KpfH, &c->Mcf.pat, &c->Mpf.pat, &c->MpfH});
+    const std::string key = pattern_key(U) + pattern_key(c->Kcf.pat) + pattern_key(c->Kpf.pat) +
+                            pattern_key(c->Mcf.pat) + pattern_key(c->Mpf.pat);
+    if (key != c->symC_key) {
+        build_union(c->opC, {&c->Kcf.pat, &c->Kpf.pat, &c->KpfH, &c->Mcf.pat, &c->Mpf.pat, &c->MpfH});
+        build_union(c->opMC, {&c->Mcf.pat, &c->Mpf.pat, &c->MpfH});
+        // transposed-constituent maps must address the un-transposed value arrays
+        for (int which : {2, 5}) {
+            const std::vector<int64_t>& tm = which == 2 ? c->kpT : c->mpT;
+            std::vector<int64_t> m = c->opC.maps[which].download();
+            for (auto& v : m) if (v >= 0) v = tm[v];
+            c->opC.maps[which].upload(m);
+        }
+        {
+            std::vector<int64_t> m = c->opMC.maps[2].download();
+            for (auto& v : m) if (v >= 0) v = c->mpT[v];
+            c->opMC.maps[2].upload(m);
+        }
+        c->symC.valid = false;
+        c->symC_key = key;
+        // real sums domain W = Kc u Kp u Kp^H (and the mass analogue)
+        build_union(c->W0, {&c->Kcf.pat, &c->Kpf.pat, &c->KpfH});
+        build_union(c->WM0, {&c->Mcf.pat, &c->Mpf.pat, &c->MpfH});
+        for (UnionMaps* w : {&c->W0, &c->WM0}) {
+            const std::vector<int64_t>& tm = (w == &c->W0) ? c->kpT : c->mpT;
+            std::vector<int64_t> m = w->maps[2].download();
+            for (auto& v : m) if (v >= 0) v = tm[v];
+            w->maps[2].upload(m);
+        }
+    }
+    // real k = 0 / N/2 matrices: filtered sums (cyclic_solver.cpp:673-723)
+    for (int h = 0; h < 2; h++) {
+        if (h == 1 && !(S.ns % 2 == 0 && S.ns / 2 > 0)) { c->real[h].valid = false; continue; }
+        const double sgn = h == 0 ? 1.0 : -1.0;
+        auto& R = c->real[h];
+        Pattern newK, newM;
+        DVec<double> kv, mv;
+        DVec<uint8_t> kf, mf;
+        for (int which = 0; which < 2; which++) {
+            UnionMaps& w = which == 0 ? c->W0 : c->WM0;
+            const FreeMat& cc = which == 0 ? c->Kcf : c->Mcf;
+            const FreeMat& pp = which == 0 ? c->Kpf : c->Mpf;
+            DVec<double>& vv = which == 0 ? kv : mv;
+            DVec<uint8_t>& ff = which == 0 ? kf : mf;
+            vv.alloc(w.U.nnz());
+            ff.alloc(w.U.nnz());
+            if (w.U.nnz())
+                TMG_LAUNCH(k_form_real_sum, nblk(w.U.nnz()), 256, 0, c->st, w.U.nnz(), w.maps[0].p, w.maps[1].p,
+                           w.maps[2].p, cc.v.p, pp.v.p, sgn, vv.p, ff.p);
+            Flagged fl = flagged(w.U, ff.download());
+            FreeMat& dst = which == 0 ? R.Kr : R.Mr;
+            dst.pat = fl.pat;
+            dst.idx.upload(fl.cand);
+            dst.v.alloc(fl.cand.size());
+            if (!fl.cand.empty())
+                TMG_LAUNCH(k_gather, nblk(fl.cand.size()), 256, 0, c->st, (int64_t)fl.cand.size(), dst.idx.p, vv.p,
+                           dst.v.p);
+            TMG_CUDA(cudaStreamSynchronize(c->st));
+        }
+        const std::string rkey = pattern_key(R.Kr.pat) + pattern_key(R.Mr.pat);
+        if (!R.valid || rkey != R.key) {
+            build_union(R.op, {&R.Kr.pat, &R.Mr.pat});
+            R.sym.valid = false;
+            R.key = rkey;
+        }
+        R.valid = true;
+    }
+    TMG_CUDA(cudaStreamSynchronize(c->st));
+    c->prepared = true;
+    c->rpm = rpm;
+    c->phase_ms[0] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+namespace {
+
+__global__ void k_form_csum(int64_t n, const int64_t* __restrict__ ic, const int64_t* __restrict__ ip,
+                            const int64_t* __restrict__ ih, const double* __restrict__ c, const double* __restrict__ p,
+                            double Pr, double Pi, zd* __restrict__ out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const double a = ic[e] >= 0 ? c[ic[e]] : 0.0;
+    const double b = ip[e] >= 0 ? p[ip[e]] : 0.0;
+    const double h = ih[e] >= 0 ? p[ih[e]] : 0.0;
+    const zd P{Pr, Pi}, Pc{Pr, -Pi};
+    out[e] = (zd{a, 0.0} + P * zd{b, 0.0}) + Pc * zd{h, 0.0};
+}
+
+// free-space degenerate duplication: column m <- src m/2, conjugated when m is odd
+__global__ void k_dup_conj(int64_t n, int nx, const zd* __restrict__ X, zd* __restrict__ Y) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int m = blockIdx.y;
+    if (i >= n || m >= nx) return;
+    const zd v = X[(int64_t)(m / 2) * n + i];
+    Y[(int64_t)m * n + i] = (m % 2 == 0) ? v : conj(v);
+}
+
+template <typename T>
+__global__ void k_resid(int64_t n, int nm, const T* __restrict__ AX, const T* __restrict__ MX, const double* __restrict__ lam,
+                        double sigma, T* __restrict__ KX, T* __restrict__ R) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int m = blockIdx.y;
+    if (i >= n || m >= nm) return;
+    const int64_t q = (int64_t)m * n + i;
+    const T kx = AX[q] + sigma * MX[q];      // K x = (K - sigma M) x + sigma M x
+    KX[q] = kx;
+    R[q] = kx - lam[m] * MX[q];
+}
+
+template <typename Tv, typename Tf>
+struct ShiftInvert {
+    tmg_context* c = nullptr;
+    const DevSymbolic* D = nullptr;
+    int32_t n = 0;
+    bool mixed = false;
+    int nref = 2;
+    DevCsr<Tv> A;                 // FP64 operator K - sigma M (CSR)
+    DVec<Tf> F, tb, xw;
+    DVec<Tv> r, d;
+    double worst_refine = 0.0;
+    int diag_left = 1;
+    DVec<double> np, nrm;
+
+    void factor(const Tv* lower_vals, int64_t nlower) {
+        F.alloc(D->front_entries);
+        F.zero(c->st);
+        if constexpr (std::is_same<Tv, Tf>::value) {
+            mf_scatter<Tf>(c->st, *D, lower_vals, F.p);
+        } else {
+            DVec<Tf> lv;
+            lv.alloc(nlower);
+            TMG_LAUNCH((k_conv_copy<Tf, Tv>), nblk(nlower), 256, 0, c->st, nlower, lower_vals, lv.p);
+            mf_scatter<Tf>(c->st, *D, lv.p, F.p);
+            TMG_CUDA(cudaStreamSynchronize(c->st));
+        }
+        DVec<int> status;
+        status.alloc(1);
+        status.zero(c->st);
+        mf_factor<Tf>(c->st, *D, F.p, status.p);
+        int hs = 0;
+        TMG_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+        TMG_CUDA(cudaStreamSynchronize(c->st));
+        if (hs) throw numeric_error("zero pivot in LDL^H factorisation at column " + std::to_string(hs - 1));
+        tb.alloc(std::max<int64_t>(1, sn_rows_total()));
+        xw.alloc(n);
+        r.alloc(n);
+        d.alloc(n);
+        np.alloc(LZ_DOT_BLOCKS);
+        nrm.alloc(2);
+    }
+    int64_t sn_rows_total() const {
+        int64_t last = 0;
+        TMG_CUDA(cudaMemcpy(&last, D->sn_row_ptr + D->ns, sizeof(int64_t), cudaMemcpyDeviceToHost));
+        return last;
+    }
+    void solve1(const Tv* b, Tv* x) {
+        mf_permute_in<Tf, Tv>(c->st, *D, b, xw.p, 1, n);
+        mf_solve<Tf>(c->st, *D, F.p, xw.p, tb.p);
+        mf_permute_out<Tf, Tv>(c->st, *D, xw.p, x, 1, n);
+    }
+    void apply(const Tv* b, Tv* x) {
+        solve1(b, x);
+        if (!mixed) return;
+        const bool diag = diag_left > 0;
+        double bn = 0.0;
+        if (diag) {
+            lz_norm2<Tv>(c->st, n, b, np.p, nrm.p);
+            TMG_CUDA(cudaMemcpy(&bn, nrm.p, sizeof(double), cudaMemcpyDeviceToHost));
+        }
+        for (int it = 0; it < nref; it++) {
+            lz_copy<Tv>(c->st, n, b, r.p);
+            lz_spmv<Tv>(c->st, A, x, r.p, 1, n, true);
+            if (diag) {
+                double rn = 0.0;
+                lz_norm2<Tv>(c->st, n, r.p, np.p, nrm.p);
+                TMG_CUDA(cudaMemcpy(&rn, nrm.p, sizeof(double), cudaMemcpyDeviceToHost));
+                worst_refine = std::max(worst_refine, std::sqrt(rn / std::max(bn, 1e-300)));
+            }
+            solve1(r.p, d.p);
+            lz_axpy<Tv>(c->st, n, 1.0, d.p, x);
+        }
+        if (diag) {
+            double rn = 0.0;
+            lz_copy<Tv>(c->st, n, b, r.p);
+            lz_spmv<Tv>(c->st, A, x, r.p, 1, n, true);
+            lz_norm2<Tv>(c->st, n, r.p, np.p, nrm.p);
+            TMG_CUDA(cudaMemcpy(&rn, nrm.p, sizeof(double), cudaMemcpyDeviceToHost));
+            last_refine = std::sqrt(rn / std::max(bn, 1e-300));
+            diag_left--;
+        }
+    }
+    double last_refine = 0.0;
+};
+
+template <typename Tv>
+struct EigOut {
+    std::vector<double> lam;
+    DVec<Tv> X;                 // n x ne
+    int ne = 0, restarts = 0;
+    bool converged = false;
+};
+
+template <typename Tv> Tv rnd_entry(std::mt19937& g, std::normal_distribution<double>& d);
+template <> double rnd_entry<double>(std::mt19937& g, std::normal_distribution<double>& d) { return d(g); }
+template <> zd rnd_entry<zd>(std::mt19937& g, std::normal_distribution<double>& d) {
+    const double a = d(g);
+    const double b = d(g);
+    return zd{a, b};
+}
+
+// Shift-invert Lanczos (src/hermitian_lanczos.cpp:264-460) with device-resident basis and
+// scalars; the host only reads the converged count after each restart cycle.
+template <typename Tv, typename Tf>
+EigOut<Tv> lanczos(tmg_context* c, ShiftInvert<Tv, Tf>& op, const DevCsr<Tv>& M, int nev, int ncv, double shift,
+                   double tol, int max_restarts) {
+    const int64_t n = op.n;
+    cudaStream_t st = c->st;
+    DVec<Tv> V, MV, w, Mw, h, dot, part;
+    V.alloc((size_t)(ncv + 1) * n); MV.alloc((size_t)(ncv + 1) * n);
+    V.zero(st); MV.zero(st);
+    w.alloc(n); Mw.alloc(n); h.alloc(ncv + 1); dot.alloc(1); part.alloc((size_t)LZ_DOT_BLOCKS * (ncv + 1));
+    DVec<double> alpha, beta, theta, lam, S, Z, Q, rot;
+    alpha.alloc(ncv); beta.alloc(ncv); theta.alloc(ncv); lam.alloc(ncv);
+    S.alloc((size_t)ncv * ncv); Z.alloc((size_t)ncv * ncv); Q.alloc((size_t)ncv * ncv);
+    rot.alloc((size_t)2 * std::max(1, ncv - nev) * std::max(1, ncv - 1));
+    alpha.zero(st); beta.zero(st);
+    DVec<int> order, nconv, flag;
+    order.alloc(ncv); nconv.alloc(1); flag.alloc(1);
+    flag.zero(st);
+    {
+        std::mt19937 gen(42);
+        std::normal_distribution<double> dist(0.0, 1.0);
+        std::vector<Tv> v0(n);
+        for (int64_t i = 0; i < n; i++) v0[i] = rnd_entry<Tv>(gen, dist);
+        TMG_CUDA(cudaMemcpy(V.p, v0.data(), n * sizeof(Tv), cudaMemcpyHostToDevice));
+        lz_spmv<Tv>(st, M, V.p, MV.p, 1, n);
+        lz_multidot<Tv>(st, n, V.p, n, 1, MV.p, part.p, dot.p);
+        lz_scale_cols<Tv>(st, n, dot.p, V.p, MV.p);
+    }
+    EigOut<Tv> out;
+    int m = ncv;
+    for (int restart = 0; restart <= max_restarts; restart++) {
+        const int j0 = restart == 0 ? 0 : nev;
+        for (int j = j0; j < m; j++) {
+            Tv* Vj = V.p + (int64_t)j * n;
+            Tv* MVj = MV.p + (int64_t)j * n;
+            op.apply(MVj, w.p);
+            lz_multidot<Tv>(st, n, MVj, n, 1, w.p, part.p, dot.p);
+            lz_three_term_dot<Tv>(st, n, j, dot.p, alpha.p, beta.p, V.p, w.p);
+            lz_multidot<Tv>(st, n, MV.p, n, j + 1, w.p, part.p, h.p);
+            lz_gemv_sub<Tv>(st, n, j + 1, V.p, h.p, w.p);
+            lz_spmv<Tv>(st, M, w.p, Mw.p, 1, n);
+            lz_multidot<Tv>(st, n, w.p, n, 1, Mw.p, part.p, dot.p);
+            lz_beta_scale<Tv>(st, n, j, dot.p, w.p, Mw.p, V.p, MV.p, beta.p, flag.p);
+            (void)Vj;
+        }
+        int hflag = 0;
+        TMG_CUDA(cudaMemcpyAsync(&hflag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TMG_CUDA(cudaStreamSynchronize(st));
+        if (hflag) throw numeric_error("Lanczos breakdown (beta < 1e-14) at step " + std::to_string(hflag - 1));
+        lz_tridiag(st, m, nev, shift, tol, alpha.p, beta.p, theta.p, S.p, lam.p, order.p, nconv.p, Z.p);
+        int hn = 0;
+        TMG_CUDA(cudaMemcpyAsync(&hn, nconv.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TMG_CUDA(cudaStreamSynchronize(st));
+        out.restarts = restart;
+        if (hn >= nev || restart == max_restarts) {
+            int ne = std::min(hn > 0 ? hn : nev, m);
+            ne = std::min(ne, nev);
+            std::vector<double> Sh = S.download(), lh = lam.download();
+            std::vector<int> oh = order.download();
+            std::vector<double> Csel((size_t)m * ne);
+            out.lam.resize(ne);
+            for (int t = 0; t < ne; t++) {
+                out.lam[t] = lh[oh[t]];
+                for (int k = 0; k < m; k++) Csel[(size_t)t * m + k] = Sh[(size_t)oh[t] * m + k];
+            }
+            DVec<double> dC;
+            dC.upload(Csel);
+            out.X.alloc((size_t)n * std::max(ne, 1));
+            lz_gemm_real<Tv>(st, n, m, ne, V.p, dC.p, m, out.X.p);
+            TMG_CUDA(cudaStreamSynchronize(st));
+            out.ne = ne;
+            out.converged = hn >= nev;
+            return out;
+        }
+        // implicit restart (src/hermitian_lanczos.cpp:114-260)
+        lz_restart_qr(st, m, nev, theta.p, alpha.p, beta.p, Q.p, rot.p);
+        DVec<Tv> Y;
+        Y.alloc((size_t)n * (nev + 1));
+        lz_gemm_real<Tv>(st, n, m, nev + 1, V.p, Q.p, m, Y.p);
+        lz_combine_f<Tv>(st, n, Y.p + (int64_t)nev * n, V.p + (int64_t)m * n, beta.p, nev, m, Q.p, w.p);
+        lz_copy<Tv>(st, (int64_t)nev * n, Y.p, V.p);
+        lz_spmv<Tv>(st, M, w.p, Mw.p, 1, n);
+        lz_multidot<Tv>(st, n, w.p, n, 1, Mw.p, part.p, dot.p);
+        TMG_LAUNCH(k_restart_norm<Tv>, nblk(n), 256, 0, st, n, nev, dot.p, w.p, Mw.p, V.p, MV.p, beta.p);
+        lz_spmv<Tv>(st, M, V.p, MV.p, nev, n);
+        TMG_CHECK_LAUNCH();
+    }
+    return out;
+}
+
+}  // namespace
+
+namespace {
+
+struct CsrHost {
+    DVec<int64_t> rp;
+    DVec<int32_t> ci;
+    DVec<int64_t> perm;     // CSR position -> CSC entry of the source values
+};
+
+void csr_of(const Pattern& P, CsrHost& out) {
+    std::vector<int64_t> map;
+    Pattern t = transpose_map(P, map);
+    out.rp.upload(t.p);
+    out.ci.upload(t.i);
+    out.perm.upload(map);
+}
+
+template <typename Tv>
+void finish_result(tmg_context* c, ResultHost& R, EigOut<Tv>& eo, ShiftInvert<Tv, Tv>* dummy, const DevCsr<Tv>& A,
+                   const DevCsr<Tv>& M, double shift, int nev_target, int num_modes, double min_frequency,
+                   bool is_degenerate, zd P) {
+    (void)dummy;
+    Sector& S = *c->sec;
+    cudaStream_t st = c->st;
+    const int64_t n = S.n_free;
+    std::vector<int> keep;
+    for (int t = 0; t < eo.ne; t++) {
+        const double lam = eo.lam[t];
+        const double f = lam > 0.0 ? std::sqrt(lam) / (2.0 * PI) : 0.0;
+        if (min_frequency > 0.0 && !(f > min_frequency)) continue;
+        keep.push_back(t);
+    }
+    if (min_frequency > 0.0 && keep.empty()) { R.status = TMG_ERR_NUMERIC; R.freqs.clear(); return; }
+    if ((int)keep.size() > nev_target) keep.resize(nev_target);
+    const int nk = (int)keep.size();
+    DVec<Tv> Xk;
+    Xk.alloc((size_t)n * std::max(nk, 1));
+    std::vector<double> lam(nk);
+    for (int t = 0; t < nk; t++) {
+        lam[t] = eo.lam[keep[t]];
+        lz_copy<Tv>(st, n, eo.X.p + (int64_t)keep[t] * n, Xk.p + (int64_t)t * n);
+        R.freqs.push_back(lam[t] > 0.0 ? std::sqrt(lam[t]) / (2.0 * PI) : 0.0);
+    }
+    // residual diagnostic ||K x - lambda M x|| / ||K x|| (cyclic_solver.cpp:1099-1114)
+    if (nk > 0) {
+        DVec<Tv> AX, MX, KX, RR;
+        DVec<double> dl, np, nr;
+        AX.alloc((size_t)n * nk); MX.alloc((size_t)n * nk); KX.alloc((size_t)n * nk); RR.alloc((size_t)n * nk);
+        dl.upload(lam);
+        np.alloc(LZ_DOT_BLOCKS); nr.alloc(2);
+        lz_spmv<Tv>(st, A, Xk.p, AX.p, nk, n);
+        lz_spmv<Tv>(st, M, Xk.p, MX.p, nk, n);
+        TMG_LAUNCH(k_resid<Tv>, dim3(nblk(n), nk), 256, 0, st, n, nk, AX.p, MX.p, dl.p, shift, KX.p, RR.p);
+        for (int t = 0; t < nk; t++) {
+            double a = 0, b = 0;
+            lz_norm2<Tv>(st, n, RR.p + (int64_t)t * n, np.p, nr.p);
+            TMG_CUDA(cudaMemcpy(&a, nr.p, sizeof(double), cudaMemcpyDeviceToHost));
+            lz_norm2<Tv>(st, n, KX.p + (int64_t)t * n, np.p, nr.p);
+            TMG_CUDA(cudaMemcpy(&b, nr.p, sizeof(double), cudaMemcpyDeviceToHost));
+            const double res = b > 0 ? std::sqrt(a / b) : std::sqrt(a);
+            R.max_residual = std::max(R.max_residual, res);
+        }
+    }
+    // complex free-space modes
+    DVec<zd> Xc;
+    Xc.alloc((size_t)n * std::max(nk, 1));
+    if constexpr (std::is_same<Tv, double>::value) {
+        if (nk) TMG_LAUNCH(k_real_to_complex, nblk(n * nk), 256, 0, st, n * nk, Xk.p, Xc.p);
+    } else {
+        if (nk) lz_copy<zd>(st, n * nk, Xk.p, Xc.p);
+    }
+    int nm = nk;
+    R.whirl.assign(nk, 0);
+    DVec<zd> Xd;
+    const zd* Xsrc = Xc.p;
+    if (is_degenerate && nk > 0) {
+        nm = std::min(2 * nk, num_modes);
+        Xd.alloc((size_t)n * nm);
+        TMG_LAUNCH(k_dup_conj, dim3(nblk(n), nm), 256, 0, st, n, nm, Xc.p, Xd.p);
+        std::vector<double> f2(nm);
+        R.whirl.assign(nm, 0);
+        for (int q = 0; q < nm; q++) { f2[q] = R.freqs[q / 2]; R.whirl[q] = (q % 2 == 0) ? 1 : -1; }
+        R.freqs = f2;
+        Xsrc = Xd.p;
+    }
+    // expansion to the full sector DOFs (cyclic_solver.cpp:1185-1211)
+    const int32_t ndof = 3 * S.nn;
+    DVec<zd> full;
+    full.alloc((size_t)ndof * std::max(nm, 1));
+    DVec<int64_t> rp;
+    DVec<int32_t> ci, r2f;
+    DVec<double> tv;
+    DVec<uint8_t> isr;
+    rp.upload(S.T0t.p); ci.upload(S.T0t.i); tv.upload(S.T0tv); isr.upload(S.is_right); r2f.upload(S.r2free);
+    if (nm) TMG_LAUNCH(k_expand, dim3(nblk(ndof), nm), 256, 0, st, ndof, rp.p, ci.p, tv.p, isr.p, r2f.p, Xsrc, n, P,
+                       full.p, (int64_t)ndof);
+    TMG_CHECK_LAUNCH();
+    R.shapes.resize((size_t)ndof * nm);
+    if (nm) TMG_CUDA(cudaMemcpy(R.shapes.data(), full.p, R.shapes.size() * sizeof(zd), cudaMemcpyDeviceToHost));
+}
+
+template <typename Tv, typename Tf>
+void run_problem(tmg_context* c, ResultHost& R, const OpSymbolic& os, const UnionMaps& um, const Tv* vals_csc,
+                 const DevCsr<Tv>& M, int nev, int ncv, double shift, int max_restarts, bool mixed, int nev_target,
+                 int num_modes, double min_frequency, bool is_degenerate, zd P) {
+    cudaStream_t st = c->st;
+    const int64_t nl = (int64_t)um.lower2csc.n;
+    DVec<Tv> lower, acsr;
+    lower.alloc(nl);
+    acsr.alloc(um.U.nnz());
+    if (nl) TMG_LAUNCH(k_gather_t<Tv>, nblk(nl), 256, 0, st, nl, um.lower2csc.p, vals_csc, lower.p);
+    if (um.U.nnz()) TMG_LAUNCH(k_gather_t<Tv>, nblk(um.U.nnz()), 256, 0, st, um.U.nnz(), um.csr2csc.p, vals_csc, acsr.p);
+    DevCsr<Tv> A;
+    A.nrows = um.U.ncols; A.nnz = um.U.nnz(); A.rowptr = um.csr_rowptr.p; A.col = um.csr_col.p; A.val = acsr.p;
+    ShiftInvert<Tv, Tf> op;
+    op.c = c; op.D = &os.D; op.n = um.U.ncols; op.mixed = mixed; op.A = A;
+    auto t0 = std::chrono::steady_clock::now();
+    op.factor(lower.p, nl);
+    auto t1 = std::chrono::steady_clock::now();
+    EigOut<Tv> eo = lanczos<Tv, Tf>(c, op, M, nev, ncv, shift, 1e-8, max_restarts);
+    auto t2 = std::chrono::steady_clock::now();
+    c->phase_ms[1] += std::chrono::duration<double, std::milli>(t1 - t0).count();
+    c->phase_ms[2] += std::chrono::duration<double, std::milli>(t2 - t1).count();
+    R.converged = eo.converged;
+    R.iterations = eo.restarts;
+    R.refine_residual = op.worst_refine > 0 ? std::max(op.worst_refine, op.last_refine) : op.last_refine;
+    if (!eo.converged && eo.ne == 0) { R.status = TMG_ERR_NUMERIC; return; }
+    finish_result<Tv>(c, R, eo, nullptr, A, M, shift, nev_target, num_modes, min_frequency, is_degenerate, P);
+    auto t3 = std::chrono::steady_clock::now();
+    c->phase_ms[3] += std::chrono::duration<double, std::milli>(t3 - t2).count();
+}
+
+ResultHost solve_harmonic(tmg_context* c, int k, int num_modes, double min_frequency, int precision) {
+    Sector& S = *c->sec;
+    cudaStream_t st = c->st;
+    ResultHost R;
+    R.k = k;
+    R.rpm = c->rpm;
+    const int N = S.ns, max_k = N / 2;
+    const double alpha = 2.0 * PI / N;
+    const zd P{std::cos(k * alpha), std::sin(k * alpha)};
+    if (S.n_free <= 1) { R.status = TMG_ERR_ARG; return R; }
+    const bool is_degenerate = (k > 0) && !(N % 2 == 0 && k == max_k);
+    const bool will_qep = c->coriolis && k > 0;
+    if (will_qep) { R.status = TMG_ERR_STATE; return R; }
+    const int nev_target = is_degenerate ? (num_modes + 1) / 2 : num_modes;
+    const int n_extra = min_frequency > 0.0 ? 6 : 0;
+    int nev = std::min(nev_target + n_extra, S.n_free - 1);
+    if (nev <= 0) { R.status = TMG_ERR_ARG; return R; }
+    int ncv = std::min(std::max(4 * nev + 1, 40), S.n_free);
+    const double shift = 1.0;
+    const bool is_real = (k == 0) || (N % 2 == 0 && k == max_k);
+    const bool mixed = precision == TMG_PREC_MIXED;
+    if (S.n_free <= 200) { R.status = TMG_ERR_ARG; return R; }
+    nev = std::min(nev, S.n_free - 1);
+    ncv = std::min(ncv, S.n_free);
+    if (is_real) {
+        auto& RO = c->real[k == 0 ? 0 : 1];
+        if (!RO.valid) { R.status = TMG_ERR_STATE; return R; }
+        if (!RO.sym.valid) analyze_op(RO.sym, RO.op);
+        DVec<double> vals;
+        vals.alloc(RO.op.U.nnz());
+        if (vals.n)
+            TMG_LAUNCH(k_form_real_op, nblk(vals.n), 256, 0, st, (int64_t)vals.n, RO.op.maps[0].p, RO.op.maps[1].p,
+                       RO.Kr.v.p, RO.Mr.v.p, shift, 1.0, vals.p);
+        CsrHost mc;
+        csr_of(RO.Mr.pat, mc);
+        DVec<double> mv;
+        mv.alloc(RO.Mr.pat.nnz());
+        if (mv.n) TMG_LAUNCH(k_gather_t<double>, nblk(mv.n), 256, 0, st, (int64_t)mv.n, mc.perm.p, RO.Mr.v.p, mv.p);
+        DevCsr<double> M;
+        M.nrows = S.n_free; M.nnz = mv.n; M.rowptr = mc.rp.p; M.col = mc.ci.p; M.val = mv.p;
+        if (mixed)
+            run_problem<double, float>(c, R, RO.sym, RO.op, vals.p, M, nev, ncv, shift, 1000, true, nev_target,
+                                       num_modes, min_frequency, false, P);
+        else
+            run_problem<double, double>(c, R, RO.sym, RO.op, vals.p, M, nev, ncv, shift, 1000, false, nev_target,
+                                        num_modes, min_frequency, false, P);
+    } else {
+        if (!c->symC.valid) analyze_op(c->symC, c->opC);
+        UnionMaps& um = c->opC;
+        DVec<zd> vals;
+        vals.alloc(um.U.nnz());
+        if (vals.n)
+            TMG_LAUNCH(k_form_complex, nblk(vals.n), 256, 0, st, (int64_t)vals.n, um.maps[0].p, um.maps[1].p,
+                       um.maps[2].p, um.maps[3].p, um.maps[4].p, um.maps[5].p, c->Kcf.v.p, c->Kpf.v.p, c->Mcf.v.p,
+                       c->Mpf.v.p, P.x, P.y, shift, 1.0, vals.p);
+        UnionMaps& mu = c->opMC;
+        DVec<zd> mvals, mcsr;
+        mvals.alloc(mu.U.nnz());
+        mcsr.alloc(mu.U.nnz());
+        if (mvals.n) {
+            TMG_LAUNCH(k_form_csum, nblk(mvals.n), 256, 0, st, (int64_t)mvals.n, mu.maps[0].p, mu.maps[1].p,
+                       mu.maps[2].p, c->Mcf.v.p, c->Mpf.v.p, P.x, P.y, mvals.p);
+            TMG_LAUNCH(k_gather_t<zd>, nblk(mvals.n), 256, 0, st, (int64_t)mvals.n, mu.csr2csc.p, mvals.p, mcsr.p);
+        }
+        DevCsr<zd> M;
+        M.nrows = S.n_free; M.nnz = mcsr.n; M.rowptr = mu.csr_rowptr.p; M.col = mu.csr_col.p; M.val = mcsr.p;
+        if (mixed)
+            run_problem<zd, zf>(c, R, c->symC, um, vals.p, M, nev, ncv, shift, 1000, true, nev_target, num_modes,
+                                min_frequency, is_degenerate, P);
+        else
+            run_problem<zd, zd>(c, R, c->symC, um, vals.p, M, nev, ncv, shift, 1000, false, nev_target, num_modes,
+                                min_frequency, is_degenerate, P);
+    }
+    TMG_CUDA(cudaStreamSynchronize(st));
+    return R;
+}
+
+int copy_csc(const Pattern& P, const double* dvals_or_null, const std::vector<double>* hvals, int64_t* nnz,
+             int32_t* colptr, int32_t* rowidx, double* values, bool complex_out) {
+    *nnz = P.nnz();
+    if (!colptr) return TMG_OK;
+    for (int32_t j = 0; j <= P.ncols; j++) colptr[j] = (int32_t)P.p[j];
+    if (rowidx) std::copy(P.i.begin(), P.i.end(), rowidx);
+    if (values) {
+        std::vector<double> v;
+        if (hvals) v = *hvals;
+        else {
+            v.resize(P.nnz());
+            if (P.nnz()) TMG_CUDA(cudaMemcpy(v.data(), dvals_or_null, v.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        }
+        if (complex_out)
+            for (int64_t q = 0; q < P.nnz(); q++) { values[2 * q] = v[q]; values[2 * q + 1] = 0.0; }
+        else
+            std::copy(v.begin(), v.end(), values);
+    }
+    return TMG_OK;
+}
+
+}  // namespace
+
+// =====================================================================================
+// C ABI
+// =====================================================================================
+extern "C" {
+
+int tmg_create(int device, size_t mem_budget_bytes, tmg_context** out) {
+    if (!out) return TMG_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return TMG_ERR_CUDA;
+    auto* c = new tmg_context();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreate(&c->st) != cudaSuccess) {
+        delete c;
+        return TMG_ERR_CUDA;
+    }
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    c->budget = mem_budget_bytes ? mem_budget_bytes : (size_t)(0.9 * fr);
+    *out = c;
+    return TMG_OK;
+}
+
+int tmg_destroy(tmg_context* c) {
+    if (!c) return TMG_ERR_ARG;
+    cudaSetDevice(c->device);
+    cudaStream_t st = c->st;
+    delete c;
+    if (st) cudaStreamDestroy(st);
+    return TMG_OK;
+}
+
+const char* tmg_last_error(const tmg_context* c) { return c ? c->err.c_str() : "null context"; }
+
+int tmg_upload_sector(tmg_context* c, const tmg_sector_desc* d) {
+    if (!c || !d) return TMG_ERR_ARG;
+    return guarded(c, [&]() { setup_sector(c, d); return TMG_OK; });
+}
+
+int tmg_assemble(tmg_context* c, int which, double rpm, int64_t* nnz, int32_t* colptr, int32_t* rowidx, double* values) {
+    if (!c || !nnz) return TMG_ERR_ARG;
+    if (!c->sec) return set_err(c, TMG_ERR_STATE, "no sector uploaded");
+    return guarded(c, [&]() {
+        Sector& S = *c->sec;
+        const double omega = rpm * 2.0 * PI / 60.0;
+        const CandMat* m = nullptr;
+        switch (which) {
+            case TMG_MAT_K: assemble_KM(c); m = &c->K; break;
+            case TMG_MAT_M: assemble_KM(c); m = &c->M; break;
+            case TMG_MAT_KOMEGA: assemble_rot(c, omega); m = &c->Kw; break;
+            case TMG_MAT_G: assemble_rot(c, omega); m = &c->G; break;
+            case TMG_MAT_KSIGMA:
+                if (!c->prepared || c->rpm != rpm) prepare(c, rpm, false);
+                if (std::fabs(omega) == 0.0 || S.hub.empty()) return set_err(c, TMG_ERR_STATE, "no stress stiffening at this speed");
+                m = &c->Ks; break;
+            case TMG_MAT_KEFF:
+                if (!c->prepared || c->rpm != rpm) prepare(c, rpm, false);
+                m = &c->Keff; break;
+            default: return set_err(c, TMG_ERR_ARG, "unknown matrix selector");
+        }
+        TMG_CUDA(cudaStreamSynchronize(c->st));
+        Flagged f = flagged(S.cand, m->f.download());
+        *nnz = f.pat.nnz();
+        if (!colptr) return TMG_OK;
+        std::vector<double> cv = m->v.download(), v(f.cand.size());
+        for (size_t q = 0; q < f.cand.size(); q++) v[q] = cv[f.cand[q]];
+        return copy_csc(f.pat, nullptr, &v, nnz, colptr, rowidx, values, false);
+    });
+}
+
+int tmg_prepare(tmg_context* c, double rpm, int coriolis) {
+    if (!c) return TMG_ERR_ARG;
+    if (!c->sec) return set_err(c, TMG_ERR_STATE, "no sector uploaded");
+    return guarded(c, [&]() { prepare(c, rpm, coriolis != 0); return TMG_OK; });
+}
+
+int tmg_projection(tmg_context* c, int which, int k, int64_t* nnz, int32_t* n, int32_t* colptr, int32_t* rowidx,
+                   double* values) {
+    if (!c || !nnz) return TMG_ERR_ARG;
+    if (!c->prepared) return set_err(c, TMG_ERR_STATE, "call tmg_prepare first");
+    return guarded(c, [&]() {
+        Sector& S = *c->sec;
+        if (n) *n = S.n_free;
+        const FreeMat* fm = nullptr;
+        bool cplx = true;
+        switch (which) {
+            case TMG_MAT_KCF: fm = &c->Kcf; break;
+            case TMG_MAT_KPF: fm = &c->Kpf; break;
+            case TMG_MAT_MCF: fm = &c->Mcf; break;
+            case TMG_MAT_MPF: fm = &c->Mpf; break;
+            case TMG_MAT_GCF: fm = &c->Gcf; break;
+            case TMG_MAT_GPF: fm = &c->Gpf; break;
+            case TMG_MAT_K0R: fm = &c->real[0].Kr; cplx = false; break;
+            case TMG_MAT_M0R: fm = &c->real[0].Mr; cplx = false; break;
+            case TMG_MAT_KHR: fm = &c->real[1].Kr; cplx = false; break;
+            case TMG_MAT_MHR: fm = &c->real[1].Mr; cplx = false; break;
+            case TMG_MAT_KK:
+            case TMG_MAT_MK: {
+                UnionMaps& w = which == TMG_MAT_KK ? c->W0 : c->WM0;
+                const FreeMat& cc = which == TMG_MAT_KK ? c->Kcf : c->Mcf;
+                const FreeMat& pp = which == TMG_MAT_KK ? c->Kpf : c->Mpf;
+                const double alpha = 2.0 * PI / S.ns;
+                DVec<zd> v;
+                v.alloc(w.U.nnz());
+                if (v.n)
+                    TMG_LAUNCH(k_form_csum, nblk(v.n), 256, 0, c->st, (int64_t)v.n, w.maps[0].p, w.maps[1].p,
+                               w.maps[2].p, cc.v.p, pp.v.p, std::cos(k * alpha), std::sin(k * alpha), v.p);
+                TMG_CUDA(cudaStreamSynchronize(c->st));
+                *nnz = w.U.nnz();
+                if (!colptr) return TMG_OK;
+                for (int32_t j = 0; j <= w.U.ncols; j++) colptr[j] = (int32_t)w.U.p[j];
+                if (rowidx) std::copy(w.U.i.begin(), w.U.i.end(), rowidx);
+                if (values && v.n) TMG_CUDA(cudaMemcpy(values, v.p, v.n * sizeof(zd), cudaMemcpyDeviceToHost));
+                return TMG_OK;
+            }
+            default: return set_err(c, TMG_ERR_ARG, "unknown projection selector");
+        }
+        TMG_CUDA(cudaStreamSynchronize(c->st));
+        return copy_csc(fm->pat, fm->v.p, nullptr, nnz, colptr, rowidx, values, cplx);
+    });
+}
+
+int tmg_symbolic(tmg_context* c, int kind, int32_t* n, int32_t* perm, int32_t* parent, int32_t* colcount) {
+    if (!c || !n) return TMG_ERR_ARG;
+    if (!c->prepared) return set_err(c, TMG_ERR_STATE, "call tmg_prepare first");
+    return guarded(c, [&]() {
+        OpSymbolic* os = nullptr;
+        if (kind == 0) {
+            if (!c->symC.valid) analyze_op(c->symC, c->opC);
+            os = &c->symC;
+        } else if (kind == 1 || kind == 2) {
+            auto& RO = c->real[kind - 1];
+            if (!RO.valid) return set_err(c, TMG_ERR_STATE, "no such real harmonic");
+            if (!RO.sym.valid) analyze_op(RO.sym, RO.op);
+            os = &RO.sym;
+        } else {
+            return set_err(c, TMG_ERR_ARG, "unknown symbolic kind");
+        }
+        *n = os->S.n;
+        if (perm) std::copy(os->S.amd.begin(), os->S.amd.end(), perm);
+        if (parent) std::copy(os->S.etree.begin(), os->S.etree.end(), parent);
+        if (colcount) std::copy(os->S.colcount.begin(), os->S.colcount.end(), colcount);
+        return TMG_OK;
+    });
+}
+
+int tmg_solve_at_rpm(tmg_context* c, double rpm, int num_modes, const int32_t* harmonics, int nh, int coriolis,
+                     double min_frequency, int precision, int32_t* num_results) {
+    if (!c || !num_results) return TMG_ERR_ARG;
+    if (!c->sec) return set_err(c, TMG_ERR_STATE, "no sector uploaded");
+    if (num_modes <= 0) return set_err(c, TMG_ERR_ARG, "num_modes must be positive");
+    return guarded(c, [&]() {
+        for (double& p : c->phase_ms) p = 0.0;
+        const int64_t l0 = g_kernel_launches;
+        const bool cor = coriolis != 0;
+        if (!c->prepared || c->rpm != rpm || c->coriolis != (cor && rpm != 0.0)) prepare(c, rpm, cor);
+        Sector& S = *c->sec;
+        const int max_k = S.ns / 2;
+        std::vector<int> hs;
+        if (!harmonics || nh == 0) for (int k = 0; k <= max_k; k++) hs.push_back(k);
+        else for (int q = 0; q < nh; q++) if (harmonics[q] >= 0 && harmonics[q] <= max_k) hs.push_back(harmonics[q]);
+        c->results.clear();
+        std::string firsterr;
+        for (int k : hs) {
+            ResultHost R;
+            try {
+                R = solve_harmonic(c, k, num_modes, min_frequency, precision);
+            } catch (const numeric_error& e) {
+                R.k = k; R.rpm = rpm; R.status = TMG_ERR_NUMERIC;
+                if (firsterr.empty()) firsterr = e.what();
+            }
+            c->results.push_back(std::move(R));
+        }
+        std::sort(c->results.begin(), c->results.end(), [](const ResultHost& a, const ResultHost& b) { return a.k < b.k; });
+        *num_results = (int32_t)c->results.size();
+        c->launches = g_kernel_launches - l0;
+        if (!firsterr.empty()) c->err = firsterr;
+        return TMG_OK;
+    });
+}
+
+int tmg_result_info(tmg_context* c, int idx, tmg_result_meta* info) {
+    if (!c || !info || idx < 0 || idx >= (int)c->results.size()) return TMG_ERR_ARG;
+    const ResultHost& R = c->results[idx];
+    info->harmonic_index = R.k;
+    info->num_modes = (int32_t)R.freqs.size();
+    info->converged = R.converged;
+    info->iterations = R.iterations;
+    info->status = R.status;
+    info->rpm = R.rpm;
+    info->max_residual = R.max_residual;
+    info->refine_residual = R.refine_residual;
+    return TMG_OK;
+}
+
+int tmg_result_copy(tmg_context* c, int idx, double* freqs, double* shapes, int32_t* whirl) {
+    if (!c || idx < 0 || idx >= (int)c->results.size()) return TMG_ERR_ARG;
+    const ResultHost& R = c->results[idx];
+    if (freqs) std::copy(R.freqs.begin(), R.freqs.end(), freqs);
+    if (whirl) std::copy(R.whirl.begin(), R.whirl.end(), whirl);
+    if (shapes && !R.shapes.empty()) std::memcpy(shapes, R.shapes.data(), R.shapes.size() * sizeof(zd));
+    return TMG_OK;
+}
+
+int tmg_last_timing(tmg_context* c, double* phase_ms, int nphase, int64_t* kernel_launches) {
+    if (!c) return TMG_ERR_ARG;
+    for (int q = 0; q < nphase && q < 8; q++) phase_ms[q] = c->phase_ms[q];
+    if (kernel_launches) *kernel_launches = c->launches;
+    return TMG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,517 @@
+// Supernodal multifrontal LDL^H (no pivoting, D real) and its triangular solves.
+//
+// Fronts are dense m x m column-major blocks (lower triangle used).  The tree is processed
+// level by level (leaves first).  For every level: children's update blocks are added into
+// their parents (one launch per child rank, so no two writers touch the same entry and the
+// sums run in a fixed order), then each front is partially factorised by 32-wide pivot
+// blocks: diagonal block (one CTA per front), panel rows (CTA per 64 rows), and the Schur
+// update of the trailing lower triangle (CTA per 64x64 tile).  The reference factorises
+// the same operator with Eigen's simplicial up-looking LDL^T (src/hermitian_lanczos.cpp:
+// 12-56); the supernodal form has the same L and D in exact arithmetic.
+#include <algorithm>
+
+#include "mf.cuh"
+
+namespace tmg {
+
+int64_t g_kernel_launches = 0;
+
+template <typename T>
+__device__ __forceinline__ T dev_div(T a, typename real_of<T>::type d) { return a / d; }
+template <>
+__device__ __forceinline__ double dev_div<double>(double a, double d) { return a / d; }
+template <>
+__device__ __forceinline__ float dev_div<float>(float a, float d) { return a / d; }
+
+template <typename T>
+__device__ __forceinline__ T mulc(T a, T b) { return a * conj(b); }   // a * conj(b)
+
+// ------------------------------------------------------------------------------------
+template <typename T>
+__global__ void k_scatter(int64_t n, const T* __restrict__ vals, const int64_t* __restrict__ dest,
+                          const uint8_t* __restrict__ cj, T* __restrict__ F) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int64_t d = dest[q];
+    if (d < 0) return;
+    const T v = vals[q];
+    F[d] = cj[q] ? conj(v) : v;
+}
+
+template <typename T>
+__global__ void k_extend_add(const int32_t* __restrict__ items, int nitems, const int32_t* __restrict__ sn_first,
+                             const int64_t* __restrict__ sn_row_ptr, const int64_t* __restrict__ front_off,
+                             const int64_t* __restrict__ rel_ptr, const int32_t* __restrict__ rel, T* __restrict__ F) {
+    for (int it = blockIdx.y; it < nitems; it += gridDim.y) {
+        const int p = items[2 * it], c = items[2 * it + 1];
+        const int64_t mc = sn_row_ptr[c + 1] - sn_row_ptr[c];
+        const int64_t wc = sn_first[c + 1] - sn_first[c];
+        const int64_t u = mc - wc;
+        const int64_t mp = sn_row_ptr[p + 1] - sn_row_ptr[p];
+        const int32_t* rl = rel + rel_ptr[c];
+        const T* Fc = F + front_off[c];
+        T* Fp = F + front_off[p];
+        for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < u * u;
+             idx += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t a = idx % u, b = idx / u;
+            if (a < b) continue;
+            Fp[(int64_t)rl[b] * mp + rl[a]] += Fc[(wc + b) * mc + wc + a];
+        }
+    }
+}
+
+// Factor the 32x32 diagonal block of pivot block kb of every listed front.
+template <typename T>
+__global__ void __launch_bounds__(256) k_diag(const int32_t* __restrict__ items, int kb,
+                                              const int32_t* __restrict__ sn_first, const int64_t* __restrict__ sn_row_ptr,
+                                              const int64_t* __restrict__ front_off, T* __restrict__ F,
+                                              int* __restrict__ status) {
+    using R = typename real_of<T>::type;
+    __shared__ T A[MF_NB][MF_NB + 1];
+    const int s = items[blockIdx.x];
+    const int64_t m = sn_row_ptr[s + 1] - sn_row_ptr[s];
+    const int w = sn_first[s + 1] - sn_first[s];
+    const int k0 = kb * MF_NB;
+    const int nb = min(MF_NB, w - k0);
+    T* Fs = F + front_off[s];
+    for (int q = threadIdx.x; q < MF_NB * MF_NB; q += blockDim.x) {
+        const int i = q % MF_NB, j = q / MF_NB;
+        if (i < nb && j <= i) A[i][j] = Fs[(int64_t)(k0 + j) * m + k0 + i];
+    }
+    __syncthreads();
+    for (int j = 0; j < nb; j++) {
+        const R d = re(A[j][j]);
+        if (d == R(0)) {
+            if (threadIdx.x == 0) atomicCAS(status, 0, sn_first[s] + k0 + j + 1);
+            return;
+        }
+        // trailing update of the block: A(i,k) -= A(i,j) conj(A(k,j)) / d, j < k <= i
+        const int t = nb - j - 1;
+        for (int q = threadIdx.x; q < t * t; q += blockDim.x) {
+            const int i = j + 1 + q % t, k = j + 1 + q / t;
+            if (k <= i) A[i][k] -= dev_div(mulc(A[i][j], A[k][j]), d);
+        }
+        __syncthreads();
+        for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) A[i][j] = dev_div(A[i][j], d);
+        if (threadIdx.x == 0) { T dd = zero_of<T>(); reinterpret_cast<R*>(&dd)[0] = d; A[j][j] = dd; }
+        __syncthreads();
+    }
+    for (int q = threadIdx.x; q < MF_NB * MF_NB; q += blockDim.x) {
+        const int i = q % MF_NB, j = q / MF_NB;
+        if (i < nb && j <= i) Fs[(int64_t)(k0 + j) * m + k0 + i] = A[i][j];
+    }
+}
+
+// Panel rows below the diagonal block: L(i, blk) = A(i, blk) (D L_kk^H)^-1
+template <typename T>
+__global__ void __launch_bounds__(64) k_panel(const int32_t* __restrict__ items, int kb,
+                                              const int32_t* __restrict__ sn_first, const int64_t* __restrict__ sn_row_ptr,
+                                              const int64_t* __restrict__ front_off, T* __restrict__ F) {
+    using R = typename real_of<T>::type;
+    __shared__ T Lk[MF_NB][MF_NB + 1];
+    __shared__ R dk[MF_NB];
+    const int s = items[2 * blockIdx.x];
+    const int r0 = items[2 * blockIdx.x + 1];
+    const int64_t m = sn_row_ptr[s + 1] - sn_row_ptr[s];
+    const int w = sn_first[s + 1] - sn_first[s];
+    const int k0 = kb * MF_NB;
+    const int nb = min(MF_NB, w - k0);
+    T* Fs = F + front_off[s];
+    for (int q = threadIdx.x; q < MF_NB * MF_NB; q += blockDim.x) {
+        const int i = q % MF_NB, j = q / MF_NB;
+        if (i < nb && j < i) Lk[i][j] = Fs[(int64_t)(k0 + j) * m + k0 + i];
+    }
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) dk[j] = re(Fs[(int64_t)(k0 + j) * m + k0 + j]);
+    __syncthreads();
+    const int64_t i = r0 + threadIdx.x;
+    if (i >= m) return;
+    T x[MF_NB];
+#pragma unroll
+    for (int j = 0; j < MF_NB; j++) x[j] = j < nb ? Fs[(int64_t)(k0 + j) * m + i] : zero_of<T>();
+#pragma unroll
+    for (int j = 0; j < MF_NB; j++) {
+        if (j < nb) {
+            T a = x[j];
+#pragma unroll
+            for (int l = 0; l < MF_NB; l++)
+                if (l < j) a -= (dk[l] * x[l]) * conj(Lk[j][l]);
+            x[j] = dev_div(a, dk[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < MF_NB; j++)
+        if (j < nb) Fs[(int64_t)(k0 + j) * m + i] = x[j];
+}
+
+// Trailing lower-triangle update: C(i,j) -= sum_l L(i,l) d_l conj(L(j,l)) over the pivot block
+template <typename T>
+__global__ void __launch_bounds__(256) k_update(const int32_t* __restrict__ items, int kb,
+                                                const int32_t* __restrict__ sn_first, const int64_t* __restrict__ sn_row_ptr,
+                                                const int64_t* __restrict__ front_off, T* __restrict__ F) {
+    using R = typename real_of<T>::type;
+    extern __shared__ unsigned char smem_raw[];
+    T* Li = reinterpret_cast<T*>(smem_raw);                  // [MF_NB][MF_TILE]
+    T* Lj = Li + MF_NB * MF_TILE;                            // [MF_NB][MF_TILE], scaled by d
+    const int s = items[3 * blockIdx.x];
+    const int ti = items[3 * blockIdx.x + 1], tj = items[3 * blockIdx.x + 2];
+    const int64_t m = sn_row_ptr[s + 1] - sn_row_ptr[s];
+    const int w = sn_first[s + 1] - sn_first[s];
+    const int k0 = kb * MF_NB;
+    const int nb = min(MF_NB, w - k0);
+    const int64_t t0 = k0 + nb;
+    const int64_t i0 = t0 + (int64_t)ti * MF_TILE, j0 = t0 + (int64_t)tj * MF_TILE;
+    T* Fs = F + front_off[s];
+    for (int q = threadIdx.x; q < MF_NB * MF_TILE; q += blockDim.x) {
+        const int r = q % MF_TILE, l = q / MF_TILE;
+        T a = zero_of<T>(), b = zero_of<T>();
+        if (l < nb) {
+            if (i0 + r < m) a = Fs[(int64_t)(k0 + l) * m + i0 + r];
+            if (j0 + r < m) {
+                const R d = re(Fs[(int64_t)(k0 + l) * m + k0 + l]);
+                b = d * Fs[(int64_t)(k0 + l) * m + j0 + r];
+            }
+        }
+        Li[l * MF_TILE + r] = a;
+        Lj[l * MF_TILE + r] = b;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    T acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc[a][b] = zero_of<T>();
+    for (int l = 0; l < nb; l++) {
+        T av[4], bv[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) av[a] = Li[l * MF_TILE + ty + 16 * a];
+#pragma unroll
+        for (int b = 0; b < 4; b++) bv[b] = conj(Lj[l * MF_TILE + tx + 16 * b]);
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) acc[a][b] += av[a] * bv[b];
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const int64_t i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
+            if (i < m && j < m && i >= j) Fs[j * m + i] -= acc[a][b];
+        }
+}
+
+// ------------------------------------------------------------------------------------
+// Triangular solves: one CTA per supernode, levels processed in order.  tbuf holds a
+// length-m vector per front; its tail [w, m) carries the front's update to its parent.
+template <typename T>
+__global__ void __launch_bounds__(256) k_fwd(const int32_t* __restrict__ lvl, const int32_t* __restrict__ sn_first,
+                                             const int64_t* __restrict__ sn_row_ptr, const int64_t* __restrict__ front_off,
+                                             const int32_t* __restrict__ child_ptr, const int32_t* __restrict__ child_list,
+                                             const int64_t* __restrict__ rel_ptr, const int32_t* __restrict__ rel,
+                                             const T* __restrict__ F, T* __restrict__ x, T* __restrict__ tbuf) {
+    using R = typename real_of<T>::type;
+    const int s = lvl[blockIdx.x];
+    const int f = sn_first[s];
+    const int w = sn_first[s + 1] - f;
+    const int64_t m = sn_row_ptr[s + 1] - sn_row_ptr[s];
+    const T* Fs = F + front_off[s];
+    T* t = tbuf + sn_row_ptr[s];
+    for (int64_t r = threadIdx.x; r < m; r += blockDim.x) t[r] = r < w ? x[f + r] : zero_of<T>();
+    __syncthreads();
+    for (int c = child_ptr[s]; c < child_ptr[s + 1]; c++) {
+        const int ch = child_list[c];
+        const int64_t mc = sn_row_ptr[ch + 1] - sn_row_ptr[ch];
+        const int wc = sn_first[ch + 1] - sn_first[ch];
+        const T* tc = tbuf + sn_row_ptr[ch] + wc;
+        const int32_t* rl = rel + rel_ptr[ch];
+        for (int64_t a = threadIdx.x; a < mc - wc; a += blockDim.x) t[rl[a]] += tc[a];
+        __syncthreads();
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int jb = 0; jb < w; jb += 32) {
+        const int nbb = min(32, w - jb);
+        if (warp == 0) {
+            T v = lane < nbb ? t[jb + lane] : zero_of<T>();
+            for (int j = 0; j < nbb; j++) {
+                T yj;
+                reinterpret_cast<R*>(&yj)[0] = __shfl_sync(0xffffffff, reinterpret_cast<R*>(&v)[0], j);
+                if constexpr (sizeof(T) == 2 * sizeof(R))
+                    reinterpret_cast<R*>(&yj)[1] = __shfl_sync(0xffffffff, reinterpret_cast<R*>(&v)[1], j);
+                if (lane > j && lane < nbb) v -= Fs[(int64_t)(jb + j) * m + jb + lane] * yj;
+            }
+            if (lane < nbb) t[jb + lane] = v;
+        }
+        __syncthreads();
+        for (int64_t r = jb + nbb + threadIdx.x; r < m; r += blockDim.x) {
+            T a = t[r];
+            for (int j = 0; j < nbb; j++) a -= Fs[(int64_t)(jb + j) * m + r] * t[jb + j];
+            t[r] = a;
+        }
+        __syncthreads();
+    }
+    for (int j = threadIdx.x; j < w; j += blockDim.x) x[f + j] = dev_div(t[j], re(Fs[(int64_t)j * m + j]));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_bwd(const int32_t* __restrict__ lvl, const int32_t* __restrict__ sn_first,
+                                             const int64_t* __restrict__ sn_row_ptr, const int32_t* __restrict__ sn_rows,
+                                             const int64_t* __restrict__ front_off, const T* __restrict__ F,
+                                             T* __restrict__ x, T* __restrict__ tbuf) {
+    using R = typename real_of<T>::type;
+    const int s = lvl[blockIdx.x];
+    const int f = sn_first[s];
+    const int w = sn_first[s + 1] - f;
+    const int64_t m = sn_row_ptr[s + 1] - sn_row_ptr[s];
+    const T* Fs = F + front_off[s];
+    const int32_t* rows = sn_rows + sn_row_ptr[s];
+    T* t = tbuf + sn_row_ptr[s];
+    for (int64_t r = threadIdx.x; r < m; r += blockDim.x) t[r] = r < w ? x[f + r] : x[rows[r]];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int last = ((w - 1) / 32) * 32;
+    for (int jb = last; jb >= 0; jb -= 32) {
+        const int nbb = min(32, w - jb);
+        for (int j = jb + warp; j < jb + nbb; j += nwarp) {
+            T a = zero_of<T>();
+            for (int64_t r = jb + nbb + lane; r < m; r += 32) a += conj(Fs[(int64_t)j * m + r]) * t[r];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                R* ap = reinterpret_cast<R*>(&a);
+                ap[0] += __shfl_xor_sync(0xffffffff, ap[0], o);
+                if constexpr (sizeof(T) == 2 * sizeof(R)) ap[1] += __shfl_xor_sync(0xffffffff, ap[1], o);
+            }
+            if (lane == 0) t[j] -= a;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            T v = lane < nbb ? t[jb + lane] : zero_of<T>();
+            for (int j = nbb - 1; j >= 0; j--) {
+                T yj;
+                reinterpret_cast<R*>(&yj)[0] = __shfl_sync(0xffffffff, reinterpret_cast<R*>(&v)[0], j);
+                if constexpr (sizeof(T) == 2 * sizeof(R))
+                    reinterpret_cast<R*>(&yj)[1] = __shfl_sync(0xffffffff, reinterpret_cast<R*>(&v)[1], j);
+                if (lane < j) v -= conj(Fs[(int64_t)(jb + lane) * m + jb + j]) * yj;
+            }
+            if (lane < nbb) t[jb + lane] = v;
+        }
+        __syncthreads();
+    }
+    for (int j = threadIdx.x; j < w; j += blockDim.x) x[f + j] = t[j];
+}
+
+template <typename T, typename U>
+__global__ void k_perm_in(int n, const int32_t* __restrict__ perm, const U* __restrict__ b, T* __restrict__ x,
+                          int nvec, int64_t ldb) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= (int64_t)n * nvec) return;
+    const int64_t v = q / n, j = q % n;
+    x[v * n + j] = conv<T, U>(b[v * ldb + perm[j]]);
+}
+
+template <typename T, typename U>
+__global__ void k_perm_out(int n, const int32_t* __restrict__ perm, const T* __restrict__ x, U* __restrict__ out,
+                           int nvec, int64_t ldo) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= (int64_t)n * nvec) return;
+    const int64_t v = q / n, j = q % n;
+    out[v * ldo + perm[j]] = conv<U, T>(x[v * n + j]);
+}
+
+// ------------------------------------------------------------------------------------
+void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, const std::vector<uint8_t>& conj_h) {
+    release();
+    n = S.n; ns = S.ns; max_front = S.max_front; front_entries = S.front_entries();
+    flops = 4.0 * S.flops_real;
+    auto put = [&](auto*& dptr, const auto& vec) {
+        using E = typename std::decay<decltype(vec[0])>::type;
+        const size_t b = std::max<size_t>(1, vec.size()) * sizeof(E);
+        TMG_CUDA(cudaMalloc((void**)&dptr, b));
+        if (!vec.empty()) TMG_CUDA(cudaMemcpy(dptr, vec.data(), vec.size() * sizeof(E), cudaMemcpyHostToDevice));
+        bytes += b;
+    };
+    put(sn_first, S.sn_first); put(sn_rows, S.sn_rows); put(rel, S.rel); put(child_ptr, S.child_ptr);
+    put(child_list, S.child_list); put(sn_row_ptr, S.sn_row_ptr); put(front_off, S.front_off);
+    put(rel_ptr, S.rel_ptr); put(perm, S.perm); put(level_sn, S.level_sn);
+    put(dest, dest_h); put(conj, conj_h);
+    nlower = (int64_t)dest_h.size();
+    level_ptr = S.level_ptr;
+    l_entries = 0;
+    for (int s = 0; s < ns; s++) {
+        const int64_t m = S.sn_row_ptr[s + 1] - S.sn_row_ptr[s];
+        const int64_t w = S.sn_first[s + 1] - S.sn_first[s];
+        l_entries += m * w - w * (w - 1) / 2;
+    }
+    // work lists
+    std::vector<int32_t> it;
+    steps.clear();
+    const int nlev = (int)S.level_ptr.size() - 1;
+    level_max_m.assign(nlev, 0);
+    for (int l = 0; l < nlev; l++) {
+        int maxw = 0;
+        int maxch = 0;
+        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+            const int s = S.level_sn[q];
+            maxw = std::max(maxw, S.sn_first[s + 1] - S.sn_first[s]);
+            maxch = std::max(maxch, S.child_ptr[s + 1] - S.child_ptr[s]);
+            level_max_m[l] = std::max<int32_t>(level_max_m[l], (int32_t)(S.sn_row_ptr[s + 1] - S.sn_row_ptr[s]));
+        }
+        const int nkb = (maxw + MF_NB - 1) / MF_NB;
+        for (int kb = 0; kb < nkb; kb++) {
+            Step st{};
+            st.kb = kb;
+            if (kb == 0) {
+                for (int r = 0; r < maxch; r++) {
+                    st.ext_off.push_back((int64_t)it.size());
+                    int cnt = 0;
+                    int64_t umax = 0;
+                    for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                        const int s = S.level_sn[q];
+                        if (S.child_ptr[s + 1] - S.child_ptr[s] > r) {
+                            const int c = S.child_list[S.child_ptr[s] + r];
+                            it.push_back(s); it.push_back(c);
+                            cnt++;
+                            const int64_t u = (S.sn_row_ptr[c + 1] - S.sn_row_ptr[c]) - (S.sn_first[c + 1] - S.sn_first[c]);
+                            umax = std::max<int64_t>(umax, u);
+                        }
+                    }
+                    st.ext_cnt.push_back(cnt);
+                    st.ext_max.push_back((int32_t)umax);
+                }
+            }
+            st.diag_off = (int64_t)it.size();
+            st.diag_cnt = 0;
+            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                const int s = S.level_sn[q];
+                if (S.sn_first[s + 1] - S.sn_first[s] > kb * MF_NB) { it.push_back(s); st.diag_cnt++; }
+            }
+            st.panel_off = (int64_t)it.size();
+            st.panel_cnt = 0;
+            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                const int s = S.level_sn[q];
+                const int w = S.sn_first[s + 1] - S.sn_first[s];
+                if (w <= kb * MF_NB) continue;
+                const int64_t m = S.sn_row_ptr[s + 1] - S.sn_row_ptr[s];
+                const int64_t r0 = kb * MF_NB + std::min(MF_NB, w - kb * MF_NB);
+                for (int64_t r = r0; r < m; r += 64) { it.push_back(s); it.push_back((int32_t)r); st.panel_cnt++; }
+            }
+            st.upd_off = (int64_t)it.size();
+            st.upd_cnt = 0;
+            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                const int s = S.level_sn[q];
+                const int w = S.sn_first[s + 1] - S.sn_first[s];
+                if (w <= kb * MF_NB) continue;
+                const int64_t m = S.sn_row_ptr[s + 1] - S.sn_row_ptr[s];
+                const int64_t t0 = kb * MF_NB + std::min(MF_NB, w - kb * MF_NB);
+                const int64_t T = (m - t0 + MF_TILE - 1) / MF_TILE;
+                for (int64_t a = 0; a < T; a++)
+                    for (int64_t b = 0; b <= a; b++) {
+                        it.push_back(s); it.push_back((int32_t)a); it.push_back((int32_t)b);
+                        st.upd_cnt++;
+                    }
+            }
+            steps.push_back(st);
+        }
+    }
+    put(items, it);
+}
+
+void DevSymbolic::release() {
+    for (void* p : {(void*)sn_first, (void*)sn_rows, (void*)rel, (void*)child_ptr, (void*)child_list,
+                    (void*)sn_row_ptr, (void*)front_off, (void*)rel_ptr, (void*)perm, (void*)level_sn,
+                    (void*)items, (void*)dest, (void*)conj})
+        if (p) cudaFree(p);
+    sn_first = sn_rows = rel = child_ptr = child_list = perm = level_sn = items = nullptr;
+    sn_row_ptr = front_off = rel_ptr = dest = nullptr;
+    conj = nullptr;
+    bytes = 0;
+}
+
+template <typename T>
+void mf_scatter(cudaStream_t st, const DevSymbolic& S, const T* vals, T* F) {
+    if (S.nlower == 0) return;
+    TMG_LAUNCH(k_scatter<T>, (unsigned)ceil_div(S.nlower, 256), 256, 0, st, S.nlower, vals, S.dest, S.conj, F);
+    TMG_CHECK_LAUNCH();
+}
+
+template <typename T>
+void mf_factor(cudaStream_t st, const DevSymbolic& S, T* F, int* status) {
+    static bool attr_set = false;
+    const size_t upd_smem = 2 * MF_NB * MF_TILE * sizeof(T);
+    if (!attr_set) {
+        TMG_CUDA(cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem));
+        attr_set = true;
+    }
+    for (const auto& stp : S.steps) {
+        for (size_t r = 0; r < stp.ext_off.size(); r++) {
+            if (stp.ext_cnt[r] == 0) continue;
+            const int64_t ent = (int64_t)stp.ext_max[r] * stp.ext_max[r];
+            const unsigned gx = (unsigned)std::min<int64_t>(std::max<int64_t>(1, ceil_div(ent, 256)), 4096);
+            const unsigned gy = (unsigned)std::min<int64_t>(stp.ext_cnt[r], 65535);
+            TMG_LAUNCH(k_extend_add<T>, dim3(gx, gy), 256, 0, st, S.items + stp.ext_off[r], stp.ext_cnt[r],
+                       S.sn_first, S.sn_row_ptr, S.front_off, S.rel_ptr, S.rel, F);
+        }
+        if (stp.diag_cnt)
+            TMG_LAUNCH(k_diag<T>, stp.diag_cnt, 256, 0, st, S.items + stp.diag_off, stp.kb, S.sn_first,
+                       S.sn_row_ptr, S.front_off, F, status);
+        if (stp.panel_cnt)
+            TMG_LAUNCH(k_panel<T>, stp.panel_cnt, 64, 0, st, S.items + stp.panel_off, stp.kb, S.sn_first,
+                       S.sn_row_ptr, S.front_off, F);
+        if (stp.upd_cnt)
+            TMG_LAUNCH(k_update<T>, stp.upd_cnt, 256, upd_smem, st, S.items + stp.upd_off, stp.kb, S.sn_first,
+                       S.sn_row_ptr, S.front_off, F);
+    }
+    TMG_CHECK_LAUNCH();
+}
+
+template <typename T>
+void mf_solve(cudaStream_t st, const DevSymbolic& S, const T* F, T* x, T* tbuf) {
+    const int nlev = (int)S.level_ptr.size() - 1;
+    for (int l = 0; l < nlev; l++) {
+        const int cnt = S.level_ptr[l + 1] - S.level_ptr[l];
+        if (cnt)
+            TMG_LAUNCH(k_fwd<T>, cnt, 256, 0, st, S.level_sn + S.level_ptr[l], S.sn_first, S.sn_row_ptr, S.front_off,
+                       S.child_ptr, S.child_list, S.rel_ptr, S.rel, F, x, tbuf);
+    }
+    for (int l = nlev - 1; l >= 0; l--) {
+        const int cnt = S.level_ptr[l + 1] - S.level_ptr[l];
+        if (cnt)
+            TMG_LAUNCH(k_bwd<T>, cnt, 256, 0, st, S.level_sn + S.level_ptr[l], S.sn_first, S.sn_row_ptr, S.sn_rows,
+                       S.front_off, F, x, tbuf);
+    }
+    TMG_CHECK_LAUNCH();
+}
+
+template <typename T, typename U>
+void mf_permute_in(cudaStream_t st, const DevSymbolic& S, const U* b, T* x, int nvec, int64_t ldb) {
+    const int64_t tot = (int64_t)S.n * nvec;
+    if (!tot) return;
+    TMG_LAUNCH((k_perm_in<T, U>), (unsigned)ceil_div(tot, 256), 256, 0, st, S.n, S.perm, b, x, nvec, ldb);
+    TMG_CHECK_LAUNCH();
+}
+template <typename T, typename U>
+void mf_permute_out(cudaStream_t st, const DevSymbolic& S, const T* x, U* out, int nvec, int64_t ldo) {
+    const int64_t tot = (int64_t)S.n * nvec;
+    if (!tot) return;
+    TMG_LAUNCH((k_perm_out<T, U>), (unsigned)ceil_div(tot, 256), 256, 0, st, S.n, S.perm, x, out, nvec, ldo);
+    TMG_CHECK_LAUNCH();
+}
+
+#define TMG_INST(T)                                                                            \
+    template void mf_factor<T>(cudaStream_t, const DevSymbolic&, T*, int*);                    \
+    template void mf_scatter<T>(cudaStream_t, const DevSymbolic&, const T*, T*);               \
+    template void mf_solve<T>(cudaStream_t, const DevSymbolic&, const T*, T*, T*);
+TMG_INST(double)
+TMG_INST(float)
+TMG_INST(zd)
+TMG_INST(zf)
+template void mf_permute_in<double, double>(cudaStream_t, const DevSymbolic&, const double*, double*, int, int64_t);
+template void mf_permute_in<float, double>(cudaStream_t, const DevSymbolic&, const double*, float*, int, int64_t);
+template void mf_permute_out<float, double>(cudaStream_t, const DevSymbolic&, const float*, double*, int, int64_t);
+template void mf_permute_in<zd, zd>(cudaStream_t, const DevSymbolic&, const zd*, zd*, int, int64_t);
+template void mf_permute_in<zf, zd>(cudaStream_t, const DevSymbolic&, const zd*, zf*, int, int64_t);
+template void mf_permute_out<double, double>(cudaStream_t, const DevSymbolic&, const double*, double*, int, int64_t);
+template void mf_permute_out<zd, zd>(cudaStream_t, const DevSymbolic&, const zd*, zd*, int, int64_t);
+template void mf_permute_out<zf, zd>(cudaStream_t, const DevSymbolic&, const zf*, zd*, int, int64_t);
+
+}  // namespace tmg

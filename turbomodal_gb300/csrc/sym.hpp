@@ -1,0 +1,82 @@
+// Host-side symbolic analysis for the GB300 supernodal LDL^H: fill-reducing order,
+// elimination tree, supernode partition, frontal structure and level schedule.
+// Pattern-only work runs once per sparsity pattern on the host; all arithmetic on
+// matrix values runs on the device.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace tmg {
+
+// Compressed sparse column pattern (rows sorted inside each column).
+struct Pattern {
+    int32_t nrows = 0, ncols = 0;
+    std::vector<int64_t> p{0};
+    std::vector<int32_t> i;
+    int64_t nnz() const { return (int64_t)i.size(); }
+};
+
+// Approximate minimum degree order of a symmetric pattern given with both triangles
+// and its diagonal.  Returns order[k] = index of the k-th pivot.  The algorithm is the
+// published AMD of Amestoy, Davis & Duff in the cs_amd formulation (T. A. Davis, Direct
+// Methods for Sparse Linear Systems, SIAM 2006), in the variant that keeps the diagonal
+// in the quotient graph (a node whose only entry is its diagonal is eliminated at once,
+// a node without a diagonal entry is ordered last) — the ordering Eigen 3.4.0's
+// AMDOrdering computes for the reference's SimplicialLDLT.
+std::vector<int32_t> amd_order(int32_t n, const std::vector<int64_t>& colptr, const std::vector<int32_t>& rowind);
+
+// Supernodal symbolic factorisation of a Hermitian matrix given by its lower triangle.
+struct Symbolic {
+    int32_t n = 0;
+    // Reference-equivalent analysis (bit-exact targets): AMD order, etree, column counts
+    // in AMD numbering, as SimplicialLDLT::analyzePattern computes them.
+    std::vector<int32_t> amd;           // amd[k] = original index of pivot k
+    std::vector<int32_t> etree;         // parent in AMD numbering (-1 = root)
+    std::vector<int32_t> colcount;      // off-diagonal nonzeros of L per column (AMD numbering)
+    int64_t nnz_l = 0;                  // sum of colcount
+    // Factorisation numbering: the etree postorder of the AMD order (same fill, same tree).
+    std::vector<int32_t> perm;          // perm[j] = original index of factor column j
+    std::vector<int32_t> iperm;         // iperm[orig] = factor column
+    // Supernodes (contiguous factor columns with nested structure)
+    int32_t ns = 0;
+    std::vector<int32_t> sn_first;      // ns + 1
+    std::vector<int32_t> sn_parent;     // supernodal tree, -1 = root
+    std::vector<int64_t> sn_row_ptr;    // ns + 1, into sn_rows
+    std::vector<int32_t> sn_rows;       // sorted global factor rows of each front
+    std::vector<int64_t> front_off;     // ns + 1, front storage offsets (m*m entries each)
+    std::vector<int64_t> rel_ptr;       // ns + 1, into rel (update rows of s -> parent local)
+    std::vector<int32_t> rel;
+    std::vector<int32_t> child_ptr, child_list;   // children of each supernode (ascending)
+    std::vector<int32_t> level_ptr, level_sn;     // supernodes grouped by tree height
+    int32_t max_front = 0;
+    double flops_real = 0.0;            // sum_j c_j^2 (multiply-adds of the factorisation)
+    int64_t front_entries() const { return front_off.empty() ? 0 : front_off.back(); }
+};
+
+// lower: lower-triangle pattern (orig numbering) of the operator.  relax: merge a child
+// supernode into its parent when the combined front adds at most this fraction of
+// explicit zeros (0 = fundamental supernodes only).
+Symbolic analyze(const Pattern& lower, double relax = 0.0, int32_t relax_max_width = 0);
+
+// Destination of every lower-triangle entry of `lower` (in its CSC order) inside the
+// front storage of `S`; conj flag set when the entry lands transposed.
+void scatter_map(const Symbolic& S, const Pattern& lower, std::vector<int64_t>& dest, std::vector<uint8_t>& conj);
+
+// Symbolic sparse product C = A*B recording, for every C entry, its contributions in the
+// accumulation order (for each B(k,j) in row order, each A(i,k) in row order).
+struct Product {
+    Pattern C;
+    std::vector<int64_t> cptr;          // C.nnz()+1
+    std::vector<int64_t> a_slot, b_slot;
+};
+Product product(const Pattern& A, const Pattern& B);
+
+Pattern transpose(const Pattern& A);
+// Union of patterns (same shape).
+Pattern pattern_union(const std::vector<const Pattern*>& parts);
+// Position of every entry of `sub` inside `sup` (-1 when absent).
+std::vector<int64_t> locate(const Pattern& sup, const Pattern& sub);
+Pattern lower_triangle(const Pattern& A);
+
+}  // namespace tmg

@@ -1,0 +1,243 @@
+"""Host-side mirror of turbomodal's solver interface over the GB300 C ABI.
+
+``CyclicSymmetrySolver.solve_at_rpm`` keeps the reference signature and result semantics
+(src/python_bindings.cpp:321-361, src/cyclic_solver.cpp:725-1357); ``solve`` and
+``rpm_sweep`` keep ``tm.solve`` / ``tm.rpm_sweep`` (python/turbomodal/solver.py:237-375,
+:499-628), including the enriched ``modal_mass_kg`` field.  All numerical work runs in
+libtmg.so on the GPU; failed harmonics are omitted with a warning, as in the reference.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import logging
+import sys
+from dataclasses import dataclass, field
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib
+from .mesh import Mesh
+from .meshgen import Material
+
+logger = logging.getLogger(__name__)
+
+
+class ModalResult:
+    """Result of one harmonic index (include/turbomodal/modal_solver.hpp:8-32)."""
+
+    def __init__(self, harmonic_index=0, rpm=0.0, frequencies=None, mode_shapes=None, whirl_direction=None,
+                 converged=True):
+        self.harmonic_index = int(harmonic_index)
+        self.rpm = float(rpm)
+        self.frequencies = np.zeros(0) if frequencies is None else frequencies
+        self.mode_shapes = np.zeros((0, 0), np.complex128) if mode_shapes is None else mode_shapes
+        self.whirl_direction = np.zeros(0, np.int32) if whirl_direction is None else whirl_direction
+        self.converged = bool(converged)
+        self.iterations = 0
+        self.max_residual = 0.0
+        self.refine_residual = 0.0
+
+    def wave_propagation_velocity(self, radius: float) -> np.ndarray:
+        k = self.harmonic_index
+        if k <= 0:
+            return np.zeros_like(self.frequencies)
+        return 2.0 * np.pi * self.frequencies * radius / k
+
+    def __repr__(self):
+        return (f"ModalResult(k={self.harmonic_index}, rpm={self.rpm}, "
+                f"freqs={np.round(self.frequencies, 3).tolist()}, converged={self.converged})")
+
+
+class CyclicSymmetrySolver:
+    """GPU cyclic-symmetry modal solver for one sector mesh and material."""
+
+    def __init__(self, mesh: Mesh, material: Material, fluid=None, apply_hub_constraint: bool = True,
+                 device: int = 0, precision: str = "fp64", mem_budget_bytes: int = 0):
+        if fluid is not None and getattr(fluid, "type", None) not in (None, 0, "NONE"):
+            raise NotImplementedError("fluid coupling is not part of the GPU path")
+        self.mesh = mesh
+        self.material = material
+        self.precision = precision
+        self.ctx = _lib.Context(device, mem_budget_bytes)
+        hub = mesh.find_node_set("hub_constraint") if apply_hub_constraint else None
+        self._keep = dict(
+            X=np.ascontiguousarray(mesh.nodes, dtype=np.float64).reshape(-1),
+            conn=np.ascontiguousarray(mesh.elements, dtype=np.int32).reshape(-1),
+            left=np.asarray(mesh.left_boundary, dtype=np.int32),
+            right=np.asarray(mesh.right_boundary, dtype=np.int32),
+            pairs=np.asarray(mesh.matched_pairs, dtype=np.int32).reshape(-1),
+            hub=np.asarray(hub.node_ids if hub is not None else [], dtype=np.int32),
+        )
+        k = self._keep
+        d = _lib.SectorDesc(
+            mesh.num_nodes(), _lib.ptr(k["X"], C.c_double), mesh.num_elements(), _lib.ptr(k["conn"], C.c_int32),
+            material.E, material.nu, material.rho, mesh.num_sectors, mesh.rotation_axis,
+            len(k["left"]), _lib.ptr(k["left"], C.c_int32), len(k["right"]), _lib.ptr(k["right"], C.c_int32),
+            len(mesh.matched_pairs), _lib.ptr(k["pairs"], C.c_int32), len(k["hub"]), _lib.ptr(k["hub"], C.c_int32))
+        self.ctx.check(self.ctx.L.tmg_upload_sector(self.ctx.h, C.byref(d)), "tmg_upload_sector")
+
+    # --- modal solve -------------------------------------------------------------------
+    def solve_at_rpm(self, rpm: float, num_modes_per_harmonic: int, harmonic_indices=(), max_threads: int = 0,
+                     include_coriolis: bool = False, min_frequency: float = 0.0, progress_cb=None,
+                     allow_condensation: bool = False, memory_reserve_fraction: float = 0.2,
+                     precision: str | None = None) -> list[ModalResult]:
+        prec = _lib.PREC[precision or self.precision]
+        hi = np.asarray(list(harmonic_indices or []), dtype=np.int32)
+        nres = C.c_int32()
+        L, h = self.ctx.L, self.ctx.h
+        rc = L.tmg_solve_at_rpm(h, float(rpm), int(num_modes_per_harmonic),
+                                _lib.ptr(hi, C.c_int32) if hi.size else None, int(hi.size),
+                                int(include_coriolis), float(min_frequency), prec, C.byref(nres))
+        self.ctx.check(rc, "tmg_solve_at_rpm")
+        out = []
+        ndof = self.mesh.num_dof()
+        for idx in range(nres.value):
+            meta = _lib.ResultMeta()
+            L.tmg_result_info(h, idx, C.byref(meta))
+            if meta.status != _lib.TMG_OK:
+                sys.stderr.write(f"[CyclicSolver] k={meta.harmonic_index} FAILED: "
+                                 f"{_lib.ERRORS.get(meta.status, meta.status)}\n")
+                continue
+            m = meta.num_modes
+            f = np.zeros(m)
+            w = np.zeros(m, np.int32)
+            s = np.zeros(2 * ndof * m)
+            L.tmg_result_copy(h, idx, _lib.ptr(f, C.c_double), _lib.ptr(s, C.c_double), _lib.ptr(w, C.c_int32))
+            r = ModalResult(meta.harmonic_index, meta.rpm, f, s.view(np.complex128).reshape(m, ndof).T.copy(), w,
+                            bool(meta.converged))
+            r.iterations = meta.iterations
+            r.max_residual = meta.max_residual
+            r.refine_residual = meta.refine_residual
+            if not r.converged:
+                sys.stderr.write(f"[CyclicSolver] WARNING: k={r.harmonic_index} eigenvalue solve did not fully converge\n")
+            out.append(r)
+            if progress_cb is not None:
+                progress_cb(dict(completed=len(out), total=nres.value, harmonic_k=r.harmonic_index,
+                                 converged=r.converged, num_modes=m))
+        return out
+
+    def solve_rpm_sweep(self, rpm_values, num_modes_per_harmonic: int, harmonic_indices=(), max_threads: int = 0,
+                        include_coriolis: bool = False, min_frequency: float = 0.0, precision: str | None = None):
+        return [self.solve_at_rpm(r, num_modes_per_harmonic, harmonic_indices, max_threads, include_coriolis,
+                                  min_frequency, precision=precision) for r in rpm_values]
+
+    def last_timing(self):
+        ph = np.zeros(8)
+        nl = C.c_int64()
+        self.ctx.L.tmg_last_timing(self.ctx.h, _lib.ptr(ph, C.c_double), 8, C.byref(nl))
+        return dict(prepare_ms=ph[0], factor_ms=ph[1], lanczos_ms=ph[2], post_ms=ph[3], kernel_launches=nl.value)
+
+    # --- matrices (parity / inspection) --------------------------------------------------
+    def assemble(self, which: str, rpm: float = 0.0) -> sp.csc_matrix:
+        L, h = self.ctx.L, self.ctx.h
+        nnz = C.c_int64()
+        self.ctx.check(L.tmg_assemble(h, _lib.MAT[which], float(rpm), C.byref(nnz), None, None, None), "tmg_assemble")
+        n = self.mesh.num_dof()
+        p = np.zeros(n + 1, np.int32)
+        i = np.zeros(max(nnz.value, 1), np.int32)
+        x = np.zeros(max(nnz.value, 1))
+        self.ctx.check(L.tmg_assemble(h, _lib.MAT[which], float(rpm), C.byref(nnz), _lib.ptr(p, C.c_int32),
+                                      _lib.ptr(i, C.c_int32), _lib.ptr(x, C.c_double)), "tmg_assemble")
+        A = sp.csc_matrix((x[: nnz.value], i[: nnz.value], p), shape=(n, n))
+        A.has_sorted_indices = True
+        return A
+
+    def prepare(self, rpm: float, coriolis: bool = False) -> None:
+        self.ctx.check(self.ctx.L.tmg_prepare(self.ctx.h, float(rpm), int(coriolis)), "tmg_prepare")
+
+    def projection(self, which: str, k: int = 0) -> sp.csc_matrix:
+        L, h = self.ctx.L, self.ctx.h
+        nnz, n = C.c_int64(), C.c_int32()
+        self.ctx.check(L.tmg_projection(h, _lib.MAT[which], k, C.byref(nnz), C.byref(n), None, None, None),
+                       "tmg_projection")
+        p = np.zeros(n.value + 1, np.int32)
+        i = np.zeros(max(nnz.value, 1), np.int32)
+        x = np.zeros(2 * max(nnz.value, 1))
+        self.ctx.check(L.tmg_projection(h, _lib.MAT[which], k, C.byref(nnz), C.byref(n), _lib.ptr(p, C.c_int32),
+                                        _lib.ptr(i, C.c_int32), _lib.ptr(x, C.c_double)), "tmg_projection")
+        vals = x[: 2 * nnz.value].view(np.complex128)
+        if which in ("K0r", "M0r", "Khr", "Mhr"):
+            vals = x[: nnz.value]
+        A = sp.csc_matrix((vals.copy(), i[: nnz.value], p), shape=(n.value, n.value))
+        A.has_sorted_indices = True
+        return A
+
+    def symbolic(self, kind: int = 0):
+        """(AMD order, elimination tree, L column counts) of the shift-invert operator."""
+        L, h = self.ctx.L, self.ctx.h
+        n = C.c_int32()
+        self.ctx.check(L.tmg_symbolic(h, kind, C.byref(n), None, None, None), "tmg_symbolic")
+        perm = np.zeros(n.value, np.int32)
+        par = np.zeros(n.value, np.int32)
+        cc = np.zeros(n.value, np.int32)
+        self.ctx.check(L.tmg_symbolic(h, kind, C.byref(n), _lib.ptr(perm, C.c_int32), _lib.ptr(par, C.c_int32),
+                                      _lib.ptr(cc, C.c_int32)), "tmg_symbolic")
+        return perm, par, cc
+
+
+@dataclass
+class EnrichedModalResult:
+    """ModalResult plus full-annulus modal mass (python/turbomodal/solver.py:30-53)."""
+
+    _result: ModalResult = field(repr=False)
+    modal_mass_kg: np.ndarray
+
+    def __getattr__(self, name):
+        return getattr(self._result, name)
+
+
+def _modal_mass_from_M(M_sector, results, num_sectors):
+    """N * Re(phi^H M phi) per mode (python/turbomodal/solver.py:91-103)."""
+    out = []
+    for r in results:
+        shapes = np.asarray(r.mode_shapes)
+        if shapes.size == 0:
+            out.append(np.zeros(0))
+            continue
+        M_phi = M_sector @ shapes
+        out.append(np.asarray(num_sectors * np.real(np.sum(shapes.conj() * M_phi, axis=0)), dtype=np.float64))
+    return out
+
+
+def _validate(results):
+    for r in results:
+        f = np.asarray(r.frequencies)
+        if f.size and np.any(np.isnan(f)):
+            logger.warning("ND=%d: NaN frequencies detected", r.harmonic_index)
+        if f.size and np.any(f < 0):
+            logger.warning("ND=%d: negative frequencies detected", r.harmonic_index)
+    return results
+
+
+def solve(mesh: Mesh, material: Material, rpm: float = 0.0, num_modes: int = 20, fluid=None, config=None,
+          verbose: int = 0, harmonic_indices=None, max_threads: int = 0, hub_constraint: str = "fixed",
+          include_coriolis: bool = False, min_frequency: float = 0.0, temperature: float | None = None,
+          memory_reserve_fraction: float = 0.2, precision: str = "fp64", solver: CyclicSymmetrySolver | None = None):
+    """tm.solve on the GPU path; returns EnrichedModalResult per harmonic index."""
+    if temperature is not None:
+        material = material.at_temperature(temperature)
+    s = solver or CyclicSymmetrySolver(mesh, material, fluid, hub_constraint == "fixed", precision=precision)
+    res = s.solve_at_rpm(rpm, num_modes, harmonic_indices or [], max_threads, include_coriolis, min_frequency,
+                         memory_reserve_fraction=memory_reserve_fraction, precision=precision)
+    res = _validate(res)
+    M = s.assemble("M")
+    masses = _modal_mass_from_M(M, res, mesh.num_sectors)
+    return [EnrichedModalResult(_result=r, modal_mass_kg=m) for r, m in zip(res, masses)]
+
+
+def rpm_sweep(mesh: Mesh, material: Material, rpm_values, num_modes: int = 10, harmonic_indices=None,
+              include_coriolis: bool = False, min_frequency: float = 0.0, precision: str = "fp64", verbose: int = 0,
+              hub_constraint: str = "fixed"):
+    """tm.rpm_sweep on the GPU path: one solver (sector assembly and symbolic analysis
+    reused across speeds), one solve per speed."""
+    s = CyclicSymmetrySolver(mesh, material, None, hub_constraint == "fixed", precision=precision)
+    M = s.assemble("M")
+    out = []
+    for rpm in np.asarray(rpm_values, dtype=np.float64):
+        res = s.solve_at_rpm(float(rpm), num_modes, harmonic_indices or [], 0, include_coriolis, min_frequency,
+                             precision=precision)
+        masses = _modal_mass_from_M(M, res, mesh.num_sectors)
+        out.append([EnrichedModalResult(_result=r, modal_mass_kg=m) for r, m in zip(res, masses)])
+    return out
