@@ -119,6 +119,11 @@ int tmg_projection(tmg_context* ctx, int which, int k, int64_t* nnz, int32_t* n,
 int tmg_symbolic(tmg_context* ctx, int kind, int32_t* n, int32_t* perm, int32_t* parent,
                  int32_t* colcount);
 
+/* Size of the symbolic factorisation of kind (see tmg_symbolic): out[0] n, [1] nnz(L) of the
+ * simplicial factor, [2] supernodes, [3] tree levels, [4] largest front, [5] front storage
+ * entries, [6] factorisation flops (real, complex arithmetic counted x4), [7] lower entries. */
+int tmg_symbolic_stats(tmg_context* ctx, int kind, double* out);
+
 /* Full modal solve at one speed; replaces CyclicSymmetrySolver::solve_at_rpm
  * (cyclic_solver.cpp:725-1357, python_bindings.cpp:332-361).  harmonics == NULL or
  * nh == 0 solves k = 0..N/2.  Results stay in the context until the next solve. */
@@ -130,9 +135,18 @@ int tmg_solve_at_rpm(tmg_context* ctx, double rpm, int num_modes, const int32_t*
 int tmg_result_info(tmg_context* ctx, int idx, tmg_result_meta* info);
 int tmg_result_copy(tmg_context* ctx, int idx, double* freqs, double* shapes, int32_t* whirl);
 
-/* Device time (ms) spent in each phase of the last solve, and launch count of this
- * library's kernels in it. */
+/* Time (ms) of the phases of the last tmg_solve_at_rpm: [0] prepare (assembly, prestress,
+ * projections), [1] factorisations, [2] Lanczos, [3] post-processing, [4] the whole call
+ * measured with CUDA events on the context's stream; and the number of this library's
+ * kernel launches in it. */
 int tmg_last_timing(tmg_context* ctx, double* phase_ms, int nphase, int64_t* kernel_launches);
+
+/* Profiling mode (measurement only; it synchronises after every triangular solve): CUDA-event
+ * time of each shift-invert triangular-solve graph.  tmg_profile_solve returns out[0] number of
+ * solves, out[1] total ms, out[2] algorithmic bytes (stored L entries read once per sweep
+ * direction + the solution vector), accumulated since tmg_set_profiling. */
+int tmg_set_profiling(tmg_context* ctx, int on);
+int tmg_profile_solve(tmg_context* ctx, double* out);
 
 #ifdef __cplusplus
 }

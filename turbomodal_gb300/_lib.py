@@ -25,7 +25,8 @@ PREC = {"fp64": 0, "mixed": 1}
 
 EXPORTED = ["tmg_create", "tmg_destroy", "tmg_last_error", "tmg_upload_sector", "tmg_assemble",
             "tmg_prepare", "tmg_projection", "tmg_symbolic", "tmg_solve_at_rpm", "tmg_result_info",
-            "tmg_result_copy", "tmg_last_timing"]
+            "tmg_result_copy", "tmg_last_timing", "tmg_symbolic_stats",
+            "tmg_set_profiling", "tmg_profile_solve"]
 
 
 class SectorDesc(C.Structure):
@@ -72,10 +73,13 @@ def load(build_if_missing: bool = True):
     L.tmg_prepare.argtypes = [P, C.c_double, C.c_int]
     L.tmg_projection.argtypes = [P, C.c_int, C.c_int, I64P, I32P, I32P, I32P, DP]
     L.tmg_symbolic.argtypes = [P, C.c_int, I32P, I32P, I32P, I32P]
+    L.tmg_symbolic_stats.argtypes = [P, C.c_int, DP]
     L.tmg_solve_at_rpm.argtypes = [P, C.c_double, C.c_int, I32P, C.c_int, C.c_int, C.c_double, C.c_int, I32P]
     L.tmg_result_info.argtypes = [P, C.c_int, C.POINTER(ResultMeta)]
     L.tmg_result_copy.argtypes = [P, C.c_int, DP, DP, I32P]
     L.tmg_last_timing.argtypes = [P, DP, C.c_int, I64P]
+    L.tmg_set_profiling.argtypes = [P, C.c_int]
+    L.tmg_profile_solve.argtypes = [P, DP]
     _lib = L
     return L
 

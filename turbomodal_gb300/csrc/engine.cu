@@ -173,6 +173,58 @@ __global__ void k_conv_copy(int64_t n, const U* __restrict__ a, T* __restrict__ 
     if (i < n) b[i] = conv<T, U>(a[i]);
 }
 
+// s_i = 1/sqrt(|Re a_ii|) from a CSR matrix (1 when the diagonal is absent or zero)
+template <typename T>
+__global__ void k_diag_scale(int32_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                             const T* __restrict__ v, double* __restrict__ s) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double d = 0.0;
+    for (int64_t q = rp[i]; q < rp[i + 1]; q++)
+        if (ci[q] == i) d = fabs(re(v[q]));
+    s[i] = d > 0.0 ? 1.0 / sqrt(d) : 1.0;
+}
+
+template <typename T, typename U>
+__global__ void k_scale_lower(int64_t n, const int32_t* __restrict__ row, const int32_t* __restrict__ col,
+                              const double* __restrict__ s, const U* __restrict__ v, T* __restrict__ out) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q < n) out[q] = conv<T, U>((s[row[q]] * s[col[q]]) * v[q]);
+}
+
+// number of non-positive pivots of a factor (D on the front diagonals)
+template <typename T>
+__global__ void k_count_nonpos(int32_t ns, const int32_t* __restrict__ sn_first, const int64_t* __restrict__ sn_row_ptr,
+                               const int64_t* __restrict__ front_off, const T* __restrict__ F, int* __restrict__ cnt) {
+    const int32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= ns) return;
+    const int64_t m = sn_row_ptr[s + 1] - sn_row_ptr[s];
+    const int w = sn_first[s + 1] - sn_first[s];
+    int c = 0;
+    for (int j = 0; j < w; j++)
+        if (!(re(F[front_off[s] + (int64_t)j * m + j]) > 0)) c++;
+    if (c) atomicAdd(cnt, c);
+}
+
+template <typename T>
+__global__ void k_pcg_xr(int64_t n, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
+                         const T* __restrict__ q, const T* __restrict__ rz, const T* __restrict__ pq) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double a = re(rz[0]) / re(pq[0]);
+    x[i] += a * p[i];
+    r[i] -= a * q[i];
+}
+
+template <typename T>
+__global__ void k_pcg_p(int64_t n, T* __restrict__ p, const T* __restrict__ z, const T* __restrict__ rznew,
+                        const T* __restrict__ rz) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double b = re(rznew[0]) / re(rz[0]);
+    p[i] = z[i] + b * p[i];
+}
+
 template <typename T>
 __global__ void k_gather_i32(int64_t n, const int32_t* __restrict__ idx, const T* __restrict__ src, T* __restrict__ dst) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -301,10 +353,13 @@ void build_union(UnionMaps& um, const std::vector<const Pattern*>& parts) {
     um.csr_col.upload(Ut.i);
     um.lower = lower_triangle(um.U);
     std::vector<int64_t> l2c;
+    std::vector<int32_t> lr, lc;
     for (int32_t j = 0; j < um.U.ncols; j++)
         for (int64_t q = um.U.p[j]; q < um.U.p[j + 1]; q++)
-            if (um.U.i[q] >= j) l2c.push_back(q);
+            if (um.U.i[q] >= j) { l2c.push_back(q); lr.push_back(um.U.i[q]); lc.push_back(j); }
     um.lower2csc.upload(l2c);
+    um.low_row.upload(lr);
+    um.low_col.upload(lc);
 }
 
 }  // namespace tmg
@@ -322,6 +377,7 @@ struct ResultHost {
     std::vector<zd> shapes;          // ndof x m
     int32_t converged = 0, iterations = 0, status = 0;
     double max_residual = 0.0, refine_residual = 0.0;
+    int64_t solves = 0, applies = 0;
 };
 
 struct tmg_context {
@@ -368,6 +424,11 @@ struct tmg_context {
     std::vector<ResultHost> results;
     double phase_ms[8] = {0};
     int64_t launches = 0;
+    // profiling mode: CUDA-event timing of every triangular-solve graph launch
+    bool profile = false;
+    double solve_ms = 0.0, solve_bytes = 0.0;
+    int64_t solve_count = 0;
+    cudaEvent_t pev0 = nullptr, pev1 = nullptr;
 };
 
 namespace {
@@ -883,15 +944,39 @@ template <typename Tv, typename Tf>
 struct ShiftInvert {
     tmg_context* c = nullptr;
     const DevSymbolic* D = nullptr;
+    const UnionMaps* um = nullptr;
     int32_t n = 0;
     bool mixed = false;
-    int nref = 2;
+    bool spd = false;             // every pivot positive: CG-accelerated refinement
+    int max_iter = 30;            // refinement iterations per solve (mixed)
+    double rtol = 1e-12;          // relative residual target of a refined solve (mixed)
     DevCsr<Tv> A;                 // FP64 operator K - sigma M (CSR)
     DVec<Tf> F, tb, xw;
-    DVec<Tv> r, d;
+    DVec<Tv> r, d, z, pp, q, sc;
+    DVec<double> scale, np, nrm;
     double worst_refine = 0.0;
-    int diag_left = 1;
-    DVec<double> np, nrm;
+    int64_t solves = 0, applies = 0, max_its = 0;
+    // the permute-in / supernodal sweeps / permute-out sequence of one solve is captured
+    // once into a CUDA graph over fixed buffers and replayed for every solve
+    DVec<Tv> gin, gout;
+    cudaGraphExec_t gexec = nullptr;
+    ~ShiftInvert() { if (gexec) cudaGraphExecDestroy(gexec); }
+
+    void capture() {
+        const double* s = mixed ? scale.p : nullptr;
+        gin.alloc(n);
+        gout.alloc(n);
+        cudaGraph_t g;
+        TMG_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+        mf_permute_in<Tf, Tv>(c->st, *D, gin.p, xw.p, 1, n, s);
+        mf_solve<Tf>(c->st, *D, F.p, xw.p, tb.p);
+        mf_permute_out<Tf, Tv>(c->st, *D, xw.p, gout.p, 1, n, s);
+        TMG_CUDA(cudaStreamEndCapture(c->st, &g));
+        TMG_CUDA(cudaGraphInstantiate(&gexec, g, 0));
+        TMG_CUDA(cudaGraphDestroy(g));
+        launches_per_solve = g_kernel_launches_delta;
+    }
+    int64_t launches_per_solve = 0, g_kernel_launches_delta = 0;
 
     void factor(const Tv* lower_vals, int64_t nlower) {
         F.alloc(D->front_entries);
@@ -899,69 +984,110 @@ struct ShiftInvert {
         if constexpr (std::is_same<Tv, Tf>::value) {
             mf_scatter<Tf>(c->st, *D, lower_vals, F.p);
         } else {
+            scale.alloc(n);
+            TMG_LAUNCH(k_diag_scale<Tv>, nblk(n), 256, 0, c->st, n, A.rowptr, A.col, A.val, scale.p);
             DVec<Tf> lv;
             lv.alloc(nlower);
-            TMG_LAUNCH((k_conv_copy<Tf, Tv>), nblk(nlower), 256, 0, c->st, nlower, lower_vals, lv.p);
+            TMG_LAUNCH((k_scale_lower<Tf, Tv>), nblk(nlower), 256, 0, c->st, nlower, um->low_row.p, um->low_col.p,
+                       scale.p, lower_vals, lv.p);
             mf_scatter<Tf>(c->st, *D, lv.p, F.p);
             TMG_CUDA(cudaStreamSynchronize(c->st));
         }
         DVec<int> status;
-        status.alloc(1);
+        status.alloc(2);
         status.zero(c->st);
         mf_factor<Tf>(c->st, *D, F.p, status.p);
-        int hs = 0;
-        TMG_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+        TMG_LAUNCH(k_count_nonpos<Tf>, nblk(D->ns), 256, 0, c->st, D->ns, D->sn_first, D->sn_row_ptr, D->front_off,
+                   F.p, status.p + 1);
+        int hs[2] = {0, 0};
+        TMG_CUDA(cudaMemcpyAsync(hs, status.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->st));
         TMG_CUDA(cudaStreamSynchronize(c->st));
-        if (hs) throw numeric_error("zero pivot in LDL^H factorisation at column " + std::to_string(hs - 1));
-        tb.alloc(std::max<int64_t>(1, sn_rows_total()));
+        if (hs[0]) throw numeric_error("zero pivot in LDL^H factorisation at column " + std::to_string(hs[0] - 1));
+        spd = hs[1] == 0;
+        int64_t last = 0;
+        TMG_CUDA(cudaMemcpy(&last, D->sn_row_ptr + D->ns, sizeof(int64_t), cudaMemcpyDeviceToHost));
+        tb.alloc(std::max<int64_t>(1, last));
         xw.alloc(n);
-        r.alloc(n);
-        d.alloc(n);
+        r.alloc(n); d.alloc(n); z.alloc(n); pp.alloc(n); q.alloc(n); sc.alloc(4);
         np.alloc(LZ_DOT_BLOCKS);
         nrm.alloc(2);
     }
-    int64_t sn_rows_total() const {
-        int64_t last = 0;
-        TMG_CUDA(cudaMemcpy(&last, D->sn_row_ptr + D->ns, sizeof(int64_t), cudaMemcpyDeviceToHost));
-        return last;
-    }
     void solve1(const Tv* b, Tv* x) {
-        mf_permute_in<Tf, Tv>(c->st, *D, b, xw.p, 1, n);
-        mf_solve<Tf>(c->st, *D, F.p, xw.p, tb.p);
-        mf_permute_out<Tf, Tv>(c->st, *D, xw.p, x, 1, n);
+        if (!gexec) {
+            const int64_t l0 = g_kernel_launches;
+            g_kernel_launches_delta = 0;
+            capture();
+            launches_per_solve = g_kernel_launches - l0;
+            g_kernel_launches = l0;
+        }
+        TMG_CUDA(cudaMemcpyAsync(gin.p, b, n * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
+        if (c->profile) {
+            if (!c->pev0) { TMG_CUDA(cudaEventCreate(&c->pev0)); TMG_CUDA(cudaEventCreate(&c->pev1)); }
+            TMG_CUDA(cudaEventRecord(c->pev0, c->st));
+        }
+        TMG_CUDA(cudaGraphLaunch(gexec, c->st));
+        if (c->profile) {
+            TMG_CUDA(cudaEventRecord(c->pev1, c->st));
+            TMG_CUDA(cudaEventSynchronize(c->pev1));
+            float ms = 0.f;
+            TMG_CUDA(cudaEventElapsedTime(&ms, c->pev0, c->pev1));
+            c->solve_ms += ms;
+            c->solve_count++;
+            // algorithmic bytes: every stored L entry read once per sweep direction, plus the
+            // solution vector read+written once per direction
+            c->solve_bytes += 2.0 * (double)D->l_entries * sizeof(Tf) + 4.0 * (double)n * sizeof(Tf);
+        }
+        g_kernel_launches += launches_per_solve;
+        TMG_CUDA(cudaMemcpyAsync(x, gout.p, n * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
+        solves++;
+    }
+    double norm2(const Tv* v) {
+        double h = 0.0;
+        lz_norm2<Tv>(c->st, n, v, np.p, nrm.p);
+        TMG_CUDA(cudaMemcpyAsync(&h, nrm.p, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+        TMG_CUDA(cudaStreamSynchronize(c->st));
+        return h;
     }
     void apply(const Tv* b, Tv* x) {
-        solve1(b, x);
-        if (!mixed) return;
-        const bool diag = diag_left > 0;
-        double bn = 0.0;
-        if (diag) {
-            lz_norm2<Tv>(c->st, n, b, np.p, nrm.p);
-            TMG_CUDA(cudaMemcpy(&bn, nrm.p, sizeof(double), cudaMemcpyDeviceToHost));
-        }
-        for (int it = 0; it < nref; it++) {
+        applies++;
+        if (!mixed) { solve1(b, x); return; }
+        const double bn = norm2(b);
+        const double tol2 = rtol * rtol * bn;
+        double rn = 0.0;
+        int it = 0;
+        if (spd) {
+            // CG on A x = b preconditioned by the FP32 factor; FP64 operator and vectors
+            TMG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(Tv), c->st));
             lz_copy<Tv>(c->st, n, b, r.p);
-            lz_spmv<Tv>(c->st, A, x, r.p, 1, n, true);
-            if (diag) {
-                double rn = 0.0;
-                lz_norm2<Tv>(c->st, n, r.p, np.p, nrm.p);
-                TMG_CUDA(cudaMemcpy(&rn, nrm.p, sizeof(double), cudaMemcpyDeviceToHost));
-                worst_refine = std::max(worst_refine, std::sqrt(rn / std::max(bn, 1e-300)));
+            solve1(r.p, z.p);
+            lz_copy<Tv>(c->st, n, z.p, pp.p);
+            lz_multidot<Tv>(c->st, n, r.p, n, 1, z.p, d.p, sc.p);        // rz
+            for (it = 1; it <= max_iter; it++) {
+                lz_spmv<Tv>(c->st, A, pp.p, q.p, 1, n);
+                lz_multidot<Tv>(c->st, n, pp.p, n, 1, q.p, d.p, sc.p + 1);  // pq
+                TMG_LAUNCH(k_pcg_xr<Tv>, nblk(n), 256, 0, c->st, n, x, r.p, pp.p, q.p, sc.p, sc.p + 1);
+                rn = norm2(r.p);
+                if (rn <= tol2) break;
+                solve1(r.p, z.p);
+                lz_multidot<Tv>(c->st, n, r.p, n, 1, z.p, d.p, sc.p + 2);  // rz_new
+                TMG_LAUNCH(k_pcg_p<Tv>, nblk(n), 256, 0, c->st, n, pp.p, z.p, sc.p + 2, sc.p);
+                TMG_CUDA(cudaMemcpyAsync(sc.p, sc.p + 2, sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
             }
-            solve1(r.p, d.p);
-            lz_axpy<Tv>(c->st, n, 1.0, d.p, x);
+        } else {
+            // plain iterative refinement with the FP64 residual
+            solve1(b, x);
+            for (it = 1; it <= max_iter; it++) {
+                lz_copy<Tv>(c->st, n, b, r.p);
+                lz_spmv<Tv>(c->st, A, x, r.p, 1, n, true);
+                rn = norm2(r.p);
+                if (rn <= tol2) break;
+                solve1(r.p, d.p);
+                lz_axpy<Tv>(c->st, n, 1.0, d.p, x);
+            }
         }
-        if (diag) {
-            double rn = 0.0;
-            lz_copy<Tv>(c->st, n, b, r.p);
-            lz_spmv<Tv>(c->st, A, x, r.p, 1, n, true);
-            lz_norm2<Tv>(c->st, n, r.p, np.p, nrm.p);
-            TMG_CUDA(cudaMemcpy(&rn, nrm.p, sizeof(double), cudaMemcpyDeviceToHost));
-            last_refine = std::sqrt(rn / std::max(bn, 1e-300));
-            diag_left--;
-        }
+        max_its = std::max<int64_t>(max_its, it);
+        worst_refine = std::max(worst_refine, std::sqrt(rn / std::max(bn, 1e-300)));
     }
-    double last_refine = 0.0;
 };
 
 template <typename Tv>
@@ -1187,7 +1313,7 @@ void run_problem(tmg_context* c, ResultHost& R, const OpSymbolic& os, const Unio
     DevCsr<Tv> A;
     A.nrows = um.U.ncols; A.nnz = um.U.nnz(); A.rowptr = um.csr_rowptr.p; A.col = um.csr_col.p; A.val = acsr.p;
     ShiftInvert<Tv, Tf> op;
-    op.c = c; op.D = &os.D; op.n = um.U.ncols; op.mixed = mixed; op.A = A;
+    op.c = c; op.D = &os.D; op.um = &um; op.n = um.U.ncols; op.mixed = mixed; op.A = A;
     auto t0 = std::chrono::steady_clock::now();
     op.factor(lower.p, nl);
     auto t1 = std::chrono::steady_clock::now();
@@ -1197,7 +1323,9 @@ void run_problem(tmg_context* c, ResultHost& R, const OpSymbolic& os, const Unio
     c->phase_ms[2] += std::chrono::duration<double, std::milli>(t2 - t1).count();
     R.converged = eo.converged;
     R.iterations = eo.restarts;
-    R.refine_residual = op.worst_refine > 0 ? std::max(op.worst_refine, op.last_refine) : op.last_refine;
+    R.refine_residual = op.worst_refine;
+    R.solves = op.solves;
+    R.applies = op.applies;
     if (!eo.converged && eo.ne == 0) { R.status = TMG_ERR_NUMERIC; return; }
     finish_result<Tv>(c, R, eo, nullptr, A, M, shift, nev_target, num_modes, min_frequency, is_degenerate, P);
     auto t3 = std::chrono::steady_clock::now();
@@ -1450,6 +1578,30 @@ int tmg_symbolic(tmg_context* c, int kind, int32_t* n, int32_t* perm, int32_t* p
     });
 }
 
+int tmg_symbolic_stats(tmg_context* c, int kind, double* out) {
+    if (!c || !out) return TMG_ERR_ARG;
+    if (!c->prepared) return set_err(c, TMG_ERR_STATE, "call tmg_prepare first");
+    return guarded(c, [&]() {
+        OpSymbolic* os = nullptr;
+        if (kind == 0) {
+            if (!c->symC.valid) analyze_op(c->symC, c->opC);
+            os = &c->symC;
+        } else if (kind == 1 || kind == 2) {
+            auto& RO = c->real[kind - 1];
+            if (!RO.valid) return set_err(c, TMG_ERR_STATE, "no such real harmonic");
+            if (!RO.sym.valid) analyze_op(RO.sym, RO.op);
+            os = &RO.sym;
+        } else {
+            return set_err(c, TMG_ERR_ARG, "unknown symbolic kind");
+        }
+        const Symbolic& S = os->S;
+        out[0] = S.n; out[1] = (double)S.nnz_l; out[2] = S.ns; out[3] = (double)S.level_ptr.size() - 1;
+        out[4] = S.max_front; out[5] = (double)S.front_entries(); out[6] = 4.0 * S.flops_real;
+        out[7] = (double)os->D.nlower;
+        return TMG_OK;
+    });
+}
+
 int tmg_solve_at_rpm(tmg_context* c, double rpm, int num_modes, const int32_t* harmonics, int nh, int coriolis,
                      double min_frequency, int precision, int32_t* num_results) {
     if (!c || !num_results) return TMG_ERR_ARG;
@@ -1458,6 +1610,10 @@ int tmg_solve_at_rpm(tmg_context* c, double rpm, int num_modes, const int32_t* h
     return guarded(c, [&]() {
         for (double& p : c->phase_ms) p = 0.0;
         const int64_t l0 = g_kernel_launches;
+        cudaEvent_t ev0, ev1;
+        TMG_CUDA(cudaEventCreate(&ev0));
+        TMG_CUDA(cudaEventCreate(&ev1));
+        TMG_CUDA(cudaEventRecord(ev0, c->st));
         const bool cor = coriolis != 0;
         if (!c->prepared || c->rpm != rpm || c->coriolis != (cor && rpm != 0.0)) prepare(c, rpm, cor);
         Sector& S = *c->sec;
@@ -1480,6 +1636,13 @@ int tmg_solve_at_rpm(tmg_context* c, double rpm, int num_modes, const int32_t* h
         std::sort(c->results.begin(), c->results.end(), [](const ResultHost& a, const ResultHost& b) { return a.k < b.k; });
         *num_results = (int32_t)c->results.size();
         c->launches = g_kernel_launches - l0;
+        TMG_CUDA(cudaEventRecord(ev1, c->st));
+        TMG_CUDA(cudaEventSynchronize(ev1));
+        float ms = 0.f;
+        TMG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        c->phase_ms[4] = ms;
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
         if (!firsterr.empty()) c->err = firsterr;
         return TMG_OK;
     });
@@ -1505,6 +1668,23 @@ int tmg_result_copy(tmg_context* c, int idx, double* freqs, double* shapes, int3
     if (freqs) std::copy(R.freqs.begin(), R.freqs.end(), freqs);
     if (whirl) std::copy(R.whirl.begin(), R.whirl.end(), whirl);
     if (shapes && !R.shapes.empty()) std::memcpy(shapes, R.shapes.data(), R.shapes.size() * sizeof(zd));
+    return TMG_OK;
+}
+
+int tmg_set_profiling(tmg_context* c, int on) {
+    if (!c) return TMG_ERR_ARG;
+    c->profile = on != 0;
+    c->solve_ms = 0.0;
+    c->solve_bytes = 0.0;
+    c->solve_count = 0;
+    return TMG_OK;
+}
+
+int tmg_profile_solve(tmg_context* c, double* out) {
+    if (!c || !out) return TMG_ERR_ARG;
+    out[0] = (double)c->solve_count;
+    out[1] = c->solve_ms;
+    out[2] = c->solve_bytes;
     return TMG_OK;
 }
 

@@ -86,6 +86,7 @@ struct UnionMaps {
     DVec<int64_t> csr_rowptr;
     DVec<int32_t> csr_col;
     DVec<int64_t> lower2csc;             // lower-triangle entry (CSC order) -> CSC entry
+    DVec<int32_t> low_row, low_col;      // (row, col) of every lower-triangle entry
     Pattern lower;
 };
 

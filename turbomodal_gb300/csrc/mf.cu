@@ -202,20 +202,45 @@ __global__ void __launch_bounds__(256) k_update(const int32_t* __restrict__ item
 }
 
 // ------------------------------------------------------------------------------------
-// Triangular solves: one CTA per supernode, levels processed in order.  tbuf holds a
-// length-m vector per front; its tail [w, m) carries the front's update to its parent.
+// Triangular solves, level by level.  Forward: gather the front vector (own entries +
+// children's update vectors, children in fixed order), then sweep 64-wide column blocks:
+// every CTA of a front re-solves the small diagonal block from the (final) block entries
+// and updates its own 256 rows below it, so a large front is spread over many CTAs and
+// the only sequential chain is the column-block loop.  Backward: off-diagonal products
+// with the ancestors' solution (warp per column), then column blocks from the last one,
+// each CTA re-solving the diagonal block and updating its own 8 columns to the left.
 template <typename T>
-__global__ void __launch_bounds__(256) k_fwd(const int32_t* __restrict__ lvl, const int32_t* __restrict__ sn_first,
-                                             const int64_t* __restrict__ sn_row_ptr, const int64_t* __restrict__ front_off,
-                                             const int32_t* __restrict__ child_ptr, const int32_t* __restrict__ child_list,
-                                             const int64_t* __restrict__ rel_ptr, const int32_t* __restrict__ rel,
-                                             const T* __restrict__ F, T* __restrict__ x, T* __restrict__ tbuf) {
+__device__ __forceinline__ T shfl_t(T v, int src) {
     using R = typename real_of<T>::type;
+    T o;
+    reinterpret_cast<R*>(&o)[0] = __shfl_sync(0xffffffff, reinterpret_cast<R*>(&v)[0], src);
+    if constexpr (sizeof(T) == 2 * sizeof(R))
+        reinterpret_cast<R*>(&o)[1] = __shfl_sync(0xffffffff, reinterpret_cast<R*>(&v)[1], src);
+    return o;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+    using R = typename real_of<T>::type;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        R* p = reinterpret_cast<R*>(&v);
+        p[0] += __shfl_xor_sync(0xffffffff, p[0], o);
+        if constexpr (sizeof(T) == 2 * sizeof(R)) p[1] += __shfl_xor_sync(0xffffffff, p[1], o);
+    }
+    return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fwd_gather(const int32_t* __restrict__ lvl, const int32_t* __restrict__ sn_first,
+                                                    const int64_t* __restrict__ sn_row_ptr, const int32_t* __restrict__ child_ptr,
+                                                    const int32_t* __restrict__ child_list, const int64_t* __restrict__ rel_ptr,
+                                                    const int32_t* __restrict__ rel, const T* __restrict__ x,
+                                                    T* __restrict__ tbuf) {
     const int s = lvl[blockIdx.x];
     const int f = sn_first[s];
     const int w = sn_first[s + 1] - f;
     const int64_t m = sn_row_ptr[s + 1] - sn_row_ptr[s];
-    const T* Fs = F + front_off[s];
     T* t = tbuf + sn_row_ptr[s];
     for (int64_t r = threadIdx.x; r < m; r += blockDim.x) t[r] = r < w ? x[f + r] : zero_of<T>();
     __syncthreads();
@@ -228,94 +253,154 @@ __global__ void __launch_bounds__(256) k_fwd(const int32_t* __restrict__ lvl, co
         for (int64_t a = threadIdx.x; a < mc - wc; a += blockDim.x) t[rl[a]] += tc[a];
         __syncthreads();
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int jb = 0; jb < w; jb += 32) {
-        const int nbb = min(32, w - jb);
-        if (warp == 0) {
-            T v = lane < nbb ? t[jb + lane] : zero_of<T>();
-            for (int j = 0; j < nbb; j++) {
-                T yj;
-                reinterpret_cast<R*>(&yj)[0] = __shfl_sync(0xffffffff, reinterpret_cast<R*>(&v)[0], j);
-                if constexpr (sizeof(T) == 2 * sizeof(R))
-                    reinterpret_cast<R*>(&yj)[1] = __shfl_sync(0xffffffff, reinterpret_cast<R*>(&v)[1], j);
-                if (lane > j && lane < nbb) v -= Fs[(int64_t)(jb + j) * m + jb + lane] * yj;
-            }
-            if (lane < nbb) t[jb + lane] = v;
-        }
-        __syncthreads();
-        for (int64_t r = jb + nbb + threadIdx.x; r < m; r += blockDim.x) {
-            T a = t[r];
-            for (int j = 0; j < nbb; j++) a -= Fs[(int64_t)(jb + j) * m + r] * t[jb + j];
-            t[r] = a;
-        }
-        __syncthreads();
-    }
-    for (int j = threadIdx.x; j < w; j += blockDim.x) x[f + j] = dev_div(t[j], re(Fs[(int64_t)j * m + j]));
 }
 
+// item = (s, row0): rows [row0, row0 + SV_RC) below the diagonal block of column block b
 template <typename T>
-__global__ void __launch_bounds__(256) k_bwd(const int32_t* __restrict__ lvl, const int32_t* __restrict__ sn_first,
-                                             const int64_t* __restrict__ sn_row_ptr, const int32_t* __restrict__ sn_rows,
-                                             const int64_t* __restrict__ front_off, const T* __restrict__ F,
-                                             T* __restrict__ x, T* __restrict__ tbuf) {
-    using R = typename real_of<T>::type;
-    const int s = lvl[blockIdx.x];
+__global__ void __launch_bounds__(256) k_fwd_block(const int32_t* __restrict__ items, int b,
+                                                   const int32_t* __restrict__ sn_first, const int64_t* __restrict__ sn_row_ptr,
+                                                   const int64_t* __restrict__ front_off, const T* __restrict__ F,
+                                                   T* __restrict__ x, T* __restrict__ tbuf) {
+    __shared__ T y[SV_B];
+    extern __shared__ unsigned char sv_smem[];
+    T (*Lb)[SV_B + 1] = reinterpret_cast<T (*)[SV_B + 1]>(sv_smem);
+    const int s = items[2 * blockIdx.x];
+    const int64_t row0 = items[2 * blockIdx.x + 1];
+    const int f = sn_first[s];
+    const int w = sn_first[s + 1] - f;
+    const int64_t m = sn_row_ptr[s + 1] - sn_row_ptr[s];
+    const int b0 = b * SV_B;
+    const int nbb = min(SV_B, w - b0);
+    const T* Fs = F + front_off[s];
+    T* t = tbuf + sn_row_ptr[s];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int q = threadIdx.x; q < SV_B * SV_B; q += blockDim.x) {
+        const int i = q % SV_B, j = q / SV_B;
+        if (i < nbb && j < i) Lb[i][j] = Fs[(int64_t)(b0 + j) * m + b0 + i];
+    }
+    if (threadIdx.x < nbb) y[threadIdx.x] = t[b0 + threadIdx.x];
+    __syncthreads();
+    if (warp == 0) {
+        // unit lower triangular solve of the diagonal block; lane owns rows lane, lane+32
+        T v0 = lane < nbb ? y[lane] : zero_of<T>();
+        T v1 = lane + 32 < nbb ? y[lane + 32] : zero_of<T>();
+        for (int j = 0; j < nbb; j++) {
+            const T yj = j < 32 ? shfl_t(v0, j) : shfl_t(v1, j - 32);
+            if (lane > j && lane < nbb) v0 -= Lb[lane][j] * yj;
+            if (lane + 32 > j && lane + 32 < nbb) v1 -= Lb[lane + 32][j] * yj;
+        }
+        if (lane < nbb) y[lane] = v0;
+        if (lane + 32 < nbb) y[lane + 32] = v1;
+    }
+    __syncthreads();
+    if (row0 == b0 + nbb)   // first chunk of this front stores the scaled block solution
+        for (int j = threadIdx.x; j < nbb; j += blockDim.x)
+            x[f + b0 + j] = dev_div(y[j], re(Fs[(int64_t)(b0 + j) * m + b0 + j]));
+    const int64_t r = row0 + threadIdx.x;
+    if (r < m && r < row0 + SV_RC) {
+        T a = t[r];
+        for (int j = 0; j < nbb; j++) a -= Fs[(int64_t)(b0 + j) * m + r] * y[j];
+        t[r] = a;
+    }
+}
+
+// item = (s, col0): z_j = x[f + j] - sum_{r >= w} conj(L(r, j)) x[rows[r]], j in [col0, col0+32)
+template <typename T>
+__global__ void __launch_bounds__(256) k_bwd_offdiag(const int32_t* __restrict__ items, const int32_t* __restrict__ sn_first,
+                                                     const int64_t* __restrict__ sn_row_ptr, const int32_t* __restrict__ sn_rows,
+                                                     const int64_t* __restrict__ front_off, const T* __restrict__ F,
+                                                     const T* __restrict__ x, T* __restrict__ tbuf) {
+    const int s = items[2 * blockIdx.x];
+    const int col0 = items[2 * blockIdx.x + 1];
     const int f = sn_first[s];
     const int w = sn_first[s + 1] - f;
     const int64_t m = sn_row_ptr[s + 1] - sn_row_ptr[s];
     const T* Fs = F + front_off[s];
     const int32_t* rows = sn_rows + sn_row_ptr[s];
     T* t = tbuf + sn_row_ptr[s];
-    for (int64_t r = threadIdx.x; r < m; r += blockDim.x) t[r] = r < w ? x[f + r] : x[rows[r]];
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    const int last = ((w - 1) / 32) * 32;
-    for (int jb = last; jb >= 0; jb -= 32) {
-        const int nbb = min(32, w - jb);
-        for (int j = jb + warp; j < jb + nbb; j += nwarp) {
-            T a = zero_of<T>();
-            for (int64_t r = jb + nbb + lane; r < m; r += 32) a += conj(Fs[(int64_t)j * m + r]) * t[r];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                R* ap = reinterpret_cast<R*>(&a);
-                ap[0] += __shfl_xor_sync(0xffffffff, ap[0], o);
-                if constexpr (sizeof(T) == 2 * sizeof(R)) ap[1] += __shfl_xor_sync(0xffffffff, ap[1], o);
-            }
-            if (lane == 0) t[j] -= a;
-        }
-        __syncthreads();
-        if (warp == 0) {
-            T v = lane < nbb ? t[jb + lane] : zero_of<T>();
-            for (int j = nbb - 1; j >= 0; j--) {
-                T yj;
-                reinterpret_cast<R*>(&yj)[0] = __shfl_sync(0xffffffff, reinterpret_cast<R*>(&v)[0], j);
-                if constexpr (sizeof(T) == 2 * sizeof(R))
-                    reinterpret_cast<R*>(&yj)[1] = __shfl_sync(0xffffffff, reinterpret_cast<R*>(&v)[1], j);
-                if (lane < j) v -= conj(Fs[(int64_t)(jb + lane) * m + jb + j]) * yj;
-            }
-            if (lane < nbb) t[jb + lane] = v;
-        }
-        __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int jj = warp; jj < SV_CC; jj += 8) {
+        const int j = col0 + jj;
+        if (j >= w) break;
+        T a = zero_of<T>();
+        for (int64_t r = w + lane; r < m; r += 32) a += conj(Fs[(int64_t)j * m + r]) * x[rows[r]];
+        a = warp_sum(a);
+        if (lane == 0) t[j] = x[f + j] - a;
     }
-    for (int j = threadIdx.x; j < w; j += blockDim.x) x[f + j] = t[j];
+}
+
+// item = (s, col0): solve L_bb^H x_b = z_b, then z_j -= sum_{r in b} conj(L(r, j)) x_r for
+// the CTA's columns j in [col0, col0+32), j < b0
+template <typename T>
+__global__ void __launch_bounds__(256) k_bwd_block(const int32_t* __restrict__ items, int b,
+                                                   const int32_t* __restrict__ sn_first, const int64_t* __restrict__ sn_row_ptr,
+                                                   const int64_t* __restrict__ front_off, const T* __restrict__ F,
+                                                   T* __restrict__ x, T* __restrict__ tbuf) {
+    __shared__ T xb[SV_B];
+    extern __shared__ unsigned char sv_smem[];
+    T (*Lb)[SV_B + 1] = reinterpret_cast<T (*)[SV_B + 1]>(sv_smem);
+    const int s = items[2 * blockIdx.x];
+    const int col0 = items[2 * blockIdx.x + 1];
+    const int f = sn_first[s];
+    const int w = sn_first[s + 1] - f;
+    const int64_t m = sn_row_ptr[s + 1] - sn_row_ptr[s];
+    const int b0 = b * SV_B;
+    const int nbb = min(SV_B, w - b0);
+    const T* Fs = F + front_off[s];
+    T* t = tbuf + sn_row_ptr[s];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int q = threadIdx.x; q < SV_B * SV_B; q += blockDim.x) {
+        const int i = q % SV_B, j = q / SV_B;
+        if (i < nbb && j < i) Lb[i][j] = Fs[(int64_t)(b0 + j) * m + b0 + i];
+    }
+    if (threadIdx.x < nbb) xb[threadIdx.x] = t[b0 + threadIdx.x];
+    __syncthreads();
+    if (warp == 0) {
+        T v0 = lane < nbb ? xb[lane] : zero_of<T>();
+        T v1 = lane + 32 < nbb ? xb[lane + 32] : zero_of<T>();
+        for (int j = nbb - 1; j >= 0; j--) {
+            const T yj = j < 32 ? shfl_t(v0, j) : shfl_t(v1, j - 32);
+            if (lane < j) v0 -= conj(Lb[j][lane]) * yj;
+            if (lane + 32 < j) v1 -= conj(Lb[j][lane + 32]) * yj;
+        }
+        if (lane < nbb) xb[lane] = v0;
+        if (lane + 32 < nbb) xb[lane + 32] = v1;
+    }
+    __syncthreads();
+    if (col0 == 0)
+        for (int j = threadIdx.x; j < nbb; j += blockDim.x) x[f + b0 + j] = xb[j];
+    for (int jj = warp; jj < SV_CC; jj += 8) {
+        const int j = col0 + jj;
+        if (j >= b0) break;
+        T a = zero_of<T>();
+        for (int r = lane; r < nbb; r += 32) a += conj(Fs[(int64_t)j * m + b0 + r]) * xb[r];
+        a = warp_sum(a);
+        if (lane == 0) t[j] -= a;
+    }
 }
 
 template <typename T, typename U>
 __global__ void k_perm_in(int n, const int32_t* __restrict__ perm, const U* __restrict__ b, T* __restrict__ x,
-                          int nvec, int64_t ldb) {
+                          int nvec, int64_t ldb, const double* __restrict__ scale) {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= (int64_t)n * nvec) return;
     const int64_t v = q / n, j = q % n;
-    x[v * n + j] = conv<T, U>(b[v * ldb + perm[j]]);
+    const int32_t o = perm[j];
+    U val = b[v * ldb + o];
+    if (scale) val = scale[o] * val;
+    x[v * n + j] = conv<T, U>(val);
 }
 
 template <typename T, typename U>
 __global__ void k_perm_out(int n, const int32_t* __restrict__ perm, const T* __restrict__ x, U* __restrict__ out,
-                           int nvec, int64_t ldo) {
+                           int nvec, int64_t ldo, const double* __restrict__ scale) {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= (int64_t)n * nvec) return;
     const int64_t v = q / n, j = q % n;
-    out[v * ldo + perm[j]] = conv<U, T>(x[v * n + j]);
+    const int32_t o = perm[j];
+    U val = conv<U, T>(x[v * n + j]);
+    if (scale) val = scale[o] * val;
+    out[v * ldo + o] = val;
 }
 
 // ------------------------------------------------------------------------------------
@@ -414,14 +499,61 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
         }
     }
     put(items, it);
+    // triangular-solve schedule
+    std::vector<int32_t> si;
+    solve_levels.assign(nlev, SolveLevel{});
+    for (int l = 0; l < nlev; l++) {
+        SolveLevel& L = solve_levels[l];
+        int maxw = 0;
+        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+            const int s = S.level_sn[q];
+            maxw = std::max(maxw, S.sn_first[s + 1] - S.sn_first[s]);
+        }
+        const int nbk = (maxw + SV_B - 1) / SV_B;
+        for (int b = 0; b < nbk; b++) {
+            L.fwd_off.push_back((int64_t)si.size());
+            int cnt = 0;
+            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                const int s = S.level_sn[q];
+                const int w = S.sn_first[s + 1] - S.sn_first[s];
+                if (w <= b * SV_B) continue;
+                const int64_t m = S.sn_row_ptr[s + 1] - S.sn_row_ptr[s];
+                const int64_t r0 = b * SV_B + std::min(SV_B, w - b * SV_B);
+                if (r0 >= m) { si.push_back(s); si.push_back((int32_t)r0); cnt++; continue; }
+                for (int64_t r = r0; r < m; r += SV_RC) { si.push_back(s); si.push_back((int32_t)r); cnt++; }
+            }
+            L.fwd_cnt.push_back(cnt);
+        }
+        L.off_items = (int64_t)si.size();
+        L.off_cnt = 0;
+        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+            const int s = S.level_sn[q];
+            const int w = S.sn_first[s + 1] - S.sn_first[s];
+            for (int c0 = 0; c0 < w; c0 += SV_CC) { si.push_back(s); si.push_back(c0); L.off_cnt++; }
+        }
+        for (int b = 0; b < nbk; b++) {
+            L.bwd_off.push_back((int64_t)si.size());
+            int cnt = 0;
+            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                const int s = S.level_sn[q];
+                const int w = S.sn_first[s + 1] - S.sn_first[s];
+                if (w <= b * SV_B) continue;
+                // col0 = 0 always present (it stores the block solution); then chunks left of b0
+                si.push_back(s); si.push_back(0); cnt++;
+                for (int c0 = SV_CC; c0 < b * SV_B; c0 += SV_CC) { si.push_back(s); si.push_back(c0); cnt++; }
+            }
+            L.bwd_cnt.push_back(cnt);
+        }
+    }
+    put(sitems, si);
 }
 
 void DevSymbolic::release() {
     for (void* p : {(void*)sn_first, (void*)sn_rows, (void*)rel, (void*)child_ptr, (void*)child_list,
                     (void*)sn_row_ptr, (void*)front_off, (void*)rel_ptr, (void*)perm, (void*)level_sn,
-                    (void*)items, (void*)dest, (void*)conj})
+                    (void*)items, (void*)dest, (void*)conj, (void*)sitems})
         if (p) cudaFree(p);
-    sn_first = sn_rows = rel = child_ptr = child_list = perm = level_sn = items = nullptr;
+    sn_first = sn_rows = rel = child_ptr = child_list = perm = level_sn = items = sitems = nullptr;
     sn_row_ptr = front_off = rel_ptr = dest = nullptr;
     conj = nullptr;
     bytes = 0;
@@ -467,33 +599,49 @@ void mf_factor(cudaStream_t st, const DevSymbolic& S, T* F, int* status) {
 template <typename T>
 void mf_solve(cudaStream_t st, const DevSymbolic& S, const T* F, T* x, T* tbuf) {
     const int nlev = (int)S.level_ptr.size() - 1;
+    static bool attr_set = false;
+    const size_t sv_smem = (size_t)SV_B * (SV_B + 1) * sizeof(T);
+    if (!attr_set) {
+        TMG_CUDA(cudaFuncSetAttribute(k_fwd_block<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sv_smem));
+        TMG_CUDA(cudaFuncSetAttribute(k_bwd_block<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sv_smem));
+        attr_set = true;
+    }
     for (int l = 0; l < nlev; l++) {
         const int cnt = S.level_ptr[l + 1] - S.level_ptr[l];
-        if (cnt)
-            TMG_LAUNCH(k_fwd<T>, cnt, 256, 0, st, S.level_sn + S.level_ptr[l], S.sn_first, S.sn_row_ptr, S.front_off,
-                       S.child_ptr, S.child_list, S.rel_ptr, S.rel, F, x, tbuf);
+        if (!cnt) continue;
+        TMG_LAUNCH(k_fwd_gather<T>, cnt, 256, 0, st, S.level_sn + S.level_ptr[l], S.sn_first, S.sn_row_ptr,
+                   S.child_ptr, S.child_list, S.rel_ptr, S.rel, x, tbuf);
+        const auto& L = S.solve_levels[l];
+        for (size_t b = 0; b < L.fwd_off.size(); b++)
+            if (L.fwd_cnt[b])
+                TMG_LAUNCH(k_fwd_block<T>, L.fwd_cnt[b], 256, sv_smem, st, S.sitems + L.fwd_off[b], (int)b, S.sn_first,
+                           S.sn_row_ptr, S.front_off, F, x, tbuf);
     }
     for (int l = nlev - 1; l >= 0; l--) {
-        const int cnt = S.level_ptr[l + 1] - S.level_ptr[l];
-        if (cnt)
-            TMG_LAUNCH(k_bwd<T>, cnt, 256, 0, st, S.level_sn + S.level_ptr[l], S.sn_first, S.sn_row_ptr, S.sn_rows,
-                       S.front_off, F, x, tbuf);
+        const auto& L = S.solve_levels[l];
+        if (L.off_cnt)
+            TMG_LAUNCH(k_bwd_offdiag<T>, L.off_cnt, 256, 0, st, S.sitems + L.off_items, S.sn_first, S.sn_row_ptr,
+                       S.sn_rows, S.front_off, F, x, tbuf);
+        for (int b = (int)L.bwd_off.size() - 1; b >= 0; b--)
+            if (L.bwd_cnt[b])
+                TMG_LAUNCH(k_bwd_block<T>, L.bwd_cnt[b], 256, sv_smem, st, S.sitems + L.bwd_off[b], b, S.sn_first,
+                           S.sn_row_ptr, S.front_off, F, x, tbuf);
     }
     TMG_CHECK_LAUNCH();
 }
 
 template <typename T, typename U>
-void mf_permute_in(cudaStream_t st, const DevSymbolic& S, const U* b, T* x, int nvec, int64_t ldb) {
+void mf_permute_in(cudaStream_t st, const DevSymbolic& S, const U* b, T* x, int nvec, int64_t ldb, const double* scale) {
     const int64_t tot = (int64_t)S.n * nvec;
     if (!tot) return;
-    TMG_LAUNCH((k_perm_in<T, U>), (unsigned)ceil_div(tot, 256), 256, 0, st, S.n, S.perm, b, x, nvec, ldb);
+    TMG_LAUNCH((k_perm_in<T, U>), (unsigned)ceil_div(tot, 256), 256, 0, st, S.n, S.perm, b, x, nvec, ldb, scale);
     TMG_CHECK_LAUNCH();
 }
 template <typename T, typename U>
-void mf_permute_out(cudaStream_t st, const DevSymbolic& S, const T* x, U* out, int nvec, int64_t ldo) {
+void mf_permute_out(cudaStream_t st, const DevSymbolic& S, const T* x, U* out, int nvec, int64_t ldo, const double* scale) {
     const int64_t tot = (int64_t)S.n * nvec;
     if (!tot) return;
-    TMG_LAUNCH((k_perm_out<T, U>), (unsigned)ceil_div(tot, 256), 256, 0, st, S.n, S.perm, x, out, nvec, ldo);
+    TMG_LAUNCH((k_perm_out<T, U>), (unsigned)ceil_div(tot, 256), 256, 0, st, S.n, S.perm, x, out, nvec, ldo, scale);
     TMG_CHECK_LAUNCH();
 }
 
@@ -505,13 +653,13 @@ TMG_INST(double)
 TMG_INST(float)
 TMG_INST(zd)
 TMG_INST(zf)
-template void mf_permute_in<double, double>(cudaStream_t, const DevSymbolic&, const double*, double*, int, int64_t);
-template void mf_permute_in<float, double>(cudaStream_t, const DevSymbolic&, const double*, float*, int, int64_t);
-template void mf_permute_out<float, double>(cudaStream_t, const DevSymbolic&, const float*, double*, int, int64_t);
-template void mf_permute_in<zd, zd>(cudaStream_t, const DevSymbolic&, const zd*, zd*, int, int64_t);
-template void mf_permute_in<zf, zd>(cudaStream_t, const DevSymbolic&, const zd*, zf*, int, int64_t);
-template void mf_permute_out<double, double>(cudaStream_t, const DevSymbolic&, const double*, double*, int, int64_t);
-template void mf_permute_out<zd, zd>(cudaStream_t, const DevSymbolic&, const zd*, zd*, int, int64_t);
-template void mf_permute_out<zf, zd>(cudaStream_t, const DevSymbolic&, const zf*, zd*, int, int64_t);
+template void mf_permute_in<double, double>(cudaStream_t, const DevSymbolic&, const double*, double*, int, int64_t, const double*);
+template void mf_permute_in<float, double>(cudaStream_t, const DevSymbolic&, const double*, float*, int, int64_t, const double*);
+template void mf_permute_out<float, double>(cudaStream_t, const DevSymbolic&, const float*, double*, int, int64_t, const double*);
+template void mf_permute_in<zd, zd>(cudaStream_t, const DevSymbolic&, const zd*, zd*, int, int64_t, const double*);
+template void mf_permute_in<zf, zd>(cudaStream_t, const DevSymbolic&, const zd*, zf*, int, int64_t, const double*);
+template void mf_permute_out<double, double>(cudaStream_t, const DevSymbolic&, const double*, double*, int, int64_t, const double*);
+template void mf_permute_out<zd, zd>(cudaStream_t, const DevSymbolic&, const zd*, zd*, int, int64_t, const double*);
+template void mf_permute_out<zf, zd>(cudaStream_t, const DevSymbolic&, const zf*, zd*, int, int64_t, const double*);
 
 }  // namespace tmg

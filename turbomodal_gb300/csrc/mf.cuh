@@ -12,6 +12,9 @@ namespace tmg {
 
 constexpr int MF_NB = 32;      // pivot block width
 constexpr int MF_TILE = 64;    // Schur-update tile
+constexpr int SV_B = 64;       // triangular-solve column block
+constexpr int SV_RC = 256;     // rows per CTA in the forward sweep
+constexpr int SV_CC = 32;      // columns per CTA (four per warp) in the backward sweeps
 
 // Device copy of a Symbolic plus the host-side launch schedule.
 struct DevSymbolic {
@@ -30,6 +33,16 @@ struct DevSymbolic {
         int32_t diag_cnt = 0, panel_cnt = 0, upd_cnt = 0, kb = 0;
     };
     std::vector<Step> steps;                   // in execution order
+    // triangular-solve schedule: per level, forward block sweeps (s, row0) and backward
+    // sweeps (s, col0), one list per column block
+    struct SolveLevel {
+        int64_t off_items = 0;                 // backward off-diagonal items (s, col0)
+        int32_t off_cnt = 0;
+        std::vector<int64_t> fwd_off, bwd_off;
+        std::vector<int32_t> fwd_cnt, bwd_cnt;
+    };
+    std::vector<SolveLevel> solve_levels;
+    int32_t* sitems = nullptr;
     std::vector<int32_t> level_ptr;            // host copy
     std::vector<int32_t> level_max_m;          // max front size per level
     int64_t* dest = nullptr;                   // scatter destination of operator lower entries
@@ -56,9 +69,13 @@ void mf_solve(cudaStream_t st, const DevSymbolic& S, const T* F, T* x, T* tbuf);
 
 // Permutation with precision conversion between the user vector (FP64) and the factor
 // numbering work vector.
+// scale (nullable, original numbering): x[j] = b[perm[j]] * scale[perm[j]] on the way in,
+// out[perm[j]] = x[j] * scale[perm[j]] on the way out.
 template <typename T, typename U>
-void mf_permute_in(cudaStream_t st, const DevSymbolic& S, const U* b, T* x, int nvec, int64_t ldb);
+void mf_permute_in(cudaStream_t st, const DevSymbolic& S, const U* b, T* x, int nvec, int64_t ldb,
+                   const double* scale = nullptr);
 template <typename T, typename U>
-void mf_permute_out(cudaStream_t st, const DevSymbolic& S, const T* x, U* out, int nvec, int64_t ldo);
+void mf_permute_out(cudaStream_t st, const DevSymbolic& S, const T* x, U* out, int nvec, int64_t ldo,
+                    const double* scale = nullptr);
 
 }  // namespace tmg

@@ -127,7 +127,16 @@ class CyclicSymmetrySolver:
         ph = np.zeros(8)
         nl = C.c_int64()
         self.ctx.L.tmg_last_timing(self.ctx.h, _lib.ptr(ph, C.c_double), 8, C.byref(nl))
-        return dict(prepare_ms=ph[0], factor_ms=ph[1], lanczos_ms=ph[2], post_ms=ph[3], kernel_launches=nl.value)
+        return dict(prepare_ms=ph[0], factor_ms=ph[1], lanczos_ms=ph[2], post_ms=ph[3], device_ms=ph[4],
+                    kernel_launches=nl.value)
+
+    def set_profiling(self, on: bool) -> None:
+        self.ctx.check(self.ctx.L.tmg_set_profiling(self.ctx.h, int(on)), "tmg_set_profiling")
+
+    def profile_solve(self) -> dict:
+        out = np.zeros(3)
+        self.ctx.check(self.ctx.L.tmg_profile_solve(self.ctx.h, _lib.ptr(out, C.c_double)), "tmg_profile_solve")
+        return dict(count=int(out[0]), ms=float(out[1]), bytes=float(out[2]))
 
     # --- matrices (parity / inspection) --------------------------------------------------
     def assemble(self, which: str, rpm: float = 0.0) -> sp.csc_matrix:
@@ -163,6 +172,13 @@ class CyclicSymmetrySolver:
         A = sp.csc_matrix((vals.copy(), i[: nnz.value], p), shape=(n.value, n.value))
         A.has_sorted_indices = True
         return A
+
+    def symbolic_stats(self, kind: int = 0) -> dict:
+        out = np.zeros(8)
+        self.ctx.check(self.ctx.L.tmg_symbolic_stats(self.ctx.h, kind, _lib.ptr(out, C.c_double)),
+                       "tmg_symbolic_stats")
+        keys = ["n", "nnz_l", "supernodes", "levels", "max_front", "front_entries", "flops", "lower_entries"]
+        return {k: float(v) for k, v in zip(keys, out)}
 
     def symbolic(self, kind: int = 0):
         """(AMD order, elimination tree, L column counts) of the shift-invert operator."""
