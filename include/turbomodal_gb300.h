@@ -119,9 +119,11 @@ int tmg_projection(tmg_context* ctx, int which, int k, int64_t* nnz, int32_t* n,
 int tmg_symbolic(tmg_context* ctx, int kind, int32_t* n, int32_t* perm, int32_t* parent,
                  int32_t* colcount);
 
-/* Size of the symbolic factorisation of kind (see tmg_symbolic): out[0] n, [1] nnz(L) of the
- * simplicial factor, [2] supernodes, [3] tree levels, [4] largest front, [5] front storage
- * entries, [6] factorisation flops (real, complex arithmetic counted x4), [7] lower entries. */
+/* Size of the symbolic factorisation of kind (see tmg_symbolic), 10 doubles: out[0] n, [1] nnz(L)
+ * of the simplicial factor, [2] supernodes, [3] tree levels, [4] largest front, [5] L-panel
+ * storage entries per problem, [6] factorisation flops (real; complex arithmetic counted x4),
+ * [7] operator lower-triangle entries, [8] update-block workspace entries per problem,
+ * [9] L entries read by one triangular solve. */
 int tmg_symbolic_stats(tmg_context* ctx, int kind, double* out);
 
 /* Full modal solve at one speed; replaces CyclicSymmetrySolver::solve_at_rpm

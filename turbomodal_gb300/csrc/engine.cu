@@ -173,58 +173,6 @@ __global__ void k_conv_copy(int64_t n, const U* __restrict__ a, T* __restrict__ 
     if (i < n) b[i] = conv<T, U>(a[i]);
 }
 
-// s_i = 1/sqrt(|Re a_ii|) from a CSR matrix (1 when the diagonal is absent or zero)
-template <typename T>
-__global__ void k_diag_scale(int32_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
-                             const T* __restrict__ v, double* __restrict__ s) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double d = 0.0;
-    for (int64_t q = rp[i]; q < rp[i + 1]; q++)
-        if (ci[q] == i) d = fabs(re(v[q]));
-    s[i] = d > 0.0 ? 1.0 / sqrt(d) : 1.0;
-}
-
-template <typename T, typename U>
-__global__ void k_scale_lower(int64_t n, const int32_t* __restrict__ row, const int32_t* __restrict__ col,
-                              const double* __restrict__ s, const U* __restrict__ v, T* __restrict__ out) {
-    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (q < n) out[q] = conv<T, U>((s[row[q]] * s[col[q]]) * v[q]);
-}
-
-// number of non-positive pivots of a factor (D on the front diagonals)
-template <typename T>
-__global__ void k_count_nonpos(int32_t ns, const int32_t* __restrict__ sn_first, const int64_t* __restrict__ sn_row_ptr,
-                               const int64_t* __restrict__ front_off, const T* __restrict__ F, int* __restrict__ cnt) {
-    const int32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= ns) return;
-    const int64_t m = sn_row_ptr[s + 1] - sn_row_ptr[s];
-    const int w = sn_first[s + 1] - sn_first[s];
-    int c = 0;
-    for (int j = 0; j < w; j++)
-        if (!(re(F[front_off[s] + (int64_t)j * m + j]) > 0)) c++;
-    if (c) atomicAdd(cnt, c);
-}
-
-template <typename T>
-__global__ void k_pcg_xr(int64_t n, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
-                         const T* __restrict__ q, const T* __restrict__ rz, const T* __restrict__ pq) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double a = re(rz[0]) / re(pq[0]);
-    x[i] += a * p[i];
-    r[i] -= a * q[i];
-}
-
-template <typename T>
-__global__ void k_pcg_p(int64_t n, T* __restrict__ p, const T* __restrict__ z, const T* __restrict__ rznew,
-                        const T* __restrict__ rz) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double b = re(rznew[0]) / re(rz[0]);
-    p[i] = z[i] + b * p[i];
-}
-
 template <typename T>
 __global__ void k_gather_i32(int64_t n, const int32_t* __restrict__ idx, const T* __restrict__ src, T* __restrict__ dst) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -396,7 +344,7 @@ struct tmg_context {
     FreeMat stat_free;
     OpSymbolic stat_sym;
     UnionMaps stat_union;
-    DVec<double> stat_F, stat_t, stat_x, stat_vals;
+    DVec<double> stat_L, stat_t, stat_x, stat_vals;
     std::vector<int32_t> stat_free_idx;     // free position -> reduced index
     DVec<int32_t> dstat_free_idx;
     DVec<double> u_static;
@@ -424,6 +372,11 @@ struct tmg_context {
     std::vector<ResultHost> results;
     double phase_ms[8] = {0};
     int64_t launches = 0;
+    // expansion maps (CSR of T(0), right-DOF flags, reduced -> free)
+    DVec<int64_t> dT0_rp;
+    DVec<int32_t> dT0_ci, d_r2free;
+    DVec<double> dT0_v;
+    DVec<uint8_t> d_isr;
     // profiling mode: CUDA-event timing of every triangular-solve graph launch
     bool profile = false;
     double solve_ms = 0.0, solve_bytes = 0.0;
@@ -624,6 +577,11 @@ void setup_sector(tmg_context* c, const tmg_sector_desc* d) {
         S->nptr.upload(np);
         S->nlist.upload(nl);
     }
+    c->dT0_rp.upload(S->T0t.p);
+    c->dT0_ci.upload(S->T0t.i);
+    c->dT0_v.upload(S->T0tv);
+    c->d_isr.upload(S->is_right);
+    c->d_r2free.upload(S->r2free);
     c->sec = std::move(S);
     c->have_KM = false;
     c->static_ready = false;
@@ -705,8 +663,11 @@ void ensure_static(tmg_context* c) {
     analyze_op(c->stat_sym, c->stat_union);
     // values -> fronts, factor (FP64 real)
     const DevSymbolic& D = c->stat_sym.D;
-    c->stat_F.alloc(D.front_entries);
-    c->stat_F.zero(c->st);
+    c->stat_L.alloc(D.l_entries);
+    c->stat_L.zero(c->st);
+    DVec<double> ustore;
+    ustore.alloc(D.u_entries);
+    const Batch<double> bt{1, c->stat_L.p, ustore.p, D.l_entries, D.u_entries};
     c->stat_vals.alloc(c->stat_union.lower2csc.n);
     DVec<double> full;
     full.alloc(c->stat_union.U.nnz());
@@ -715,16 +676,16 @@ void ensure_static(tmg_context* c) {
     if (c->stat_vals.n)
         TMG_LAUNCH(k_gather_t<double>, nblk(c->stat_vals.n), 256, 0, c->st, (int64_t)c->stat_vals.n,
                    c->stat_union.lower2csc.p, full.p, c->stat_vals.p);
-    mf_scatter<double>(c->st, D, c->stat_vals.p, c->stat_F.p);
+    mf_scatter<double>(c->st, D, bt, c->stat_vals.p);
     DVec<int> status;
     status.alloc(1);
     status.zero(c->st);
-    mf_factor<double>(c->st, D, c->stat_F.p, status.p);
+    mf_factor<double>(c->st, D, bt, status.p);
     int hs = 0;
     TMG_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     TMG_CUDA(cudaStreamSynchronize(c->st));
     if (hs) throw numeric_error("static prestress factorisation hit a zero pivot");
-    c->stat_t.alloc(std::max<int64_t>(1, D.ns ? (int64_t)c->stat_sym.S.sn_row_ptr.back() : 1));
+    c->stat_t.alloc(std::max<int64_t>(1, D.t_entries));
     c->stat_x.alloc(S.n_free);
     std::vector<int32_t> fr(S.free_reduced_map.begin(), S.free_reduced_map.end());
     c->dstat_free_idx.upload(fr);
@@ -751,9 +712,10 @@ void static_solve(tmg_context* c, double omega) {
     DVec<double> ff;
     ff.alloc(S.n_free);
     TMG_LAUNCH(k_gather_i32<double>, nblk(S.n_free), 256, 0, c->st, (int64_t)S.n_free, c->dstat_free_idx.p, Fc.p, ff.p);
-    mf_permute_in<double, double>(c->st, D, ff.p, c->stat_x.p, 1, S.n_free);
-    mf_solve<double>(c->st, D, c->stat_F.p, c->stat_x.p, c->stat_t.p);
-    mf_permute_out<double, double>(c->st, D, c->stat_x.p, ff.p, 1, S.n_free);
+    const Batch<double> bt{1, c->stat_L.p, nullptr, D.l_entries, 0};
+    mf_permute_in<double, double>(c->st, D, 1, ff.p, S.n_free, c->stat_x.p, nullptr);
+    mf_solve<double>(c->st, D, bt, c->stat_x.p, c->stat_t.p);
+    mf_permute_out<double, double>(c->st, D, 1, c->stat_x.p, ff.p, S.n_free, nullptr);
     uc.alloc(S.n_reduced);
     uc.zero(c->st);
     TMG_LAUNCH(k_scatter_vec<double>, nblk(S.n_free), 256, 0, c->st, (int64_t)S.n_free, c->dstat_free_idx.p, ff.p, uc.p);
@@ -907,16 +869,44 @@ void prepare(tmg_context* c, double rpm, bool coriolis) {
 
 namespace {
 
+// ---- batched kernels of the harmonic solves ---------------------------------------------
+// (Kc + P Kp) + conj(P) Kp^H per problem (phase p from ph[2p], ph[2p+1])
 __global__ void k_form_csum(int64_t n, const int64_t* __restrict__ ic, const int64_t* __restrict__ ip,
-                            const int64_t* __restrict__ ih, const double* __restrict__ c, const double* __restrict__ p,
-                            double Pr, double Pi, zd* __restrict__ out) {
+                            const int64_t* __restrict__ ih, const double* __restrict__ c, const double* __restrict__ pv,
+                            const double* __restrict__ ph, zd* __restrict__ out) {
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t p = blockIdx.y;
     if (e >= n) return;
     const double a = ic[e] >= 0 ? c[ic[e]] : 0.0;
-    const double b = ip[e] >= 0 ? p[ip[e]] : 0.0;
-    const double h = ih[e] >= 0 ? p[ih[e]] : 0.0;
-    const zd P{Pr, Pi}, Pc{Pr, -Pi};
-    out[e] = (zd{a, 0.0} + P * zd{b, 0.0}) + Pc * zd{h, 0.0};
+    const double b = ip[e] >= 0 ? pv[ip[e]] : 0.0;
+    const double h = ih[e] >= 0 ? pv[ih[e]] : 0.0;
+    const zd P{ph[2 * p], ph[2 * p + 1]}, Pc{ph[2 * p], -ph[2 * p + 1]};
+    out[p * n + e] = (zd{a, 0.0} + P * zd{b, 0.0}) + Pc * zd{h, 0.0};
+}
+
+// Complex harmonic operator on the union pattern, per problem:
+//   ((kc + P kp) + conj(P) kph) - sigma ((mc + P mp) + conj(P) mph)
+// with missing constituents read as exact zeros (the reference's sparse-sum semantics,
+// src/cyclic_solver.cpp:946-947, src/hermitian_lanczos.cpp:15).
+__global__ void k_form_complex(int64_t n, const int64_t* __restrict__ ikc, const int64_t* __restrict__ ikp,
+                               const int64_t* __restrict__ ikh, const int64_t* __restrict__ imc,
+                               const int64_t* __restrict__ imp, const int64_t* __restrict__ imh,
+                               const double* __restrict__ kc, const double* __restrict__ kp,
+                               const double* __restrict__ mc, const double* __restrict__ mp,
+                               const double* __restrict__ ph, double sigma, zd* __restrict__ out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t p = blockIdx.y;
+    if (e >= n) return;
+    const double a = ikc[e] >= 0 ? kc[ikc[e]] : 0.0;
+    const double b = ikp[e] >= 0 ? kp[ikp[e]] : 0.0;
+    const double c = ikh[e] >= 0 ? kp[ikh[e]] : 0.0;
+    const double am = imc[e] >= 0 ? mc[imc[e]] : 0.0;
+    const double bm = imp[e] >= 0 ? mp[imp[e]] : 0.0;
+    const double cm = imh[e] >= 0 ? mp[imh[e]] : 0.0;
+    const zd P{ph[2 * p], ph[2 * p + 1]}, Pc{ph[2 * p], -ph[2 * p + 1]};
+    const zd kk = (zd{a, 0.0} + P * zd{b, 0.0}) + Pc * zd{c, 0.0};
+    const zd mm = (zd{am, 0.0} + P * zd{bm, 0.0}) + Pc * zd{cm, 0.0};
+    out[p * n + e] = kk - sigma * mm;
 }
 
 // free-space degenerate duplication: column m <- src m/2, conjugated when m is odd
@@ -940,87 +930,163 @@ __global__ void k_resid(int64_t n, int nm, const T* __restrict__ AX, const T* __
     R[q] = kx - lam[m] * MX[q];
 }
 
+template <typename T>
+__global__ void k_gather_b(int64_t n, const int64_t* __restrict__ idx, const T* __restrict__ src, int64_t ss,
+                           T* __restrict__ dst, int64_t ds) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t p = blockIdx.y;
+    if (e < n) dst[p * ds + e] = src[p * ss + idx[e]];
+}
+
+// s_i = 1/sqrt(|Re a_ii|) per problem from a CSR matrix (1 when the diagonal is absent or zero)
+template <typename T>
+__global__ void k_diag_scale(int32_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                             const T* __restrict__ v, int64_t vs, double* __restrict__ s) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t p = blockIdx.y;
+    if (i >= n) return;
+    double d = 0.0;
+    for (int64_t q = rp[i]; q < rp[i + 1]; q++)
+        if (ci[q] == i) d = fabs(re(v[p * vs + q]));
+    s[p * n + i] = d > 0.0 ? 1.0 / sqrt(d) : 1.0;
+}
+
+template <typename T, typename U>
+__global__ void k_scale_lower(int64_t nl, int32_t n, const int32_t* __restrict__ row, const int32_t* __restrict__ col,
+                              const double* __restrict__ s, const U* __restrict__ v, T* __restrict__ out) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t p = blockIdx.y;
+    if (q < nl) out[p * nl + q] = conv<T, U>((s[p * n + row[q]] * s[p * n + col[q]]) * v[p * nl + q]);
+}
+
+template <typename T>
+__global__ void k_pcg_xr(int64_t n, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ pp,
+                         const T* __restrict__ q, const T* __restrict__ rz, const T* __restrict__ pq,
+                         const int* __restrict__ done) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t p = blockIdx.y;
+    if (i >= n || done[p]) return;
+    const double a = re(rz[p]) / re(pq[p]);
+    x[p * n + i] += a * pp[p * n + i];
+    r[p * n + i] -= a * q[p * n + i];
+}
+
+template <typename T>
+__global__ void k_pcg_p(int64_t n, T* __restrict__ pp, const T* __restrict__ z, const T* __restrict__ rznew,
+                        const T* __restrict__ rz, const int* __restrict__ done) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t p = blockIdx.y;
+    if (i >= n || done[p]) return;
+    const double b = re(rznew[p]) / re(rz[p]);
+    pp[p * n + i] = z[p * n + i] + b * pp[p * n + i];
+}
+
+template <typename T>
+__global__ void k_ir_update(int64_t n, T* __restrict__ x, const T* __restrict__ d, const int* __restrict__ done) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t p = blockIdx.y;
+    if (i >= n || done[p]) return;
+    x[p * n + i] += d[p * n + i];
+}
+
+template <typename T>
+__global__ void k_count_nonpos_dummy() {}
+
+// ---- shift-invert operator of a batch ----------------------------------------------------
 template <typename Tv, typename Tf>
-struct ShiftInvert {
+struct ShiftInvertB {
     tmg_context* c = nullptr;
     const DevSymbolic* D = nullptr;
     const UnionMaps* um = nullptr;
     int32_t n = 0;
+    int B = 1;
     bool mixed = false;
     bool spd = false;             // every pivot positive: CG-accelerated refinement
     int max_iter = 30;            // refinement iterations per solve (mixed)
     double rtol = 1e-12;          // relative residual target of a refined solve (mixed)
-    DevCsr<Tv> A;                 // FP64 operator K - sigma M (CSR)
-    DVec<Tf> F, tb, xw;
-    DVec<Tv> r, d, z, pp, q, sc;
+    DevCsr<Tv> A;                 // FP64 operator K - sigma M (CSR, per-problem values)
+    DVec<Tf> L, U, tb, xw;
+    DVec<Tv> gin, gout, r, d, z, pp, q, sc, bin;
     DVec<double> scale, np, nrm;
-    double worst_refine = 0.0;
+    DVec<int> ddone;
+    std::vector<double> worst;    // worst relative residual of a refined solve, per problem
+    std::vector<int> skip;        // problems finished or failed: refinement leaves them alone
+    std::vector<std::string> failed;   // per problem: why its factorisation failed ("" = fine)
     int64_t solves = 0, applies = 0, max_its = 0;
-    // the permute-in / supernodal sweeps / permute-out sequence of one solve is captured
-    // once into a CUDA graph over fixed buffers and replayed for every solve
-    DVec<Tv> gin, gout;
     cudaGraphExec_t gexec = nullptr;
-    ~ShiftInvert() { if (gexec) cudaGraphExecDestroy(gexec); }
+    int64_t launches_per_solve = 0;
+    ~ShiftInvertB() { if (gexec) cudaGraphExecDestroy(gexec); }
 
-    void capture() {
-        const double* s = mixed ? scale.p : nullptr;
-        gin.alloc(n);
-        gout.alloc(n);
-        cudaGraph_t g;
-        TMG_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-        mf_permute_in<Tf, Tv>(c->st, *D, gin.p, xw.p, 1, n, s);
-        mf_solve<Tf>(c->st, *D, F.p, xw.p, tb.p);
-        mf_permute_out<Tf, Tv>(c->st, *D, xw.p, gout.p, 1, n, s);
-        TMG_CUDA(cudaStreamEndCapture(c->st, &g));
-        TMG_CUDA(cudaGraphInstantiate(&gexec, g, 0));
-        TMG_CUDA(cudaGraphDestroy(g));
-        launches_per_solve = g_kernel_launches_delta;
-    }
-    int64_t launches_per_solve = 0, g_kernel_launches_delta = 0;
-
-    void factor(const Tv* lower_vals, int64_t nlower) {
-        F.alloc(D->front_entries);
-        F.zero(c->st);
+    void factor(const Tv* lower_vals) {
+        const int64_t nl = D->nlower;
+        L.alloc((size_t)B * D->l_entries);
+        U.alloc((size_t)B * std::max<int64_t>(D->u_entries, 1));
+        L.zero(c->st);
+        const Batch<Tf> bt{B, L.p, U.p, D->l_entries, D->u_entries};
         if constexpr (std::is_same<Tv, Tf>::value) {
-            mf_scatter<Tf>(c->st, *D, lower_vals, F.p);
+            mf_scatter<Tf>(c->st, *D, bt, lower_vals);
         } else {
-            scale.alloc(n);
-            TMG_LAUNCH(k_diag_scale<Tv>, nblk(n), 256, 0, c->st, n, A.rowptr, A.col, A.val, scale.p);
+            scale.alloc((size_t)B * n);
+            TMG_LAUNCH(k_diag_scale<Tv>, dim3(nblk(n), B), 256, 0, c->st, n, A.rowptr, A.col, A.val, A.vstride, scale.p);
             DVec<Tf> lv;
-            lv.alloc(nlower);
-            TMG_LAUNCH((k_scale_lower<Tf, Tv>), nblk(nlower), 256, 0, c->st, nlower, um->low_row.p, um->low_col.p,
+            lv.alloc((size_t)B * nl);
+            TMG_LAUNCH((k_scale_lower<Tf, Tv>), dim3(nblk(nl), B), 256, 0, c->st, nl, n, um->low_row.p, um->low_col.p,
                        scale.p, lower_vals, lv.p);
-            mf_scatter<Tf>(c->st, *D, lv.p, F.p);
+            mf_scatter<Tf>(c->st, *D, bt, lv.p);
             TMG_CUDA(cudaStreamSynchronize(c->st));
         }
         DVec<int> status;
-        status.alloc(2);
+        status.alloc(2 * B);
         status.zero(c->st);
-        mf_factor<Tf>(c->st, *D, F.p, status.p);
-        TMG_LAUNCH(k_count_nonpos<Tf>, nblk(D->ns), 256, 0, c->st, D->ns, D->sn_first, D->sn_row_ptr, D->front_off,
-                   F.p, status.p + 1);
-        int hs[2] = {0, 0};
-        TMG_CUDA(cudaMemcpyAsync(hs, status.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+        mf_factor<Tf>(c->st, *D, bt, status.p);
+        mf_count_nonpos<Tf>(c->st, *D, bt, status.p + B);
+        std::vector<int> hs(2 * B);
+        TMG_CUDA(cudaMemcpyAsync(hs.data(), status.p, 2 * B * sizeof(int), cudaMemcpyDeviceToHost, c->st));
         TMG_CUDA(cudaStreamSynchronize(c->st));
-        if (hs[0]) throw numeric_error("zero pivot in LDL^H factorisation at column " + std::to_string(hs[0] - 1));
-        spd = hs[1] == 0;
-        int64_t last = 0;
-        TMG_CUDA(cudaMemcpy(&last, D->sn_row_ptr + D->ns, sizeof(int64_t), cudaMemcpyDeviceToHost));
-        tb.alloc(std::max<int64_t>(1, last));
-        xw.alloc(n);
-        r.alloc(n); d.alloc(n); z.alloc(n); pp.alloc(n); q.alloc(n); sc.alloc(4);
-        np.alloc(LZ_DOT_BLOCKS);
-        nrm.alloc(2);
+        spd = true;
+        skip.assign(B, 0);
+        failed.assign(B, std::string());
+        int nfail = 0;
+        for (int p = 0; p < B; p++) {
+            if (hs[p]) {   // this problem fails alone; the rest of the batch goes on
+                failed[p] = "zero pivot in LDL^H factorisation at column " + std::to_string(hs[p] - 1);
+                skip[p] = 1;
+                nfail++;
+                continue;
+            }
+            if (hs[B + p]) spd = false;
+        }
+        if (nfail == B) throw numeric_error(failed[0]);
+        U.release();                  // the update workspace is only needed while factorising
+        tb.alloc((size_t)B * std::max<int64_t>(1, D->t_entries));
+        xw.alloc((size_t)B * n);
+        for (DVec<Tv>* v : {&gin, &gout, &r, &d, &z, &pp, &q}) v->alloc((size_t)B * n);
+        sc.alloc(4 * B);
+        np.alloc((size_t)B * LZ_DOT_BLOCKS);
+        nrm.alloc(B);
+        ddone.alloc(B);
+        worst.assign(B, 0.0);
     }
+    Batch<Tf> batch() const { return Batch<Tf>{B, L.p, nullptr, D->l_entries, 0}; }
+
+    // the permute / supernodal sweeps / permute sequence of one batched solve is captured
+    // once into a CUDA graph over fixed buffers and replayed for every solve
     void solve1(const Tv* b, Tv* x) {
+        const double* s = mixed ? scale.p : nullptr;
         if (!gexec) {
             const int64_t l0 = g_kernel_launches;
-            g_kernel_launches_delta = 0;
-            capture();
+            cudaGraph_t g;
+            TMG_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+            mf_permute_in<Tf, Tv>(c->st, *D, B, gin.p, n, xw.p, s);
+            mf_solve<Tf>(c->st, *D, batch(), xw.p, tb.p);
+            mf_permute_out<Tf, Tv>(c->st, *D, B, xw.p, gout.p, n, s);
+            TMG_CUDA(cudaStreamEndCapture(c->st, &g));
+            TMG_CUDA(cudaGraphInstantiate(&gexec, g, 0));
+            TMG_CUDA(cudaGraphDestroy(g));
             launches_per_solve = g_kernel_launches - l0;
             g_kernel_launches = l0;
         }
-        TMG_CUDA(cudaMemcpyAsync(gin.p, b, n * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
+        TMG_CUDA(cudaMemcpyAsync(gin.p, b, (size_t)B * n * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
         if (c->profile) {
             if (!c->pev0) { TMG_CUDA(cudaEventCreate(&c->pev0)); TMG_CUDA(cudaEventCreate(&c->pev1)); }
             TMG_CUDA(cudaEventRecord(c->pev0, c->st));
@@ -1034,59 +1100,77 @@ struct ShiftInvert {
             c->solve_ms += ms;
             c->solve_count++;
             // algorithmic bytes: every stored L entry read once per sweep direction, plus the
-            // solution vector read+written once per direction
-            c->solve_bytes += 2.0 * (double)D->l_entries * sizeof(Tf) + 4.0 * (double)n * sizeof(Tf);
+            // solution vector read and written once per direction, for each problem
+            c->solve_bytes += (double)B * (2.0 * (double)D->l_stored * sizeof(Tf) + 4.0 * (double)n * sizeof(Tf));
         }
         g_kernel_launches += launches_per_solve;
-        TMG_CUDA(cudaMemcpyAsync(x, gout.p, n * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
+        TMG_CUDA(cudaMemcpyAsync(x, gout.p, (size_t)B * n * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
         solves++;
     }
-    double norm2(const Tv* v) {
-        double h = 0.0;
-        lz_norm2<Tv>(c->st, n, v, np.p, nrm.p);
-        TMG_CUDA(cudaMemcpyAsync(&h, nrm.p, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    std::vector<double> norms(const Tv* v) {
+        std::vector<double> h(B);
+        lz_norm2<Tv>(c->st, B, n, v, n, np.p, nrm.p);
+        TMG_CUDA(cudaMemcpyAsync(h.data(), nrm.p, B * sizeof(double), cudaMemcpyDeviceToHost, c->st));
         TMG_CUDA(cudaStreamSynchronize(c->st));
         return h;
     }
-    void apply(const Tv* b, Tv* x) {
+    // x = (K - sigma M)^-1 b for every problem of the batch; problem p's right-hand side
+    // starts at b + p * bs, its solution at x + p * n
+    void apply(const Tv* b, int64_t bs, Tv* x) {
         applies++;
+        if (bs != n) {
+            if (!bin.p) bin.alloc((size_t)B * n);
+            TMG_CUDA(cudaMemcpy2DAsync(bin.p, n * sizeof(Tv), b, bs * sizeof(Tv), n * sizeof(Tv), B,
+                                       cudaMemcpyDeviceToDevice, c->st));
+            b = bin.p;
+        }
         if (!mixed) { solve1(b, x); return; }
-        const double bn = norm2(b);
-        const double tol2 = rtol * rtol * bn;
-        double rn = 0.0;
+        const std::vector<double> bn = norms(b);
+        std::vector<int> done(skip);
+        std::vector<double> rn;
+        TMG_CUDA(cudaMemcpyAsync(ddone.p, done.data(), B * sizeof(int), cudaMemcpyHostToDevice, c->st));
         int it = 0;
+        auto check = [&]() {
+            rn = norms(r.p);
+            bool all = true, changed = false;
+            for (int p = 0; p < B; p++) {
+                if (!done[p] && rn[p] <= rtol * rtol * bn[p]) { done[p] = 1; changed = true; }
+                all = all && done[p];
+            }
+            if (changed) TMG_CUDA(cudaMemcpyAsync(ddone.p, done.data(), B * sizeof(int), cudaMemcpyHostToDevice, c->st));
+            return all;
+        };
         if (spd) {
             // CG on A x = b preconditioned by the FP32 factor; FP64 operator and vectors
-            TMG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(Tv), c->st));
-            lz_copy<Tv>(c->st, n, b, r.p);
+            TMG_CUDA(cudaMemsetAsync(x, 0, (size_t)B * n * sizeof(Tv), c->st));
+            lz_copy<Tv>(c->st, (int64_t)B * n, b, r.p);
             solve1(r.p, z.p);
-            lz_copy<Tv>(c->st, n, z.p, pp.p);
-            lz_multidot<Tv>(c->st, n, r.p, n, 1, z.p, d.p, sc.p);        // rz
+            lz_copy<Tv>(c->st, (int64_t)B * n, z.p, pp.p);
+            lz_multidot<Tv>(c->st, B, n, r.p, n, n, 1, z.p, n, d.p, sc.p);           // rz
             for (it = 1; it <= max_iter; it++) {
-                lz_spmv<Tv>(c->st, A, pp.p, q.p, 1, n);
-                lz_multidot<Tv>(c->st, n, pp.p, n, 1, q.p, d.p, sc.p + 1);  // pq
-                TMG_LAUNCH(k_pcg_xr<Tv>, nblk(n), 256, 0, c->st, n, x, r.p, pp.p, q.p, sc.p, sc.p + 1);
-                rn = norm2(r.p);
-                if (rn <= tol2) break;
+                lz_spmv<Tv>(c->st, B, A, pp.p, n, q.p, n, 1, n);
+                lz_multidot<Tv>(c->st, B, n, pp.p, n, n, 1, q.p, n, d.p, sc.p + B);   // pq
+                TMG_LAUNCH(k_pcg_xr<Tv>, dim3(nblk(n), B), 256, 0, c->st, n, x, r.p, pp.p, q.p, sc.p, sc.p + B, ddone.p);
+                if (check()) break;
                 solve1(r.p, z.p);
-                lz_multidot<Tv>(c->st, n, r.p, n, 1, z.p, d.p, sc.p + 2);  // rz_new
-                TMG_LAUNCH(k_pcg_p<Tv>, nblk(n), 256, 0, c->st, n, pp.p, z.p, sc.p + 2, sc.p);
-                TMG_CUDA(cudaMemcpyAsync(sc.p, sc.p + 2, sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
+                lz_multidot<Tv>(c->st, B, n, r.p, n, n, 1, z.p, n, d.p, sc.p + 2 * B);  // rz_new
+                TMG_LAUNCH(k_pcg_p<Tv>, dim3(nblk(n), B), 256, 0, c->st, n, pp.p, z.p, sc.p + 2 * B, sc.p, ddone.p);
+                TMG_CUDA(cudaMemcpyAsync(sc.p, sc.p + 2 * B, B * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
             }
         } else {
             // plain iterative refinement with the FP64 residual
             solve1(b, x);
             for (it = 1; it <= max_iter; it++) {
-                lz_copy<Tv>(c->st, n, b, r.p);
-                lz_spmv<Tv>(c->st, A, x, r.p, 1, n, true);
-                rn = norm2(r.p);
-                if (rn <= tol2) break;
+                lz_copy<Tv>(c->st, (int64_t)B * n, b, r.p);
+                lz_spmv<Tv>(c->st, B, A, x, n, r.p, n, 1, n, true);
+                if (check()) break;
                 solve1(r.p, d.p);
-                lz_axpy<Tv>(c->st, n, 1.0, d.p, x);
+                TMG_LAUNCH(k_ir_update<Tv>, dim3(nblk(n), B), 256, 0, c->st, n, x, d.p, ddone.p);
             }
         }
         max_its = std::max<int64_t>(max_its, it);
-        worst_refine = std::max(worst_refine, std::sqrt(rn / std::max(bn, 1e-300)));
+        for (int p = 0; p < B; p++)
+            if (!skip[p]) worst[p] = std::max(worst[p], std::sqrt(rn[p] / std::max(bn[p], 1e-300)));
     }
 };
 
@@ -1095,7 +1179,8 @@ struct EigOut {
     std::vector<double> lam;
     DVec<Tv> X;                 // n x ne
     int ne = 0, restarts = 0;
-    bool converged = false;
+    bool converged = false, done = false;
+    std::string failed;         // non-empty: the problem stopped with this error
 };
 
 template <typename Tv> Tv rnd_entry(std::mt19937& g, std::normal_distribution<double>& d);
@@ -1106,121 +1191,133 @@ template <> zd rnd_entry<zd>(std::mt19937& g, std::normal_distribution<double>& 
     return zd{a, b};
 }
 
-// Shift-invert Lanczos (src/hermitian_lanczos.cpp:264-460) with device-resident basis and
-// scalars; the host only reads the converged count after each restart cycle.
+// Shift-invert Lanczos (src/hermitian_lanczos.cpp:264-460) for a batch in lockstep, with
+// device-resident bases and scalars; the host reads the converged counts after each
+// restart cycle and extracts every problem as soon as it has converged.
 template <typename Tv, typename Tf>
-EigOut<Tv> lanczos(tmg_context* c, ShiftInvert<Tv, Tf>& op, const DevCsr<Tv>& M, int nev, int ncv, double shift,
-                   double tol, int max_restarts) {
+std::vector<EigOut<Tv>> lanczos(tmg_context* c, ShiftInvertB<Tv, Tf>& op, const DevCsr<Tv>& M, int nev, int ncv,
+                                double shift, double tol, int max_restarts) {
     const int64_t n = op.n;
+    const int B = op.B;
     cudaStream_t st = c->st;
+    const int64_t vs = (int64_t)(ncv + 1) * n;
     DVec<Tv> V, MV, w, Mw, h, dot, part;
-    V.alloc((size_t)(ncv + 1) * n); MV.alloc((size_t)(ncv + 1) * n);
+    V.alloc((size_t)B * vs); MV.alloc((size_t)B * vs);
     V.zero(st); MV.zero(st);
-    w.alloc(n); Mw.alloc(n); h.alloc(ncv + 1); dot.alloc(1); part.alloc((size_t)LZ_DOT_BLOCKS * (ncv + 1));
+    w.alloc((size_t)B * n); Mw.alloc((size_t)B * n); h.alloc((size_t)B * (ncv + 1)); dot.alloc(B);
+    part.alloc((size_t)B * LZ_DOT_BLOCKS * (ncv + 1));
     DVec<double> alpha, beta, theta, lam, S, Z, Q, rot;
-    alpha.alloc(ncv); beta.alloc(ncv); theta.alloc(ncv); lam.alloc(ncv);
-    S.alloc((size_t)ncv * ncv); Z.alloc((size_t)ncv * ncv); Q.alloc((size_t)ncv * ncv);
-    rot.alloc((size_t)2 * std::max(1, ncv - nev) * std::max(1, ncv - 1));
+    alpha.alloc((size_t)B * ncv); beta.alloc((size_t)B * ncv); theta.alloc((size_t)B * ncv); lam.alloc((size_t)B * ncv);
+    S.alloc((size_t)B * ncv * ncv); Z.alloc((size_t)B * ncv * ncv); Q.alloc((size_t)B * ncv * ncv);
+    const int64_t rs = (int64_t)2 * std::max(1, ncv - nev) * std::max(1, ncv - 1);
+    rot.alloc((size_t)B * rs);
     alpha.zero(st); beta.zero(st);
     DVec<int> order, nconv, flag;
-    order.alloc(ncv); nconv.alloc(1); flag.alloc(1);
+    order.alloc((size_t)B * ncv); nconv.alloc(B); flag.alloc(B);
     flag.zero(st);
     {
         std::mt19937 gen(42);
         std::normal_distribution<double> dist(0.0, 1.0);
         std::vector<Tv> v0(n);
         for (int64_t i = 0; i < n; i++) v0[i] = rnd_entry<Tv>(gen, dist);
-        TMG_CUDA(cudaMemcpy(V.p, v0.data(), n * sizeof(Tv), cudaMemcpyHostToDevice));
-        lz_spmv<Tv>(st, M, V.p, MV.p, 1, n);
-        lz_multidot<Tv>(st, n, V.p, n, 1, MV.p, part.p, dot.p);
-        lz_scale_cols<Tv>(st, n, dot.p, V.p, MV.p);
+        for (int p = 0; p < B; p++)
+            TMG_CUDA(cudaMemcpy(V.p + p * vs, v0.data(), n * sizeof(Tv), cudaMemcpyHostToDevice));
+        lz_spmv<Tv>(st, B, M, V.p, vs, MV.p, vs, 1, n);
+        lz_multidot<Tv>(st, B, n, V.p, vs, n, 1, MV.p, vs, part.p, dot.p);
+        lz_scale_first<Tv>(st, B, n, dot.p, V.p, MV.p, vs);
     }
-    EigOut<Tv> out;
-    int m = ncv;
-    for (int restart = 0; restart <= max_restarts; restart++) {
+    std::vector<EigOut<Tv>> out(B);
+    const int m = ncv;
+    int remaining = B;
+    for (int p = 0; p < B; p++)
+        if (!op.failed[p].empty()) { out[p].failed = op.failed[p]; out[p].done = true; remaining--; }
+    for (int restart = 0; restart <= max_restarts && remaining > 0; restart++) {
         const int j0 = restart == 0 ? 0 : nev;
         for (int j = j0; j < m; j++) {
-            Tv* Vj = V.p + (int64_t)j * n;
-            Tv* MVj = MV.p + (int64_t)j * n;
-            op.apply(MVj, w.p);
-            lz_multidot<Tv>(st, n, MVj, n, 1, w.p, part.p, dot.p);
-            lz_three_term_dot<Tv>(st, n, j, dot.p, alpha.p, beta.p, V.p, w.p);
-            lz_multidot<Tv>(st, n, MV.p, n, j + 1, w.p, part.p, h.p);
-            lz_gemv_sub<Tv>(st, n, j + 1, V.p, h.p, w.p);
-            lz_spmv<Tv>(st, M, w.p, Mw.p, 1, n);
-            lz_multidot<Tv>(st, n, w.p, n, 1, Mw.p, part.p, dot.p);
-            lz_beta_scale<Tv>(st, n, j, dot.p, w.p, Mw.p, V.p, MV.p, beta.p, flag.p);
-            (void)Vj;
+            op.apply(MV.p + (int64_t)j * n, vs, w.p);
+            lz_multidot<Tv>(st, B, n, MV.p + (int64_t)j * n, vs, n, 1, w.p, n, part.p, dot.p);
+            lz_three_term<Tv>(st, B, n, j, dot.p, alpha.p, beta.p, ncv, V.p, vs, w.p, n);
+            lz_multidot<Tv>(st, B, n, MV.p, vs, n, j + 1, w.p, n, part.p, h.p);
+            lz_gemv_sub<Tv>(st, B, n, j + 1, V.p, vs, h.p, j + 1, w.p, n);
+            lz_spmv<Tv>(st, B, M, w.p, n, Mw.p, n, 1, n);
+            lz_multidot<Tv>(st, B, n, w.p, n, n, 1, Mw.p, n, part.p, dot.p);
+            lz_beta_scale<Tv>(st, B, n, j, dot.p, w.p, Mw.p, n, V.p, MV.p, vs, beta.p, ncv, flag.p);
         }
-        int hflag = 0;
-        TMG_CUDA(cudaMemcpyAsync(&hflag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        std::vector<int> hflag(B), hn(B);
+        TMG_CUDA(cudaMemcpyAsync(hflag.data(), flag.p, B * sizeof(int), cudaMemcpyDeviceToHost, st));
         TMG_CUDA(cudaStreamSynchronize(st));
-        if (hflag) throw numeric_error("Lanczos breakdown (beta < 1e-14) at step " + std::to_string(hflag - 1));
-        lz_tridiag(st, m, nev, shift, tol, alpha.p, beta.p, theta.p, S.p, lam.p, order.p, nconv.p, Z.p);
-        int hn = 0;
-        TMG_CUDA(cudaMemcpyAsync(&hn, nconv.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        for (int p = 0; p < B; p++)
+            if (hflag[p] && !out[p].done) {   // this problem stops alone; the batch goes on
+                out[p].failed = "Lanczos breakdown (beta < 1e-14) at step " + std::to_string(hflag[p] - 1);
+                out[p].done = true;
+                op.skip[p] = 1;
+                remaining--;
+            }
+        if (remaining == 0) break;
+        lz_tridiag(st, B, m, ncv, nev, shift, tol, alpha.p, beta.p, theta.p, S.p, lam.p, order.p, nconv.p, Z.p);
+        TMG_CUDA(cudaMemcpyAsync(hn.data(), nconv.p, B * sizeof(int), cudaMemcpyDeviceToHost, st));
         TMG_CUDA(cudaStreamSynchronize(st));
-        out.restarts = restart;
-        if (hn >= nev || restart == max_restarts) {
-            int ne = std::min(hn > 0 ? hn : nev, m);
+        for (int p = 0; p < B; p++) {
+            if (out[p].done) continue;
+            out[p].restarts = restart;
+            if (!(hn[p] >= nev || restart == max_restarts)) continue;
+            int ne = std::min(hn[p] > 0 ? hn[p] : nev, m);
             ne = std::min(ne, nev);
-            std::vector<double> Sh = S.download(), lh = lam.download();
-            std::vector<int> oh = order.download();
+            std::vector<double> Sh((size_t)m * m), lh(m);
+            std::vector<int> oh(m);
+            TMG_CUDA(cudaMemcpy(Sh.data(), S.p + (int64_t)p * ncv * ncv, Sh.size() * sizeof(double), cudaMemcpyDeviceToHost));
+            TMG_CUDA(cudaMemcpy(lh.data(), lam.p + (int64_t)p * ncv, m * sizeof(double), cudaMemcpyDeviceToHost));
+            TMG_CUDA(cudaMemcpy(oh.data(), order.p + (int64_t)p * ncv, m * sizeof(int), cudaMemcpyDeviceToHost));
             std::vector<double> Csel((size_t)m * ne);
-            out.lam.resize(ne);
+            out[p].lam.resize(ne);
             for (int t = 0; t < ne; t++) {
-                out.lam[t] = lh[oh[t]];
+                out[p].lam[t] = lh[oh[t]];
                 for (int k = 0; k < m; k++) Csel[(size_t)t * m + k] = Sh[(size_t)oh[t] * m + k];
             }
             DVec<double> dC;
             dC.upload(Csel);
-            out.X.alloc((size_t)n * std::max(ne, 1));
-            lz_gemm_real<Tv>(st, n, m, ne, V.p, dC.p, m, out.X.p);
+            out[p].X.alloc((size_t)n * std::max(ne, 1));
+            lz_gemm_real<Tv>(st, 1, n, m, ne, V.p + p * vs, 0, dC.p, 0, m, out[p].X.p, 0);
             TMG_CUDA(cudaStreamSynchronize(st));
-            out.ne = ne;
-            out.converged = hn >= nev;
-            return out;
+            out[p].ne = ne;
+            out[p].converged = hn[p] >= nev;
+            out[p].done = true;
+            op.skip[p] = 1;
+            remaining--;
         }
-        // implicit restart (src/hermitian_lanczos.cpp:114-260)
-        lz_restart_qr(st, m, nev, theta.p, alpha.p, beta.p, Q.p, rot.p);
+        if (remaining == 0) break;
+        // implicit restart (src/hermitian_lanczos.cpp:114-260) for the whole batch
+        lz_restart_qr(st, B, m, ncv, nev, theta.p, alpha.p, beta.p, Q.p, rot.p, rs);
         DVec<Tv> Y;
-        Y.alloc((size_t)n * (nev + 1));
-        lz_gemm_real<Tv>(st, n, m, nev + 1, V.p, Q.p, m, Y.p);
-        lz_combine_f<Tv>(st, n, Y.p + (int64_t)nev * n, V.p + (int64_t)m * n, beta.p, nev, m, Q.p, w.p);
-        lz_copy<Tv>(st, (int64_t)nev * n, Y.p, V.p);
-        lz_spmv<Tv>(st, M, w.p, Mw.p, 1, n);
-        lz_multidot<Tv>(st, n, w.p, n, 1, Mw.p, part.p, dot.p);
-        TMG_LAUNCH(k_restart_norm<Tv>, nblk(n), 256, 0, st, n, nev, dot.p, w.p, Mw.p, V.p, MV.p, beta.p);
-        lz_spmv<Tv>(st, M, V.p, MV.p, nev, n);
-        TMG_CHECK_LAUNCH();
+        Y.alloc((size_t)B * n * (nev + 1));
+        const int64_t yst = (int64_t)n * (nev + 1);
+        lz_gemm_real<Tv>(st, B, n, m, nev + 1, V.p, vs, Q.p, (int64_t)ncv * ncv, m, Y.p, yst);
+        lz_combine_f<Tv>(st, B, n, Y.p + (int64_t)nev * n, yst, V.p + (int64_t)m * n, vs, beta.p, ncv, nev, m, Q.p, w.p, n);
+        for (int p = 0; p < B; p++) lz_copy<Tv>(st, (int64_t)nev * n, Y.p + p * yst, V.p + p * vs);
+        lz_spmv<Tv>(st, B, M, w.p, n, Mw.p, n, 1, n);
+        lz_multidot<Tv>(st, B, n, w.p, n, n, 1, Mw.p, n, part.p, dot.p);
+        lz_restart_norm<Tv>(st, B, n, nev, dot.p, w.p, Mw.p, n, V.p, MV.p, vs, beta.p, ncv);
+        lz_spmv<Tv>(st, B, M, V.p, vs, MV.p, vs, nev, n);
     }
     return out;
 }
 
-}  // namespace
-
-namespace {
-
-struct CsrHost {
-    DVec<int64_t> rp;
-    DVec<int32_t> ci;
-    DVec<int64_t> perm;     // CSR position -> CSC entry of the source values
+struct Problem {
+    int k = 0;
+    zd P{1.0, 0.0};
+    bool degenerate = false;
+    int nev_target = 0;
+    ResultHost* R = nullptr;
 };
 
-void csr_of(const Pattern& P, CsrHost& out) {
-    std::vector<int64_t> map;
-    Pattern t = transpose_map(P, map);
-    out.rp.upload(t.p);
-    out.ci.upload(t.i);
-    out.perm.upload(map);
-}
-
+// Post-processing of one problem (cyclic_solver.cpp:1058-1211): frequencies, min-frequency
+// filter, truncation, residual diagnostic, degenerate duplication, expansion to the full
+// sector DOFs.
 template <typename Tv>
-void finish_result(tmg_context* c, ResultHost& R, EigOut<Tv>& eo, ShiftInvert<Tv, Tv>* dummy, const DevCsr<Tv>& A,
-                   const DevCsr<Tv>& M, double shift, int nev_target, int num_modes, double min_frequency,
-                   bool is_degenerate, zd P) {
-    (void)dummy;
+void finish_result(tmg_context* c, const Problem& pr, EigOut<Tv>& eo, const DevCsr<Tv>& A, const DevCsr<Tv>& M,
+                   double shift, int num_modes, double min_frequency) {
     Sector& S = *c->sec;
+    ResultHost& R = *pr.R;
     cudaStream_t st = c->st;
     const int64_t n = S.n_free;
     std::vector<int> keep;
@@ -1231,7 +1328,7 @@ void finish_result(tmg_context* c, ResultHost& R, EigOut<Tv>& eo, ShiftInvert<Tv
         keep.push_back(t);
     }
     if (min_frequency > 0.0 && keep.empty()) { R.status = TMG_ERR_NUMERIC; R.freqs.clear(); return; }
-    if ((int)keep.size() > nev_target) keep.resize(nev_target);
+    if ((int)keep.size() > pr.nev_target) keep.resize(pr.nev_target);
     const int nk = (int)keep.size();
     DVec<Tv> Xk;
     Xk.alloc((size_t)n * std::max(nk, 1));
@@ -1241,27 +1338,25 @@ void finish_result(tmg_context* c, ResultHost& R, EigOut<Tv>& eo, ShiftInvert<Tv
         lz_copy<Tv>(st, n, eo.X.p + (int64_t)keep[t] * n, Xk.p + (int64_t)t * n);
         R.freqs.push_back(lam[t] > 0.0 ? std::sqrt(lam[t]) / (2.0 * PI) : 0.0);
     }
-    // residual diagnostic ||K x - lambda M x|| / ||K x|| (cyclic_solver.cpp:1099-1114)
-    if (nk > 0) {
+    if (nk > 0) {   // ||K x - lambda M x|| / ||K x|| (cyclic_solver.cpp:1099-1114)
         DVec<Tv> AX, MX, KX, RR;
         DVec<double> dl, np, nr;
         AX.alloc((size_t)n * nk); MX.alloc((size_t)n * nk); KX.alloc((size_t)n * nk); RR.alloc((size_t)n * nk);
         dl.upload(lam);
-        np.alloc(LZ_DOT_BLOCKS); nr.alloc(2);
-        lz_spmv<Tv>(st, A, Xk.p, AX.p, nk, n);
-        lz_spmv<Tv>(st, M, Xk.p, MX.p, nk, n);
+        np.alloc((size_t)nk * LZ_DOT_BLOCKS); nr.alloc(nk);
+        lz_spmv<Tv>(st, 1, A, Xk.p, 0, AX.p, 0, nk, n);
+        lz_spmv<Tv>(st, 1, M, Xk.p, 0, MX.p, 0, nk, n);
         TMG_LAUNCH(k_resid<Tv>, dim3(nblk(n), nk), 256, 0, st, n, nk, AX.p, MX.p, dl.p, shift, KX.p, RR.p);
-        for (int t = 0; t < nk; t++) {
-            double a = 0, b = 0;
-            lz_norm2<Tv>(st, n, RR.p + (int64_t)t * n, np.p, nr.p);
-            TMG_CUDA(cudaMemcpy(&a, nr.p, sizeof(double), cudaMemcpyDeviceToHost));
-            lz_norm2<Tv>(st, n, KX.p + (int64_t)t * n, np.p, nr.p);
-            TMG_CUDA(cudaMemcpy(&b, nr.p, sizeof(double), cudaMemcpyDeviceToHost));
-            const double res = b > 0 ? std::sqrt(a / b) : std::sqrt(a);
-            R.max_residual = std::max(R.max_residual, res);
-        }
+        std::vector<double> a(nk), b(nk);
+        lz_norm2<Tv>(st, nk, n, RR.p, n, np.p, nr.p);
+        TMG_CUDA(cudaMemcpyAsync(a.data(), nr.p, nk * sizeof(double), cudaMemcpyDeviceToHost, st));
+        TMG_CUDA(cudaStreamSynchronize(st));
+        lz_norm2<Tv>(st, nk, n, KX.p, n, np.p, nr.p);
+        TMG_CUDA(cudaMemcpyAsync(b.data(), nr.p, nk * sizeof(double), cudaMemcpyDeviceToHost, st));
+        TMG_CUDA(cudaStreamSynchronize(st));
+        for (int t = 0; t < nk; t++)
+            R.max_residual = std::max(R.max_residual, b[t] > 0 ? std::sqrt(a[t] / b[t]) : std::sqrt(a[t]));
     }
-    // complex free-space modes
     DVec<zd> Xc;
     Xc.alloc((size_t)n * std::max(nk, 1));
     if constexpr (std::is_same<Tv, double>::value) {
@@ -1273,7 +1368,7 @@ void finish_result(tmg_context* c, ResultHost& R, EigOut<Tv>& eo, ShiftInvert<Tv
     R.whirl.assign(nk, 0);
     DVec<zd> Xd;
     const zd* Xsrc = Xc.p;
-    if (is_degenerate && nk > 0) {
+    if (pr.degenerate && nk > 0) {
         nm = std::min(2 * nk, num_modes);
         Xd.alloc((size_t)n * nm);
         TMG_LAUNCH(k_dup_conj, dim3(nblk(n), nm), 256, 0, st, n, nm, Xc.p, Xd.p);
@@ -1283,131 +1378,196 @@ void finish_result(tmg_context* c, ResultHost& R, EigOut<Tv>& eo, ShiftInvert<Tv
         R.freqs = f2;
         Xsrc = Xd.p;
     }
-    // expansion to the full sector DOFs (cyclic_solver.cpp:1185-1211)
     const int32_t ndof = 3 * S.nn;
     DVec<zd> full;
     full.alloc((size_t)ndof * std::max(nm, 1));
-    DVec<int64_t> rp;
-    DVec<int32_t> ci, r2f;
-    DVec<double> tv;
-    DVec<uint8_t> isr;
-    rp.upload(S.T0t.p); ci.upload(S.T0t.i); tv.upload(S.T0tv); isr.upload(S.is_right); r2f.upload(S.r2free);
-    if (nm) TMG_LAUNCH(k_expand, dim3(nblk(ndof), nm), 256, 0, st, ndof, rp.p, ci.p, tv.p, isr.p, r2f.p, Xsrc, n, P,
-                       full.p, (int64_t)ndof);
+    if (nm) TMG_LAUNCH(k_expand, dim3(nblk(ndof), nm), 256, 0, st, ndof, c->dT0_rp.p, c->dT0_ci.p, c->dT0_v.p,
+                       c->d_isr.p, c->d_r2free.p, Xsrc, n, pr.P, full.p, (int64_t)ndof);
     TMG_CHECK_LAUNCH();
     R.shapes.resize((size_t)ndof * nm);
     if (nm) TMG_CUDA(cudaMemcpy(R.shapes.data(), full.p, R.shapes.size() * sizeof(zd), cudaMemcpyDeviceToHost));
 }
 
+// Factor and solve a batch of problems that share one symbolic analysis.
 template <typename Tv, typename Tf>
-void run_problem(tmg_context* c, ResultHost& R, const OpSymbolic& os, const UnionMaps& um, const Tv* vals_csc,
-                 const DevCsr<Tv>& M, int nev, int ncv, double shift, int max_restarts, bool mixed, int nev_target,
-                 int num_modes, double min_frequency, bool is_degenerate, zd P) {
+void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os, const UnionMaps& um,
+               const Tv* vals_csc, const DevCsr<Tv>& M, int nev, int ncv, double shift, int max_restarts, bool mixed,
+               int num_modes, double min_frequency) {
     cudaStream_t st = c->st;
-    const int64_t nl = (int64_t)um.lower2csc.n;
+    const int B = (int)probs.size();
+    const int64_t nl = (int64_t)um.lower2csc.n, nU = um.U.nnz();
     DVec<Tv> lower, acsr;
-    lower.alloc(nl);
-    acsr.alloc(um.U.nnz());
-    if (nl) TMG_LAUNCH(k_gather_t<Tv>, nblk(nl), 256, 0, st, nl, um.lower2csc.p, vals_csc, lower.p);
-    if (um.U.nnz()) TMG_LAUNCH(k_gather_t<Tv>, nblk(um.U.nnz()), 256, 0, st, um.U.nnz(), um.csr2csc.p, vals_csc, acsr.p);
+    lower.alloc((size_t)B * nl);
+    acsr.alloc((size_t)B * nU);
+    if (nl) TMG_LAUNCH(k_gather_b<Tv>, dim3(nblk(nl), B), 256, 0, st, nl, um.lower2csc.p, vals_csc, nU, lower.p, nl);
+    if (nU) TMG_LAUNCH(k_gather_b<Tv>, dim3(nblk(nU), B), 256, 0, st, nU, um.csr2csc.p, vals_csc, nU, acsr.p, nU);
     DevCsr<Tv> A;
-    A.nrows = um.U.ncols; A.nnz = um.U.nnz(); A.rowptr = um.csr_rowptr.p; A.col = um.csr_col.p; A.val = acsr.p;
-    ShiftInvert<Tv, Tf> op;
-    op.c = c; op.D = &os.D; op.um = &um; op.n = um.U.ncols; op.mixed = mixed; op.A = A;
+    A.nrows = um.U.ncols; A.nnz = nU; A.rowptr = um.csr_rowptr.p; A.col = um.csr_col.p; A.val = acsr.p; A.vstride = nU;
+    ShiftInvertB<Tv, Tf> op;
+    op.c = c; op.D = &os.D; op.um = &um; op.n = um.U.ncols; op.B = B; op.mixed = mixed; op.A = A;
     auto t0 = std::chrono::steady_clock::now();
-    op.factor(lower.p, nl);
+    op.factor(lower.p);
+    lower.release();
     auto t1 = std::chrono::steady_clock::now();
-    EigOut<Tv> eo = lanczos<Tv, Tf>(c, op, M, nev, ncv, shift, 1e-8, max_restarts);
+    std::vector<EigOut<Tv>> eo = lanczos<Tv, Tf>(c, op, M, nev, ncv, shift, 1e-8, max_restarts);
     auto t2 = std::chrono::steady_clock::now();
     c->phase_ms[1] += std::chrono::duration<double, std::milli>(t1 - t0).count();
     c->phase_ms[2] += std::chrono::duration<double, std::milli>(t2 - t1).count();
-    R.converged = eo.converged;
-    R.iterations = eo.restarts;
-    R.refine_residual = op.worst_refine;
-    R.solves = op.solves;
-    R.applies = op.applies;
-    if (!eo.converged && eo.ne == 0) { R.status = TMG_ERR_NUMERIC; return; }
-    finish_result<Tv>(c, R, eo, nullptr, A, M, shift, nev_target, num_modes, min_frequency, is_degenerate, P);
+    for (int p = 0; p < B; p++) {
+        ResultHost& R = *probs[p].R;
+        R.converged = eo[p].converged;
+        R.iterations = eo[p].restarts;
+        R.refine_residual = op.worst[p];
+        R.solves = op.solves;
+        R.applies = op.applies;
+        if (!eo[p].failed.empty()) { R.status = TMG_ERR_NUMERIC; c->err = eo[p].failed; continue; }
+        if (!eo[p].converged && eo[p].ne == 0) { R.status = TMG_ERR_NUMERIC; continue; }
+        DevCsr<Tv> Ap = A, Mp = M;
+        Ap.val = A.val + p * A.vstride;
+        Mp.val = M.val + p * M.vstride;
+        finish_result<Tv>(c, probs[p], eo[p], Ap, Mp, shift, num_modes, min_frequency);
+    }
     auto t3 = std::chrono::steady_clock::now();
     c->phase_ms[3] += std::chrono::duration<double, std::milli>(t3 - t2).count();
 }
 
-ResultHost solve_harmonic(tmg_context* c, int k, int num_modes, double min_frequency, int precision) {
+// Problems per batch that fit the device-memory budget.
+int batch_size(tmg_context* c, const OpSymbolic& os, const UnionMaps& um, int64_t nM, int ncv, bool cplx, bool mixed,
+               int nprob) {
+    const double vb = cplx ? 16.0 : 8.0;                       // FP64 vector entry
+    const double fb = mixed ? vb / 2 : vb;                     // factor entry
+    const DevSymbolic& D = os.D;
+    const double n = um.U.ncols;
+    const double per = fb * (double)(D.l_entries + D.u_entries + D.t_entries + n) +
+                       vb * (double)(3 * um.U.nnz() + 2 * um.lower2csc.n + 2 * nM) +
+                       vb * n * (2.0 * (ncv + 1) + 12.0) + 8.0 * ncv * ncv * 4;
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    const double avail = std::min<double>((double)c->budget, 0.85 * (double)fr);
+    const int b = (int)std::floor(avail / per);
+    if (b < 1) throw numeric_error("device memory budget too small for one problem");
+    return std::max(1, std::min(nprob, b));
+}
+
+void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double min_frequency, int precision,
+               std::vector<ResultHost>& results) {
     Sector& S = *c->sec;
     cudaStream_t st = c->st;
-    ResultHost R;
-    R.k = k;
-    R.rpm = c->rpm;
     const int N = S.ns, max_k = N / 2;
     const double alpha = 2.0 * PI / N;
-    const zd P{std::cos(k * alpha), std::sin(k * alpha)};
-    if (S.n_free <= 1) { R.status = TMG_ERR_ARG; return R; }
-    const bool is_degenerate = (k > 0) && !(N % 2 == 0 && k == max_k);
-    const bool will_qep = c->coriolis && k > 0;
-    if (will_qep) { R.status = TMG_ERR_STATE; return R; }
-    const int nev_target = is_degenerate ? (num_modes + 1) / 2 : num_modes;
-    const int n_extra = min_frequency > 0.0 ? 6 : 0;
-    int nev = std::min(nev_target + n_extra, S.n_free - 1);
-    if (nev <= 0) { R.status = TMG_ERR_ARG; return R; }
-    int ncv = std::min(std::max(4 * nev + 1, 40), S.n_free);
-    const double shift = 1.0;
-    const bool is_real = (k == 0) || (N % 2 == 0 && k == max_k);
     const bool mixed = precision == TMG_PREC_MIXED;
-    if (S.n_free <= 200) { R.status = TMG_ERR_ARG; return R; }
-    nev = std::min(nev, S.n_free - 1);
-    ncv = std::min(ncv, S.n_free);
-    if (is_real) {
-        auto& RO = c->real[k == 0 ? 0 : 1];
-        if (!RO.valid) { R.status = TMG_ERR_STATE; return R; }
+    const double shift = 1.0;
+    results.assign(ks.size(), ResultHost{});
+    std::vector<Problem> cplx, real0, realh;
+    for (size_t q = 0; q < ks.size(); q++) {
+        const int k = ks[q];
+        ResultHost& R = results[q];
+        R.k = k;
+        R.rpm = c->rpm;
+        Problem pr;
+        pr.k = k;
+        pr.P = zd{std::cos(k * alpha), std::sin(k * alpha)};
+        pr.R = &R;
+        if (S.n_free <= 1) { R.status = TMG_ERR_ARG; continue; }
+        pr.degenerate = (k > 0) && !(N % 2 == 0 && k == max_k);
+        if (c->coriolis && k > 0) { R.status = TMG_ERR_STATE; continue; }
+        pr.nev_target = pr.degenerate ? (num_modes + 1) / 2 : num_modes;
+        if (S.n_free <= 200) { R.status = TMG_ERR_ARG; continue; }
+        const bool is_real = (k == 0) || (N % 2 == 0 && k == max_k);
+        if (!is_real) cplx.push_back(pr);
+        else if (k == 0) real0.push_back(pr);
+        else realh.push_back(pr);
+    }
+    const int n_extra = min_frequency > 0.0 ? 6 : 0;
+    // real harmonics k = 0, N/2 (B = 1 each: own operators)
+    for (auto* grp : {&real0, &realh}) {
+        if (grp->empty()) continue;
+        Problem& pr = (*grp)[0];
+        auto& RO = c->real[pr.k == 0 ? 0 : 1];
+        if (!RO.valid) { pr.R->status = TMG_ERR_STATE; continue; }
         if (!RO.sym.valid) analyze_op(RO.sym, RO.op);
+        int nev = std::min(pr.nev_target + n_extra, S.n_free - 1);
+        const int ncv = std::min(std::max(4 * nev + 1, 40), S.n_free);
+        nev = std::min(nev, S.n_free - 1);
         DVec<double> vals;
         vals.alloc(RO.op.U.nnz());
         if (vals.n)
             TMG_LAUNCH(k_form_real_op, nblk(vals.n), 256, 0, st, (int64_t)vals.n, RO.op.maps[0].p, RO.op.maps[1].p,
                        RO.Kr.v.p, RO.Mr.v.p, shift, 1.0, vals.p);
-        CsrHost mc;
-        csr_of(RO.Mr.pat, mc);
+        std::vector<int64_t> mp;
+        Pattern Mt = transpose_map(RO.Mr.pat, mp);
+        DVec<int64_t> mrp, mperm;
+        DVec<int32_t> mci;
+        mrp.upload(Mt.p); mci.upload(Mt.i); mperm.upload(mp);
         DVec<double> mv;
-        mv.alloc(RO.Mr.pat.nnz());
-        if (mv.n) TMG_LAUNCH(k_gather_t<double>, nblk(mv.n), 256, 0, st, (int64_t)mv.n, mc.perm.p, RO.Mr.v.p, mv.p);
+        mv.alloc(mp.size());
+        if (mv.n) TMG_LAUNCH(k_gather_t<double>, nblk(mv.n), 256, 0, st, (int64_t)mv.n, mperm.p, RO.Mr.v.p, mv.p);
         DevCsr<double> M;
-        M.nrows = S.n_free; M.nnz = mv.n; M.rowptr = mc.rp.p; M.col = mc.ci.p; M.val = mv.p;
-        if (mixed)
-            run_problem<double, float>(c, R, RO.sym, RO.op, vals.p, M, nev, ncv, shift, 1000, true, nev_target,
-                                       num_modes, min_frequency, false, P);
-        else
-            run_problem<double, double>(c, R, RO.sym, RO.op, vals.p, M, nev, ncv, shift, 1000, false, nev_target,
-                                        num_modes, min_frequency, false, P);
-    } else {
+        M.nrows = S.n_free; M.nnz = mv.n; M.rowptr = mrp.p; M.col = mci.p; M.val = mv.p; M.vstride = 0;
+        try {
+            if (mixed)
+                run_batch<double, float>(c, *grp, RO.sym, RO.op, vals.p, M, nev, ncv, shift, 1000, true, num_modes,
+                                         min_frequency);
+            else
+                run_batch<double, double>(c, *grp, RO.sym, RO.op, vals.p, M, nev, ncv, shift, 1000, false, num_modes,
+                                          min_frequency);
+        } catch (const numeric_error& e) {
+            pr.R->status = TMG_ERR_NUMERIC;
+            c->err = e.what();
+        }
+    }
+    // complex harmonics: one shared symbolic analysis, batched under the memory budget
+    if (!cplx.empty()) {
         if (!c->symC.valid) analyze_op(c->symC, c->opC);
         UnionMaps& um = c->opC;
-        DVec<zd> vals;
-        vals.alloc(um.U.nnz());
-        if (vals.n)
-            TMG_LAUNCH(k_form_complex, nblk(vals.n), 256, 0, st, (int64_t)vals.n, um.maps[0].p, um.maps[1].p,
-                       um.maps[2].p, um.maps[3].p, um.maps[4].p, um.maps[5].p, c->Kcf.v.p, c->Kpf.v.p, c->Mcf.v.p,
-                       c->Mpf.v.p, P.x, P.y, shift, 1.0, vals.p);
         UnionMaps& mu = c->opMC;
-        DVec<zd> mvals, mcsr;
-        mvals.alloc(mu.U.nnz());
-        mcsr.alloc(mu.U.nnz());
-        if (mvals.n) {
-            TMG_LAUNCH(k_form_csum, nblk(mvals.n), 256, 0, st, (int64_t)mvals.n, mu.maps[0].p, mu.maps[1].p,
-                       mu.maps[2].p, c->Mcf.v.p, c->Mpf.v.p, P.x, P.y, mvals.p);
-            TMG_LAUNCH(k_gather_t<zd>, nblk(mvals.n), 256, 0, st, (int64_t)mvals.n, mu.csr2csc.p, mvals.p, mcsr.p);
+        int nev = std::min(cplx[0].nev_target + n_extra, S.n_free - 1);
+        const int ncv = std::min(std::max(4 * nev + 1, 40), S.n_free);
+        const int bmax = batch_size(c, c->symC, um, mu.U.nnz(), ncv, true, mixed, (int)cplx.size());
+        for (size_t b0 = 0; b0 < cplx.size(); b0 += bmax) {
+            std::vector<Problem> grp(cplx.begin() + b0, cplx.begin() + std::min(cplx.size(), b0 + bmax));
+            const int B = (int)grp.size();
+            std::vector<double> ph(2 * B);
+            for (int p = 0; p < B; p++) { ph[2 * p] = grp[p].P.x; ph[2 * p + 1] = grp[p].P.y; }
+            DVec<double> dph;
+            dph.upload(ph);
+            DVec<zd> vals, mvals, mcsr;
+            vals.alloc((size_t)B * um.U.nnz());
+            mvals.alloc((size_t)B * mu.U.nnz());
+            mcsr.alloc((size_t)B * mu.U.nnz());
+            if (um.U.nnz())
+                TMG_LAUNCH(k_form_complex, dim3(nblk(um.U.nnz()), B), 256, 0, st, um.U.nnz(), um.maps[0].p, um.maps[1].p,
+                           um.maps[2].p, um.maps[3].p, um.maps[4].p, um.maps[5].p, c->Kcf.v.p, c->Kpf.v.p, c->Mcf.v.p,
+                           c->Mpf.v.p, dph.p, shift, vals.p);
+            if (mu.U.nnz()) {
+                TMG_LAUNCH(k_form_csum, dim3(nblk(mu.U.nnz()), B), 256, 0, st, mu.U.nnz(), mu.maps[0].p, mu.maps[1].p,
+                           mu.maps[2].p, c->Mcf.v.p, c->Mpf.v.p, dph.p, mvals.p);
+                TMG_LAUNCH(k_gather_b<zd>, dim3(nblk(mu.U.nnz()), B), 256, 0, st, mu.U.nnz(), mu.csr2csc.p, mvals.p,
+                           mu.U.nnz(), mcsr.p, mu.U.nnz());
+            }
+            mvals.release();
+            DevCsr<zd> M;
+            M.nrows = S.n_free; M.nnz = mu.U.nnz(); M.rowptr = mu.csr_rowptr.p; M.col = mu.csr_col.p; M.val = mcsr.p;
+            M.vstride = mu.U.nnz();
+            try {
+                if (mixed)
+                    run_batch<zd, zf>(c, grp, c->symC, um, vals.p, M, nev, ncv, shift, 1000, true, num_modes,
+                                      min_frequency);
+                else
+                    run_batch<zd, zd>(c, grp, c->symC, um, vals.p, M, nev, ncv, shift, 1000, false, num_modes,
+                                      min_frequency);
+            } catch (const numeric_error& e) {
+                for (auto& pr : grp) pr.R->status = TMG_ERR_NUMERIC;
+                c->err = e.what();
+            }
         }
-        DevCsr<zd> M;
-        M.nrows = S.n_free; M.nnz = mcsr.n; M.rowptr = mu.csr_rowptr.p; M.col = mu.csr_col.p; M.val = mcsr.p;
-        if (mixed)
-            run_problem<zd, zf>(c, R, c->symC, um, vals.p, M, nev, ncv, shift, 1000, true, nev_target, num_modes,
-                                min_frequency, is_degenerate, P);
-        else
-            run_problem<zd, zd>(c, R, c->symC, um, vals.p, M, nev, ncv, shift, 1000, false, nev_target, num_modes,
-                                min_frequency, is_degenerate, P);
     }
     TMG_CUDA(cudaStreamSynchronize(st));
-    return R;
 }
+
+}  // namespace
+
+namespace {
 
 int copy_csc(const Pattern& P, const double* dvals_or_null, const std::vector<double>* hvals, int64_t* nnz,
              int32_t* colptr, int32_t* rowidx, double* values, bool complex_out) {
@@ -1536,9 +1696,11 @@ int tmg_projection(tmg_context* c, int which, int k, int64_t* nnz, int32_t* n, i
                 const double alpha = 2.0 * PI / S.ns;
                 DVec<zd> v;
                 v.alloc(w.U.nnz());
+                DVec<double> ph;
+                ph.upload(std::vector<double>{std::cos(k * alpha), std::sin(k * alpha)});
                 if (v.n)
-                    TMG_LAUNCH(k_form_csum, nblk(v.n), 256, 0, c->st, (int64_t)v.n, w.maps[0].p, w.maps[1].p,
-                               w.maps[2].p, cc.v.p, pp.v.p, std::cos(k * alpha), std::sin(k * alpha), v.p);
+                    TMG_LAUNCH(k_form_csum, dim3(nblk(v.n), 1), 256, 0, c->st, (int64_t)v.n, w.maps[0].p, w.maps[1].p,
+                               w.maps[2].p, cc.v.p, pp.v.p, ph.p, v.p);
                 TMG_CUDA(cudaStreamSynchronize(c->st));
                 *nnz = w.U.nnz();
                 if (!colptr) return TMG_OK;
@@ -1596,8 +1758,8 @@ int tmg_symbolic_stats(tmg_context* c, int kind, double* out) {
         }
         const Symbolic& S = os->S;
         out[0] = S.n; out[1] = (double)S.nnz_l; out[2] = S.ns; out[3] = (double)S.level_ptr.size() - 1;
-        out[4] = S.max_front; out[5] = (double)S.front_entries(); out[6] = 4.0 * S.flops_real;
-        out[7] = (double)os->D.nlower;
+        out[4] = S.max_front; out[5] = (double)os->D.l_entries; out[6] = 4.0 * S.flops_real;
+        out[7] = (double)os->D.nlower; out[8] = (double)os->D.u_entries; out[9] = (double)os->D.l_stored;
         return TMG_OK;
     });
 }
@@ -1622,17 +1784,8 @@ int tmg_solve_at_rpm(tmg_context* c, double rpm, int num_modes, const int32_t* h
         if (!harmonics || nh == 0) for (int k = 0; k <= max_k; k++) hs.push_back(k);
         else for (int q = 0; q < nh; q++) if (harmonics[q] >= 0 && harmonics[q] <= max_k) hs.push_back(harmonics[q]);
         c->results.clear();
-        std::string firsterr;
-        for (int k : hs) {
-            ResultHost R;
-            try {
-                R = solve_harmonic(c, k, num_modes, min_frequency, precision);
-            } catch (const numeric_error& e) {
-                R.k = k; R.rpm = rpm; R.status = TMG_ERR_NUMERIC;
-                if (firsterr.empty()) firsterr = e.what();
-            }
-            c->results.push_back(std::move(R));
-        }
+        c->err.clear();
+        solve_set(c, hs, num_modes, min_frequency, precision, c->results);
         std::sort(c->results.begin(), c->results.end(), [](const ResultHost& a, const ResultHost& b) { return a.k < b.k; });
         *num_results = (int32_t)c->results.size();
         c->launches = g_kernel_launches - l0;
@@ -1643,7 +1796,6 @@ int tmg_solve_at_rpm(tmg_context* c, double rpm, int num_modes, const int32_t* h
         c->phase_ms[4] = ms;
         cudaEventDestroy(ev0);
         cudaEventDestroy(ev1);
-        if (!firsterr.empty()) c->err = firsterr;
         return TMG_OK;
     });
 }

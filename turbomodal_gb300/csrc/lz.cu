@@ -1,7 +1,7 @@
-// Lanczos eigensolver device kernels: sparse matrix-vector products with the shared
-// projection matrices, deterministic two-stage reductions, classical Gram-Schmidt
+// Lanczos eigensolver device kernels, batched over problems (grid y/z = problem):
+// sparse matrix-vector products, deterministic two-stage reductions, classical Gram-Schmidt
 // reorthogonalisation, and the small FP64 tridiagonal problems (eigen-decomposition by
-// implicit QL, implicit-restart QR sweeps) on one CTA.
+// implicit QL, implicit-restart QR sweeps) with one CTA per problem.
 #include <algorithm>
 
 #include "lz.cuh"
@@ -10,35 +10,38 @@ namespace tmg {
 
 template <typename T>
 __global__ void k_spmv(int32_t nrows, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
-                       const T* __restrict__ av, const T* __restrict__ x, T* __restrict__ y, int64_t ld, int sub) {
+                       const T* __restrict__ av, int64_t vstride, const T* __restrict__ x, int64_t xs,
+                       T* __restrict__ y, int64_t ys, int64_t ld, int sub) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= nrows) return;
-    const int64_t v = blockIdx.y;
-    const T* xv = x + v * ld;
+    const int64_t v = blockIdx.y, p = blockIdx.z;
+    const T* xv = x + p * xs + v * ld;
+    const T* a = av + p * vstride;
     T s = zero_of<T>();
-    for (int64_t p = rp[i]; p < rp[i + 1]; p++) s += av[p] * xv[ci[p]];
-    if (sub) y[v * ld + i] -= s;
-    else y[v * ld + i] = s;
+    for (int64_t q = rp[i]; q < rp[i + 1]; q++) s += a[q] * xv[ci[q]];
+    T* yv = y + p * ys + v * ld;
+    if (sub) yv[i] -= s;
+    else yv[i] = s;
 }
 
 template <typename T>
-void lz_spmv(cudaStream_t st, const DevCsr<T>& A, const T* x, T* y, int nvec, int64_t ld, bool subtract) {
-    if (A.nrows == 0 || nvec == 0) return;
-    TMG_LAUNCH(k_spmv<T>, dim3((unsigned)ceil_div(A.nrows, 128), nvec), 128, 0, st, A.nrows, A.rowptr, A.col, A.val,
-               x, y, ld, subtract ? 1 : 0);
+void lz_spmv(cudaStream_t st, int B, const DevCsr<T>& A, const T* x, int64_t xs, T* y, int64_t ys, int nvec, int64_t ld,
+             bool subtract) {
+    if (A.nrows == 0 || nvec == 0 || B == 0) return;
+    TMG_LAUNCH(k_spmv<T>, dim3((unsigned)ceil_div(A.nrows, 128), nvec, B), 128, 0, st, A.nrows, A.rowptr, A.col, A.val,
+               A.vstride, x, xs, y, ys, ld, subtract ? 1 : 0);
     TMG_CHECK_LAUNCH();
 }
 
 template <typename T>
 __device__ T block_sum(T v, T* sh) {
     using R = typename real_of<T>::type;
-    // warp tree then first warp
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        R* p = reinterpret_cast<R*>(&v);
-        p[0] += __shfl_down_sync(0xffffffff, p[0], o);
-        if constexpr (sizeof(T) == 2 * sizeof(R)) p[1] += __shfl_down_sync(0xffffffff, p[1], o);
+        R* q = reinterpret_cast<R*>(&v);
+        q[0] += __shfl_down_sync(0xffffffff, q[0], o);
+        if constexpr (sizeof(T) == 2 * sizeof(R)) q[1] += __shfl_down_sync(0xffffffff, q[1], o);
     }
     if (lane == 0) sh[warp] = v;
     __syncthreads();
@@ -50,120 +53,140 @@ __device__ T block_sum(T v, T* sh) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_multidot1(int64_t n, const T* __restrict__ A, int64_t lda, int K,
-                                                   const T* __restrict__ y, T* __restrict__ partial) {
+__global__ void __launch_bounds__(256) k_multidot1(int64_t n, const T* __restrict__ A, int64_t as, int64_t lda, int K,
+                                                   const T* __restrict__ y, int64_t ys, T* __restrict__ partial) {
     __shared__ T sh[8];
+    const int64_t p = blockIdx.y;
+    A += p * as;
+    y += p * ys;
     const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
     const int64_t lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
     for (int k = 0; k < K; k++) {
         T s = zero_of<T>();
         for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) s += conj(A[k * lda + i]) * y[i];
         s = block_sum(s, sh);
-        if (threadIdx.x == 0) partial[(int64_t)k * gridDim.x + blockIdx.x] = s;
+        if (threadIdx.x == 0) partial[((int64_t)p * K + k) * gridDim.x + blockIdx.x] = s;
     }
 }
 
 template <typename T>
-__global__ void k_multidot2(int K, int nb, const T* __restrict__ partial, T* __restrict__ out) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= K) return;
+__global__ void k_multidot2(int n_out, int nb, const T* __restrict__ partial, T* __restrict__ out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_out) return;
     T s = zero_of<T>();
-    for (int b = 0; b < nb; b++) s += partial[(int64_t)k * nb + b];
-    out[k] = s;
+    for (int b = 0; b < nb; b++) s += partial[(int64_t)q * nb + b];
+    out[q] = s;
 }
 
 template <typename T>
-void lz_multidot(cudaStream_t st, int64_t n, const T* A, int64_t lda, int K, const T* y, T* partial, T* out) {
-    TMG_LAUNCH(k_multidot1<T>, LZ_DOT_BLOCKS, 256, 0, st, n, A, lda, K, y, partial);
-    TMG_LAUNCH(k_multidot2<T>, (unsigned)ceil_div(K, 128), 128, 0, st, K, LZ_DOT_BLOCKS, partial, out);
+void lz_multidot(cudaStream_t st, int B, int64_t n, const T* A, int64_t as, int64_t lda, int K, const T* y, int64_t ys,
+                 T* partial, T* out) {
+    TMG_LAUNCH(k_multidot1<T>, dim3(LZ_DOT_BLOCKS, B), 256, 0, st, n, A, as, lda, K, y, ys, partial);
+    TMG_LAUNCH(k_multidot2<T>, (unsigned)ceil_div((int64_t)K * B, 128), 128, 0, st, K * B, LZ_DOT_BLOCKS, partial, out);
     TMG_CHECK_LAUNCH();
 }
 
-// w -= alpha_j v_j + beta_{j-1} v_{j-1}; alpha_j = re(dot) stored by thread 0
 template <typename T>
 __global__ void k_three_term(int64_t n, int j, const T* __restrict__ dot, double* __restrict__ alpha,
-                             const double* __restrict__ beta, const T* __restrict__ V, T* __restrict__ w) {
+                             const double* __restrict__ beta, int ldab, const T* __restrict__ V, int64_t vs,
+                             T* __restrict__ w, int64_t ws) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const double a = re(dot[0]);
-    if (i == 0) alpha[j] = a;
+    const int64_t p = blockIdx.y;
+    const double a = re(dot[p]);
+    if (i == 0) alpha[p * ldab + j] = a;
     if (i >= n) return;
-    T v = w[i] - a * V[(int64_t)j * n + i];
-    if (j > 0) v = v - beta[j - 1] * V[(int64_t)(j - 1) * n + i];
-    w[i] = v;
+    const T* Vp = V + p * vs;
+    T v = w[p * ws + i] - a * Vp[(int64_t)j * n + i];
+    if (j > 0) v = v - beta[p * ldab + j - 1] * Vp[(int64_t)(j - 1) * n + i];
+    w[p * ws + i] = v;
 }
 template <typename T>
-void lz_three_term_dot(cudaStream_t st, int64_t n, int j, const T* dot, double* alpha, const double* beta, const T* V,
-                       T* w) {
-    TMG_LAUNCH(k_three_term<T>, (unsigned)ceil_div(n, 256), 256, 0, st, n, j, dot, alpha, beta, V, w);
+void lz_three_term(cudaStream_t st, int B, int64_t n, int j, const T* dot, double* alpha, const double* beta, int ldab,
+                   const T* V, int64_t vs, T* w, int64_t ws) {
+    TMG_LAUNCH(k_three_term<T>, dim3((unsigned)ceil_div(n, 256), B), 256, 0, st, n, j, dot, alpha, beta, ldab, V, vs, w, ws);
     TMG_CHECK_LAUNCH();
 }
 
-// w -= V(:, 0:K) h
 template <typename T>
-__global__ void k_gemv_sub(int64_t n, int K, const T* __restrict__ V, const T* __restrict__ h, T* __restrict__ w) {
+__global__ void k_gemv_sub(int64_t n, int K, const T* __restrict__ V, int64_t vs, const T* __restrict__ h, int ldh,
+                           T* __restrict__ w, int64_t ws) {
     __shared__ T hs[256];
-    for (int k = threadIdx.x; k < K && k < 256; k += blockDim.x) hs[k] = h[k];
+    const int64_t p = blockIdx.y;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) hs[k] = h[p * ldh + k];
     __syncthreads();
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const T* Vp = V + p * vs;
     T acc = zero_of<T>();
-    for (int k = 0; k < K; k++) acc += V[(int64_t)k * n + i] * hs[k];
-    w[i] -= acc;
+    for (int k = 0; k < K; k++) acc += Vp[(int64_t)k * n + i] * hs[k];
+    w[p * ws + i] -= acc;
 }
 template <typename T>
-void lz_gemv_sub(cudaStream_t st, int64_t n, int K, const T* V, const T* h, T* w) {
-    TMG_LAUNCH(k_gemv_sub<T>, (unsigned)ceil_div(n, 256), 256, 0, st, n, K, V, h, w);
+void lz_gemv_sub(cudaStream_t st, int B, int64_t n, int K, const T* V, int64_t vs, const T* h, int ldh, T* w, int64_t ws) {
+    if (K > 256) throw std::runtime_error("Lanczos subspace above 256 vectors is not supported");
+    TMG_LAUNCH(k_gemv_sub<T>, dim3((unsigned)ceil_div(n, 256), B), 256, 0, st, n, K, V, vs, h, ldh, w, ws);
     TMG_CHECK_LAUNCH();
 }
 
 template <typename T>
 __global__ void k_beta_scale(int64_t n, int j, const T* __restrict__ dot, const T* __restrict__ w,
-                             const T* __restrict__ Mw, T* __restrict__ V, T* __restrict__ MV, double* __restrict__ beta,
-                             int* __restrict__ flag) {
-    const double b = sqrt(fabs(re(dot[0])));
+                             const T* __restrict__ Mw, int64_t ws, T* __restrict__ V, T* __restrict__ MV, int64_t vs,
+                             double* __restrict__ beta, int ldab, int* __restrict__ flag) {
+    const int64_t p = blockIdx.y;
+    const double b = sqrt(fabs(re(dot[p])));
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i == 0) {
-        beta[j] = b;
-        if (b < 1e-14 && flag[0] == 0) flag[0] = j + 1;
+        beta[p * ldab + j] = b;
+        if (b < 1e-14 && flag[p] == 0) flag[p] = j + 1;
     }
     if (i >= n) return;
     const double ib = 1.0 / b;
-    V[(int64_t)(j + 1) * n + i] = ib * w[i];
-    MV[(int64_t)(j + 1) * n + i] = ib * Mw[i];
+    V[p * vs + (int64_t)(j + 1) * n + i] = ib * w[p * ws + i];
+    MV[p * vs + (int64_t)(j + 1) * n + i] = ib * Mw[p * ws + i];
 }
 template <typename T>
-void lz_beta_scale(cudaStream_t st, int64_t n, int j, const T* dot, const T* w, const T* Mw, T* V, T* MV, double* beta,
-                   int* flag) {
-    TMG_LAUNCH(k_beta_scale<T>, (unsigned)ceil_div(n, 256), 256, 0, st, n, j, dot, w, Mw, V, MV, beta, flag);
+void lz_beta_scale(cudaStream_t st, int B, int64_t n, int j, const T* dot, const T* w, const T* Mw, int64_t ws, T* V,
+                   T* MV, int64_t vs, double* beta, int ldab, int* flag) {
+    TMG_LAUNCH(k_beta_scale<T>, dim3((unsigned)ceil_div(n, 256), B), 256, 0, st, n, j, dot, w, Mw, ws, V, MV, vs, beta,
+               ldab, flag);
     TMG_CHECK_LAUNCH();
 }
 
 template <typename T>
-__global__ void k_scale_cols(int64_t n, const T* __restrict__ dot, T* __restrict__ x, T* __restrict__ Mx) {
-    const double s = sqrt(re(dot[0]));
+__global__ void k_scale_first(int64_t n, const T* __restrict__ dot, T* __restrict__ V, T* __restrict__ MV, int64_t vs) {
+    const int64_t p = blockIdx.y;
+    const double s = sqrt(re(dot[p]));
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    x[i] = x[i] / s;
-    Mx[i] = Mx[i] / s;
+    V[p * vs + i] = V[p * vs + i] / s;
+    MV[p * vs + i] = MV[p * vs + i] / s;
 }
 template <typename T>
-void lz_scale_cols(cudaStream_t st, int64_t n, const T* dot, T* x, T* Mx) {
-    TMG_LAUNCH(k_scale_cols<T>, (unsigned)ceil_div(n, 256), 256, 0, st, n, dot, x, Mx);
+void lz_scale_first(cudaStream_t st, int B, int64_t n, const T* dot, T* V, T* MV, int64_t vs) {
+    TMG_LAUNCH(k_scale_first<T>, dim3((unsigned)ceil_div(n, 256), B), 256, 0, st, n, dot, V, MV, vs);
     TMG_CHECK_LAUNCH();
 }
 
 // ------------------------------------------------------------------------------------
-// Tridiagonal eigenproblem (implicit QL with eigenvectors, EISPACK tql2 formulation).
-// Thread 0 runs the scalar recurrences and records each sweep's rotations; every thread
-// then applies the sweep to its own row of Z.
-__global__ void __launch_bounds__(256) k_tridiag(int m, int nev, double shift, double tol,
-                                                 const double* __restrict__ alpha, const double* __restrict__ beta,
-                                                 double* __restrict__ theta, double* __restrict__ S,
-                                                 double* __restrict__ lam, int* __restrict__ order,
-                                                 int* __restrict__ nconv, double* __restrict__ Z) {
+// Tridiagonal eigenproblem (implicit QL with eigenvectors, EISPACK tql2 formulation), one
+// CTA per problem.  Thread 0 runs the scalar recurrences and records each sweep's
+// rotations; every thread then applies the sweep to its own row of Z.
+__global__ void __launch_bounds__(256) k_tridiag(int m, int ldab, int nev, double shift, double tol,
+                                                 const double* __restrict__ alpha_b, const double* __restrict__ beta_b,
+                                                 double* __restrict__ theta_b, double* __restrict__ S_b,
+                                                 double* __restrict__ lam_b, int* __restrict__ order_b,
+                                                 int* __restrict__ nconv, double* __restrict__ Z_b) {
     __shared__ double d[256], e[256], rc[256], rs[256], lamv[256];
     __shared__ int perm[256], ord[256];
-    __shared__ int s_l, s_m, s_go, s_lo, s_hi;
+    __shared__ int s_m, s_go, s_lo, s_hi;
+    const int p = blockIdx.x;
+    const double* alpha = alpha_b + (int64_t)p * ldab;
+    const double* beta = beta_b + (int64_t)p * ldab;
+    double* theta = theta_b + (int64_t)p * ldab;
+    double* lam = lam_b + (int64_t)p * ldab;
+    int* order = order_b + (int64_t)p * ldab;
+    double* S = S_b + (int64_t)p * ldab * ldab;
+    double* Z = Z_b + (int64_t)p * ldab * ldab;
     const int k = threadIdx.x;
     for (int c = 0; c < m; c++)
         if (k < m) Z[(int64_t)c * m + k] = (c == k) ? 1.0 : 0.0;
@@ -189,35 +212,35 @@ __global__ void __launch_bounds__(256) k_tridiag(int m, int nev, double shift, d
                 const int mm = s_m;
                 iter++;
                 double g = d[l];
-                double p = (d[l + 1] - g) / (2.0 * e[l]);
-                double r = hypot(p, 1.0);
-                if (p < 0) r = -r;
-                d[l] = e[l] / (p + r);
-                d[l + 1] = e[l] * (p + r);
+                double pp = (d[l + 1] - g) / (2.0 * e[l]);
+                double r = hypot(pp, 1.0);
+                if (pp < 0) r = -r;
+                d[l] = e[l] / (pp + r);
+                d[l + 1] = e[l] * (pp + r);
                 const double dl1 = d[l + 1];
                 double h = g - d[l];
                 for (int i = l + 2; i < m; i++) d[i] -= h;
                 f = f + h;
-                p = d[mm];
+                pp = d[mm];
                 double c = 1.0, c2 = c, c3 = c;
                 const double el1 = e[l + 1];
                 double s = 0.0, s2 = 0.0;
                 for (int i = mm - 1; i >= l; i--) {
                     c3 = c2; c2 = c; s2 = s;
                     g = c * e[i];
-                    h = c * p;
-                    r = hypot(p, e[i]);
+                    h = c * pp;
+                    r = hypot(pp, e[i]);
                     e[i + 1] = s * r;
                     s = e[i] / r;
-                    c = p / r;
-                    p = c * d[i] - s * g;
+                    c = pp / r;
+                    pp = c * d[i] - s * g;
                     d[i + 1] = h + s * (c * g + s * d[i]);
                     rc[i] = c;
                     rs[i] = s;
                 }
-                p = -s * s2 * c3 * el1 * e[l] / dl1;
-                e[l] = s * p;
-                d[l] = c * p;
+                pp = -s * s2 * c3 * el1 * e[l] / dl1;
+                e[l] = s * pp;
+                d[l] = c * pp;
                 s_lo = l;
                 s_hi = mm - 1;
                 s_go = (fabs(e[l]) > eps * tst1 && iter < 200) ? 1 : 0;
@@ -241,9 +264,9 @@ __global__ void __launch_bounds__(256) k_tridiag(int m, int nev, double shift, d
         for (int i = 0; i < m; i++) perm[i] = i;
         for (int i = 0; i < m - 1; i++) {   // selection sort ascending, as tql2's final pass
             int kk = i;
-            double p = d[perm[i]];
+            double pp = d[perm[i]];
             for (int j = i + 1; j < m; j++)
-                if (d[perm[j]] < p) { kk = j; p = d[perm[j]]; }
+                if (d[perm[j]] < pp) { kk = j; pp = d[perm[j]]; }
             if (kk != i) { const int t = perm[i]; perm[i] = perm[kk]; perm[kk] = t; }
         }
         for (int i = 0; i < m; i++) {
@@ -274,22 +297,29 @@ __global__ void __launch_bounds__(256) k_tridiag(int m, int nev, double shift, d
             const double res = fabs(bl * S[(int64_t)ii * m + m - 1]);
             if (res < tol * fmax(1.0, fabs(d[perm[ii]]))) nc++;
         }
-        nconv[0] = nc;
+        nconv[p] = nc;
     }
 }
 
-void lz_tridiag(cudaStream_t st, int m, int nev, double shift, double tol, const double* alpha, const double* beta,
-                double* theta, double* S, double* lam, int* order, int* nconv, double* work) {
+void lz_tridiag(cudaStream_t st, int B, int m, int ldab, int nev, double shift, double tol, const double* alpha,
+                const double* beta, double* theta, double* S, double* lam, int* order, int* nconv, double* Z) {
     if (m > 256) throw std::runtime_error("Lanczos subspace above 256 vectors is not supported");
-    TMG_LAUNCH(k_tridiag, 1, 256, 0, st, m, nev, shift, tol, alpha, beta, theta, S, lam, order, nconv, work);
+    TMG_LAUNCH(k_tridiag, B, 256, 0, st, m, ldab, nev, shift, tol, alpha, beta, theta, S, lam, order, nconv, Z);
     TMG_CHECK_LAUNCH();
 }
 
 // src/hermitian_lanczos.cpp:141-218: shifts = the m-nev smallest theta; bulge-chasing
 // Givens sweeps on (alpha, beta); rotations accumulated into Q by rows.
-__global__ void __launch_bounds__(256) k_restart_qr(int m, int nev, const double* __restrict__ theta,
-                                                    double* __restrict__ alpha, double* __restrict__ beta,
-                                                    double* __restrict__ Q, double* __restrict__ rot) {
+__global__ void __launch_bounds__(256) k_restart_qr(int m, int ldab, int nev, const double* __restrict__ theta_b,
+                                                    double* __restrict__ alpha_b, double* __restrict__ beta_b,
+                                                    double* __restrict__ Q_b, double* __restrict__ rot_b,
+                                                    int64_t rot_stride) {
+    const int p = blockIdx.x;
+    const double* theta = theta_b + (int64_t)p * ldab;
+    double* alpha = alpha_b + (int64_t)p * ldab;
+    double* beta = beta_b + (int64_t)p * ldab;
+    double* Q = Q_b + (int64_t)p * ldab * ldab;
+    double* rot = rot_b + (int64_t)p * rot_stride;
     const int ns = m - nev;
     if (threadIdx.x == 0) {
         for (int s = 0; s < ns; s++) {
@@ -328,17 +358,21 @@ __global__ void __launch_bounds__(256) k_restart_qr(int m, int nev, const double
         }
 }
 
-void lz_restart_qr(cudaStream_t st, int m, int nev, const double* theta, double* alpha, double* beta, double* Q,
-                   double* rot) {
-    TMG_LAUNCH(k_restart_qr, 1, 256, 0, st, m, nev, theta, alpha, beta, Q, rot);
+void lz_restart_qr(cudaStream_t st, int B, int m, int ldab, int nev, const double* theta, double* alpha, double* beta,
+                   double* Q, double* rot, int64_t rot_stride) {
+    TMG_LAUNCH(k_restart_qr, B, 256, 0, st, m, ldab, nev, theta, alpha, beta, Q, rot, rot_stride);
     TMG_CHECK_LAUNCH();
 }
 
 template <typename T>
-__global__ void k_gemm_real(int64_t n, int K, int ncol, const T* __restrict__ X, const double* __restrict__ C, int ldc,
-                            T* __restrict__ Y) {
+__global__ void k_gemm_real(int64_t n, int K, int ncol, const T* __restrict__ X, int64_t xs, const double* __restrict__ C,
+                            int64_t cs, int ldc, T* __restrict__ Y, int64_t ys) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t p = blockIdx.y;
     if (i >= n) return;
+    X += p * xs;
+    C += p * cs;
+    Y += p * ys;
     for (int c0 = 0; c0 < ncol; c0 += 8) {
         T acc[8];
 #pragma unroll
@@ -355,26 +389,55 @@ __global__ void k_gemm_real(int64_t n, int K, int ncol, const T* __restrict__ X,
     }
 }
 template <typename T>
-void lz_gemm_real(cudaStream_t st, int64_t n, int K, int ncol, const T* X, const double* C, int ldc, T* Y) {
-    if (n == 0 || ncol == 0) return;
-    TMG_LAUNCH(k_gemm_real<T>, (unsigned)ceil_div(n, 128), 128, 0, st, n, K, ncol, X, C, ldc, Y);
+void lz_gemm_real(cudaStream_t st, int B, int64_t n, int K, int ncol, const T* X, int64_t xs, const double* C, int64_t cs,
+                  int ldc, T* Y, int64_t ys) {
+    if (n == 0 || ncol == 0 || B == 0) return;
+    TMG_LAUNCH(k_gemm_real<T>, dim3((unsigned)ceil_div(n, 128), B), 128, 0, st, n, K, ncol, X, xs, C, cs, ldc, Y, ys);
     TMG_CHECK_LAUNCH();
 }
 
 template <typename T>
-__global__ void k_combine_f(int64_t n, const T* __restrict__ Y, const T* __restrict__ v, const double* __restrict__ beta,
-                            int nev, int m, const double* __restrict__ Q, T* __restrict__ f) {
+__global__ void k_combine_f(int64_t n, const T* __restrict__ Y, int64_t ys, const T* __restrict__ v, int64_t vs,
+                            const double* __restrict__ beta, int ldab, int nev, int m, const double* __restrict__ Q,
+                            T* __restrict__ f, int64_t fs) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t p = blockIdx.y;
     if (i >= n) return;
-    const double bt = beta[nev - 1];
-    const double bd = beta[m - 1];
-    const double qd = Q[(int64_t)(nev - 1) * m + m - 1];
-    f[i] = bt * Y[i] + (bd * qd) * v[i];
+    const double bt = beta[p * ldab + nev - 1];
+    const double bd = beta[p * ldab + m - 1];
+    const double qd = Q[p * (int64_t)ldab * ldab + (int64_t)(nev - 1) * m + m - 1];
+    f[p * fs + i] = bt * Y[p * ys + i] + (bd * qd) * v[p * vs + i];
 }
 template <typename T>
-void lz_combine_f(cudaStream_t st, int64_t n, const T* Y, const T* v, const double* beta, int nev, int m,
-                  const double* Q, T* f) {
-    TMG_LAUNCH(k_combine_f<T>, (unsigned)ceil_div(n, 256), 256, 0, st, n, Y, v, beta, nev, m, Q, f);
+void lz_combine_f(cudaStream_t st, int B, int64_t n, const T* Y, int64_t ys, const T* v, int64_t vs, const double* beta,
+                  int ldab, int nev, int m, const double* Q, T* f, int64_t fs) {
+    TMG_LAUNCH(k_combine_f<T>, dim3((unsigned)ceil_div(n, 256), B), 256, 0, st, n, Y, ys, v, vs, beta, ldab, nev, m, Q, f,
+               fs);
+    TMG_CHECK_LAUNCH();
+}
+
+template <typename T>
+__global__ void k_restart_norm(int64_t n, int nev, const T* __restrict__ dot, const T* __restrict__ f,
+                               const T* __restrict__ Mf, int64_t fs, T* __restrict__ V, T* __restrict__ MV, int64_t vs,
+                               double* __restrict__ beta, int ldab) {
+    const int64_t p = blockIdx.y;
+    const double b = sqrt(fabs(re(dot[p])));
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b > 1e-14) {
+        if (i == 0) beta[p * ldab + nev - 1] = b;
+        if (i < n) {
+            V[p * vs + (int64_t)nev * n + i] = f[p * fs + i] / b;
+            MV[p * vs + (int64_t)nev * n + i] = Mf[p * fs + i] / b;
+        }
+    } else if (i == 0) {
+        beta[p * ldab + nev - 1] = 0.0;
+    }
+}
+template <typename T>
+void lz_restart_norm(cudaStream_t st, int B, int64_t n, int nev, const T* dot, const T* f, const T* Mf, int64_t fs, T* V,
+                     T* MV, int64_t vs, double* beta, int ldab) {
+    TMG_LAUNCH(k_restart_norm<T>, dim3((unsigned)ceil_div(n, 256), B), 256, 0, st, n, nev, dot, f, Mf, fs, V, MV, vs, beta,
+               ldab);
     TMG_CHECK_LAUNCH();
 }
 
@@ -385,67 +448,54 @@ __global__ void k_copy(int64_t n, const T* __restrict__ s, T* __restrict__ d) {
 }
 template <typename T>
 void lz_copy(cudaStream_t st, int64_t n, const T* src, T* dst) {
+    if (n <= 0) return;
     TMG_LAUNCH(k_copy<T>, (unsigned)ceil_div(n, 256), 256, 0, st, n, src, dst);
     TMG_CHECK_LAUNCH();
 }
+
 template <typename T>
-__global__ void k_axpy(int64_t n, double a, const T* __restrict__ x, T* __restrict__ y) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n) y[i] += a * x[i];
-}
-template <typename T>
-void lz_axpy(cudaStream_t st, int64_t n, double a, const T* x, T* y) {
-    TMG_LAUNCH(k_axpy<T>, (unsigned)ceil_div(n, 256), 256, 0, st, n, a, x, y);
-    TMG_CHECK_LAUNCH();
-}
-template <typename T>
-__global__ void k_sub(int64_t n, const T* __restrict__ b, const T* __restrict__ ax, T* __restrict__ r) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n) r[i] = b[i] - ax[i];
-}
-template <typename T>
-void lz_sub(cudaStream_t st, int64_t n, const T* b, const T* ax, T* r) {
-    TMG_LAUNCH(k_sub<T>, (unsigned)ceil_div(n, 256), 256, 0, st, n, b, ax, r);
-    TMG_CHECK_LAUNCH();
-}
-template <typename T>
-__global__ void __launch_bounds__(256) k_norm2a(int64_t n, const T* __restrict__ x, double* __restrict__ partial) {
+__global__ void __launch_bounds__(256) k_norm2a(int64_t n, const T* __restrict__ x, int64_t xs, double* __restrict__ partial) {
     __shared__ double sh[8];
+    const int64_t p = blockIdx.y;
+    x += p * xs;
     const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
     const int64_t lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
     double s = 0.0;
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) s += abs2(x[i]);
     s = block_sum(s, sh);
-    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+    if (threadIdx.x == 0) partial[p * gridDim.x + blockIdx.x] = s;
 }
-__global__ void k_norm2b(int nb, const double* __restrict__ partial, double* __restrict__ out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double s = 0.0;
-        for (int b = 0; b < nb; b++) s += partial[b];
-        out[0] = s;
-    }
+__global__ void k_norm2b(int B, int nb, const double* __restrict__ partial, double* __restrict__ out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= B) return;
+    double s = 0.0;
+    for (int b = 0; b < nb; b++) s += partial[(int64_t)p * nb + b];
+    out[p] = s;
 }
 template <typename T>
-void lz_norm2(cudaStream_t st, int64_t n, const T* x, double* partial, double* out) {
-    TMG_LAUNCH(k_norm2a<T>, LZ_DOT_BLOCKS, 256, 0, st, n, x, partial);
-    TMG_LAUNCH(k_norm2b, 1, 32, 0, st, LZ_DOT_BLOCKS, partial, out);
+void lz_norm2(cudaStream_t st, int B, int64_t n, const T* x, int64_t xs, double* partial, double* out) {
+    TMG_LAUNCH(k_norm2a<T>, dim3(LZ_DOT_BLOCKS, B), 256, 0, st, n, x, xs, partial);
+    TMG_LAUNCH(k_norm2b, (unsigned)ceil_div(B, 128), 128, 0, st, B, LZ_DOT_BLOCKS, partial, out);
     TMG_CHECK_LAUNCH();
 }
 
-#define TMG_LZ_INST(T)                                                                                         \
-    template void lz_spmv<T>(cudaStream_t, const DevCsr<T>&, const T*, T*, int, int64_t, bool);    \
-    template void lz_multidot<T>(cudaStream_t, int64_t, const T*, int64_t, int, const T*, T*, T*);             \
-    template void lz_three_term_dot<T>(cudaStream_t, int64_t, int, const T*, double*, const double*, const T*, T*); \
-    template void lz_gemv_sub<T>(cudaStream_t, int64_t, int, const T*, const T*, T*);                         \
-    template void lz_beta_scale<T>(cudaStream_t, int64_t, int, const T*, const T*, const T*, T*, T*, double*, int*); \
-    template void lz_scale_cols<T>(cudaStream_t, int64_t, const T*, T*, T*);                                 \
-    template void lz_gemm_real<T>(cudaStream_t, int64_t, int, int, const T*, const double*, int, T*);         \
-    template void lz_combine_f<T>(cudaStream_t, int64_t, const T*, const T*, const double*, int, int,          \
-                                  const double*, T*);                                                         \
-    template void lz_copy<T>(cudaStream_t, int64_t, const T*, T*);                                             \
-    template void lz_axpy<T>(cudaStream_t, int64_t, double, const T*, T*);                                     \
-    template void lz_sub<T>(cudaStream_t, int64_t, const T*, const T*, T*);                                    \
-    template void lz_norm2<T>(cudaStream_t, int64_t, const T*, double*, double*);
+#define TMG_LZ_INST(T)                                                                                                 \
+    template void lz_spmv<T>(cudaStream_t, int, const DevCsr<T>&, const T*, int64_t, T*, int64_t, int, int64_t, bool); \
+    template void lz_multidot<T>(cudaStream_t, int, int64_t, const T*, int64_t, int64_t, int, const T*, int64_t, T*, T*); \
+    template void lz_three_term<T>(cudaStream_t, int, int64_t, int, const T*, double*, const double*, int, const T*,  \
+                                   int64_t, T*, int64_t);                                                           \
+    template void lz_gemv_sub<T>(cudaStream_t, int, int64_t, int, const T*, int64_t, const T*, int, T*, int64_t);     \
+    template void lz_beta_scale<T>(cudaStream_t, int, int64_t, int, const T*, const T*, const T*, int64_t, T*, T*,    \
+                                   int64_t, double*, int, int*);                                                    \
+    template void lz_scale_first<T>(cudaStream_t, int, int64_t, const T*, T*, T*, int64_t);                          \
+    template void lz_gemm_real<T>(cudaStream_t, int, int64_t, int, int, const T*, int64_t, const double*, int64_t, int, \
+                                  T*, int64_t);                                                                     \
+    template void lz_combine_f<T>(cudaStream_t, int, int64_t, const T*, int64_t, const T*, int64_t, const double*,    \
+                                  int, int, int, const double*, T*, int64_t);                                       \
+    template void lz_restart_norm<T>(cudaStream_t, int, int64_t, int, const T*, const T*, const T*, int64_t, T*, T*,  \
+                                     int64_t, double*, int);                                                        \
+    template void lz_copy<T>(cudaStream_t, int64_t, const T*, T*);                                                   \
+    template void lz_norm2<T>(cudaStream_t, int, int64_t, const T*, int64_t, double*, double*);
 TMG_LZ_INST(double)
 TMG_LZ_INST(zd)
 

@@ -1,4 +1,8 @@
-// Device kernels of the shift-invert Lanczos eigensolver (FP64 vectors).
+// Device kernels of the shift-invert Lanczos eigensolver, batched over B problems that
+// advance in lockstep (FP64 vectors; per-problem scalars stay on the device).
+//
+// Every vector argument is a batch base pointer with a per-problem stride; scalar arrays
+// (alpha, beta, dots, ...) are laid out problem-major.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -8,7 +12,7 @@
 
 namespace tmg {
 
-// CSR matrix on the device with values of type T.
+// CSR matrix with a shared pattern and per-problem values (val + p * vstride).
 template <typename T>
 struct DevCsr {
     int32_t nrows = 0;
@@ -16,57 +20,64 @@ struct DevCsr {
     const int64_t* rowptr = nullptr;
     const int32_t* col = nullptr;
     const T* val = nullptr;
+    int64_t vstride = 0;
 };
 
-// y(:,v) = A x(:,v) (or y -= A x), ld = leading dimension of x and y.
-template <typename T>
-void lz_spmv(cudaStream_t st, const DevCsr<T>& A, const T* x, T* y, int nvec, int64_t ld, bool subtract = false);
-
-// out[k] = sum_i conj(A[k*lda + i]) * y[i], k < K  (partials buffer: >= nblk * K entries)
-template <typename T>
-void lz_multidot(cudaStream_t st, int64_t n, const T* A, int64_t lda, int K, const T* y, T* partial, T* out);
 constexpr int LZ_DOT_BLOCKS = 152;
 
-// Lanczos step pieces (scalars live on the device).
-// alpha_j = re(dot); w -= alpha_j v_j + beta_{j-1} v_{j-1}
+// y[p](:, v) = A[p] x[p](:, v)   (or y -= A x); vectors of length A.nrows at x + p*xs + v*ld
 template <typename T>
-void lz_three_term_dot(cudaStream_t st, int64_t n, int j, const T* dot, double* alpha, const double* beta, const T* V,
-                       T* w);
-template <typename T>
-void lz_gemv_sub(cudaStream_t st, int64_t n, int K, const T* V, const T* h, T* w);
-template <typename T>
-void lz_beta_scale(cudaStream_t st, int64_t n, int j, const T* dot, const T* w, const T* Mw, T* V, T* MV, double* beta,
-                   int* flag);
-template <typename T>
-void lz_scale_cols(cudaStream_t st, int64_t n, const T* dot, T* x, T* Mx);   // x, Mx /= sqrt(re(dot))
+void lz_spmv(cudaStream_t st, int B, const DevCsr<T>& A, const T* x, int64_t xs, T* y, int64_t ys, int nvec, int64_t ld,
+             bool subtract = false);
 
-// Tridiagonal eigenproblem of (alpha, beta) of size m on one CTA: theta ascending,
+// out[p*K + k] = sum_i conj(A[p*as + k*lda + i]) * y[p*ys + i]; partial: >= B*K*LZ_DOT_BLOCKS
+template <typename T>
+void lz_multidot(cudaStream_t st, int B, int64_t n, const T* A, int64_t as, int64_t lda, int K, const T* y, int64_t ys,
+                 T* partial, T* out);
+
+// alpha[p*ldab + j] = re(dot[p]); w -= alpha_j v_j + beta_{j-1} v_{j-1}
+template <typename T>
+void lz_three_term(cudaStream_t st, int B, int64_t n, int j, const T* dot, double* alpha, const double* beta, int ldab,
+                   const T* V, int64_t vs, T* w, int64_t ws);
+// w[p] -= V[p](:, 0:K) h[p*ldh : ...]
+template <typename T>
+void lz_gemv_sub(cudaStream_t st, int B, int64_t n, int K, const T* V, int64_t vs, const T* h, int ldh, T* w, int64_t ws);
+// beta_j = sqrt|re(dot)|, v_{j+1} = w / beta_j, Mv_{j+1} = Mw / beta_j; flag[p] = j+1 on breakdown
+template <typename T>
+void lz_beta_scale(cudaStream_t st, int B, int64_t n, int j, const T* dot, const T* w, const T* Mw, int64_t ws, T* V,
+                   T* MV, int64_t vs, double* beta, int ldab, int* flag);
+// v_0, Mv_0 /= sqrt(re(dot)) (first basis vector)
+template <typename T>
+void lz_scale_first(cudaStream_t st, int B, int64_t n, const T* dot, T* V, T* MV, int64_t vs);
+
+// Tridiagonal eigenproblem of each problem (one CTA per problem): theta ascending,
 // S (m x m column-major), lambda = shift + 1/theta, order (by lambda), nconv.
-void lz_tridiag(cudaStream_t st, int m, int nev, double shift, double tol, const double* alpha, const double* beta,
-                double* theta, double* S, double* lam, int* order, int* nconv, double* work);
+void lz_tridiag(cudaStream_t st, int B, int m, int ldab, int nev, double shift, double tol, const double* alpha,
+                const double* beta, double* theta, double* S, double* lam, int* order, int* nconv, double* Z);
 
-// Implicit restart: QR shift sweeps on (alpha, beta) with the m-nev smallest theta,
-// accumulating Q (m x m column-major).  rot: scratch of 2*(m-nev)*(m-1) doubles.
-void lz_restart_qr(cudaStream_t st, int m, int nev, const double* theta, double* alpha, double* beta, double* Q,
-                   double* rot);
+// Implicit restart QR sweeps of each problem; Q: m x m per problem; rot: scratch per problem
+void lz_restart_qr(cudaStream_t st, int B, int m, int ldab, int nev, const double* theta, double* alpha, double* beta,
+                   double* Q, double* rot, int64_t rot_stride);
 
-// Y(:, c) = sum_k X(:, k) * C[k + c*ldc], c < ncol (complex/real X, real C)
+// Y[p](:, c) = sum_k X[p](:, k) C[p*cs + k + c*ldc], c < ncol
 template <typename T>
-void lz_gemm_real(cudaStream_t st, int64_t n, int K, int ncol, const T* X, const double* C, int ldc, T* Y);
+void lz_gemm_real(cudaStream_t st, int B, int64_t n, int K, int ncol, const T* X, int64_t xs, const double* C, int64_t cs,
+                  int ldc, T* Y, int64_t ys);
 
-// f = beta[nev-1] * Y + beta[m-1] * Q(m-1, nev-1) * v  (scalars read on the device; beta[m-1]
-// is the dangling coefficient, untouched by the QR sweeps)
+// f = beta[nev-1] * Y + beta[m-1] * Q(m-1, nev-1) * v   (per problem)
 template <typename T>
-void lz_combine_f(cudaStream_t st, int64_t n, const T* Y, const T* v, const double* beta, int nev, int m,
-                  const double* Q, T* f);
+void lz_combine_f(cudaStream_t st, int B, int64_t n, const T* Y, int64_t ys, const T* v, int64_t vs, const double* beta,
+                  int ldab, int nev, int m, const double* Q, T* f, int64_t fs);
+
+// continuation vector normalisation of the restart (src/hermitian_lanczos.cpp:243-254)
+template <typename T>
+void lz_restart_norm(cudaStream_t st, int B, int64_t n, int nev, const T* dot, const T* f, const T* Mf, int64_t fs, T* V,
+                     T* MV, int64_t vs, double* beta, int ldab);
 
 template <typename T>
 void lz_copy(cudaStream_t st, int64_t n, const T* src, T* dst);
+// ||x[p]||^2 -> out[p]
 template <typename T>
-void lz_axpy(cudaStream_t st, int64_t n, double a, const T* x, T* y);     // y += a x
-template <typename T>
-void lz_sub(cudaStream_t st, int64_t n, const T* b, const T* ax, T* r);   // r = b - ax
-template <typename T>
-void lz_norm2(cudaStream_t st, int64_t n, const T* x, double* partial, double* out);   // out = ||x||^2
+void lz_norm2(cudaStream_t st, int B, int64_t n, const T* x, int64_t xs, double* partial, double* out);
 
 }  // namespace tmg

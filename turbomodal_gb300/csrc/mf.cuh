@@ -1,4 +1,9 @@
-// Supernodal multifrontal LDL^H on the device: factorisation and triangular solves.
+// Supernodal multifrontal LDL^H on the device, batched over problems that share one
+// symbolic analysis (e.g. every complex harmonic at one speed).
+//
+// Storage per problem: L panels (m x w column-major per supernode, persistent) and a
+// reusable workspace of update blocks ((m-w) x (m-w) per supernode, live from the start of
+// the supernode's level until its parent's extend-add; offsets from a first-fit plan).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -16,66 +21,98 @@ constexpr int SV_B = 64;       // triangular-solve column block
 constexpr int SV_RC = 256;     // rows per CTA in the forward sweep
 constexpr int SV_CC = 32;      // columns per CTA (four per warp) in the backward sweeps
 
-// Device copy of a Symbolic plus the host-side launch schedule.
+// Per-supernode geometry shared by the kernels.
+struct SnDev {
+    const int32_t* first;      // ns+1
+    const int64_t* row_ptr;    // ns+1 (front row lists; m = row_ptr[s+1]-row_ptr[s])
+    const int32_t* rows;       // global factor rows of each front
+    const int64_t* loff;       // ns+1 L panel offsets
+    const int64_t* uoff;       // ns update-block offsets in the workspace
+    const int32_t* child_ptr;
+    const int32_t* child_list;
+    const int64_t* rel_ptr;
+    const int32_t* rel;
+};
+
+// Device copy of a Symbolic plus the launch schedules.
 struct DevSymbolic {
     int32_t n = 0, ns = 0, max_front = 0;
-    int64_t front_entries = 0;
+    int64_t l_entries = 0;     // L storage per problem (sum m*w)
+    int64_t u_entries = 0;     // update workspace per problem (first-fit peak)
+    int64_t t_entries = 0;     // solve scratch per problem (sum m)
+    int64_t l_stored = 0;      // entries of L actually read by a solve (lower trapezoids)
     int32_t *sn_first = nullptr, *sn_rows = nullptr, *rel = nullptr, *child_ptr = nullptr, *child_list = nullptr;
-    int64_t *sn_row_ptr = nullptr, *front_off = nullptr, *rel_ptr = nullptr;
-    int32_t *perm = nullptr;
-    int32_t *level_sn = nullptr;               // supernodes grouped by level (device copy)
-    // factorisation work lists (device), with host offsets per (level, kb)
-    int32_t* items = nullptr;                  // packed int32 work items
+    int64_t *sn_row_ptr = nullptr, *loff = nullptr, *uoff = nullptr, *rel_ptr = nullptr;
+    int32_t* perm = nullptr;
+    int32_t* level_sn = nullptr;
+    int32_t* items = nullptr;
+    int32_t* sitems = nullptr;
+    int64_t* dest = nullptr;   // scatter destination (L storage) of operator lower entries
+    uint8_t* conj = nullptr;
+    int64_t nlower = 0;
+    double flops = 0.0;        // real flops of one complex factorisation (4 sum c_j^2)
+    size_t bytes = 0;
     struct Step {
-        std::vector<int64_t> ext_off;          // extend-add lists, one per child rank
-        std::vector<int32_t> ext_cnt, ext_max; // items and largest update size per list
+        int32_t level = 0, kb = 0;
+        int64_t uzero_off = 0;                 // (s) items whose update blocks are zeroed
+        int32_t uzero_cnt = 0;
+        int64_t uzero_max = 0;
+        std::vector<int64_t> ext_off;          // extend-add lists (parent, child), one per child rank
+        std::vector<int32_t> ext_cnt, ext_max;
         int64_t diag_off = 0, panel_off = 0, upd_off = 0;
-        int32_t diag_cnt = 0, panel_cnt = 0, upd_cnt = 0, kb = 0;
+        int32_t diag_cnt = 0, panel_cnt = 0, upd_cnt = 0;
     };
-    std::vector<Step> steps;                   // in execution order
-    // triangular-solve schedule: per level, forward block sweeps (s, row0) and backward
-    // sweeps (s, col0), one list per column block
+    std::vector<Step> steps;
     struct SolveLevel {
-        int64_t off_items = 0;                 // backward off-diagonal items (s, col0)
+        int64_t off_items = 0;
         int32_t off_cnt = 0;
         std::vector<int64_t> fwd_off, bwd_off;
         std::vector<int32_t> fwd_cnt, bwd_cnt;
     };
     std::vector<SolveLevel> solve_levels;
-    int32_t* sitems = nullptr;
-    std::vector<int32_t> level_ptr;            // host copy
-    std::vector<int32_t> level_max_m;          // max front size per level
-    int64_t* dest = nullptr;                   // scatter destination of operator lower entries
-    uint8_t* conj = nullptr;
-    int64_t nlower = 0;
-    double flops = 0.0;                        // real flops of one complex factorisation
-    int64_t l_entries = 0;                     // stored L entries (panels)
-    size_t bytes = 0;
+    std::vector<int32_t> level_ptr;
+    SnDev sn() const {
+        return SnDev{sn_first, sn_row_ptr, sn_rows, loff, uoff, child_ptr, child_list, rel_ptr, rel};
+    }
     void upload(const Symbolic& S, const std::vector<int64_t>& dest_h, const std::vector<uint8_t>& conj_h);
     void release();
+    DevSymbolic() = default;
+    DevSymbolic(const DevSymbolic&) = delete;
+    DevSymbolic& operator=(const DevSymbolic&) = delete;
+    ~DevSymbolic() { release(); }
 };
 
-// Numeric factorisation of the fronts in F (already holding the scattered operator).
-// status[0] receives 1 + the first zero-pivot column, or stays 0.
+// B problems sharing one DevSymbolic; per-problem arrays are strided.
 template <typename T>
-void mf_factor(cudaStream_t st, const DevSymbolic& S, T* F, int* status);
+struct Batch {
+    int B = 1;
+    T* L = nullptr;            // B * lstride
+    T* U = nullptr;            // B * ustride
+    int64_t lstride = 0, ustride = 0;
+};
 
+// Scatter operator values (B x nlower, problem stride nlower) into zeroed L panels.
 template <typename T>
-void mf_scatter(cudaStream_t st, const DevSymbolic& S, const T* vals, T* F);
+void mf_scatter(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, const T* vals);
 
-// x_work (factor precision, factor numbering) <- L^-H D^-1 L^-1 x_work
+// Numeric factorisation; status[p] receives 1 + the first zero-pivot column of problem p.
 template <typename T>
-void mf_solve(cudaStream_t st, const DevSymbolic& S, const T* F, T* x, T* tbuf);
+void mf_factor(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, int* status);
 
-// Permutation with precision conversion between the user vector (FP64) and the factor
-// numbering work vector.
-// scale (nullable, original numbering): x[j] = b[perm[j]] * scale[perm[j]] on the way in,
-// out[perm[j]] = x[j] * scale[perm[j]] on the way out.
+// x (B x n, factor numbering, factor precision) <- L^-H D^-1 L^-1 x ; tbuf: B x t_entries
+template <typename T>
+void mf_solve(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, T* x, T* tbuf);
+
+// Permutation with precision conversion between user vectors (problem stride ld) and the
+// factor-numbering work vectors (problem stride n); optional per-problem diagonal scaling
+// (problem stride n, original numbering).
 template <typename T, typename U>
-void mf_permute_in(cudaStream_t st, const DevSymbolic& S, const U* b, T* x, int nvec, int64_t ldb,
-                   const double* scale = nullptr);
+void mf_permute_in(cudaStream_t st, const DevSymbolic& S, int B, const U* b, int64_t ldb, T* x, const double* scale);
 template <typename T, typename U>
-void mf_permute_out(cudaStream_t st, const DevSymbolic& S, const T* x, U* out, int nvec, int64_t ldo,
-                    const double* scale = nullptr);
+void mf_permute_out(cudaStream_t st, const DevSymbolic& S, int B, const T* x, U* out, int64_t ldo, const double* scale);
+
+// Count non-positive pivots of each problem into cnt[p].
+template <typename T>
+void mf_count_nonpos(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, int* cnt);
 
 }  // namespace tmg

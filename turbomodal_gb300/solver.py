@@ -97,8 +97,9 @@ class CyclicSymmetrySolver:
             meta = _lib.ResultMeta()
             L.tmg_result_info(h, idx, C.byref(meta))
             if meta.status != _lib.TMG_OK:
+                detail = L.tmg_last_error(h).decode(errors="replace")
                 sys.stderr.write(f"[CyclicSolver] k={meta.harmonic_index} FAILED: "
-                                 f"{_lib.ERRORS.get(meta.status, meta.status)}\n")
+                                 f"{_lib.ERRORS.get(meta.status, meta.status)} ({detail})\n")
                 continue
             m = meta.num_modes
             f = np.zeros(m)
@@ -174,10 +175,11 @@ class CyclicSymmetrySolver:
         return A
 
     def symbolic_stats(self, kind: int = 0) -> dict:
-        out = np.zeros(8)
+        out = np.zeros(10)
         self.ctx.check(self.ctx.L.tmg_symbolic_stats(self.ctx.h, kind, _lib.ptr(out, C.c_double)),
                        "tmg_symbolic_stats")
-        keys = ["n", "nnz_l", "supernodes", "levels", "max_front", "front_entries", "flops", "lower_entries"]
+        keys = ["n", "nnz_l", "supernodes", "levels", "max_front", "l_entries", "flops", "lower_entries",
+                "u_entries", "l_stored"]
         return {k: float(v) for k, v in zip(keys, out)}
 
     def symbolic(self, kind: int = 0):
