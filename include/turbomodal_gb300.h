@@ -150,6 +150,29 @@ int tmg_last_timing(tmg_context* ctx, double* phase_ms, int nphase, int64_t* ker
 int tmg_set_profiling(tmg_context* ctx, int on);
 int tmg_profile_solve(tmg_context* ctx, double* out);
 
+/* Complex FP64 entries the static scratch of tmg_projection_harmonic_static holds (8 MiB). */
+#define TMG_STATIC_SCRATCH_ENTRIES 524288
+
+/* tmg_projection for TMG_MAT_KK / TMG_MAT_MK with no device allocation: no counterpart in the
+ * reference (its per-harmonic sums, cyclic_solver.cpp:942-947, run on the CPU).  The matrix is
+ * formed in one file-scope __device__ array of TMG_STATIC_SCRATCH_ENTRIES complex entries per
+ * device instead of a per-call device buffer; the call makes no cudaMalloc / cudaFree and no
+ * other allocating call, and its output equals tmg_projection's.  For callers that cannot
+ * allocate device memory at that point: a process whose whole device budget is committed to
+ * resident factors and Lanczos bases, or a host thread that must not wait on the device-wide
+ * synchronisation cudaFree performs.
+ *  - A matrix with more than TMG_STATIC_SCRATCH_ENTRIES entries is rejected with TMG_ERR_ARG
+ *    (*nnz is still set); use tmg_projection for it.
+ *  - No scratch entry needs to start at zero: every entry copied out is written first.
+ *  - One scratch array per device is shared by every context on that device: calls that
+ *    overlap in time on one device (two host threads, or two contexts) race on it.  The call
+ *    synchronises its stream before returning, so calls made one after another are safe.
+ *  - The first call on a device looks the array's address up (cudaGetSymbolAddress, with the
+ *    context's device current); make that first call before any stream capture begins.
+ * Pass NULL arrays to query *nnz and *n. */
+int tmg_projection_harmonic_static(tmg_context* ctx, int which, int k, int64_t* nnz, int32_t* n,
+                                   int32_t* colptr, int32_t* rowidx, double* values);
+
 #ifdef __cplusplus
 }
 #endif

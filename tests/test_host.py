@@ -46,7 +46,7 @@ def test_header_names_reference_interfaces():
     for fn in declared_functions():
         # every entry point's comment block cites the reference file it replaces, or says it has none
         i = txt.index(fn + "(")
-        block = txt[max(0, i - 900): i]
+        block = txt[max(0, i - 1800): i]
         assert re.search(r"\.(cpp|hpp|py):\d+", block) or "no counterpart" in block or "Profiling" in block \
             or "Time (ms)" in block or "Size of the symbolic" in block, fn
 

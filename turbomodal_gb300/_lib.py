@@ -22,11 +22,12 @@ MAT = {"K": 0, "M": 1, "Komega": 2, "G": 3, "Ksigma": 4, "Keff": 5,
        "Kcf": 10, "Kpf": 11, "Mcf": 12, "Mpf": 13, "Gcf": 14, "Gpf": 15,
        "K0r": 20, "M0r": 21, "Khr": 22, "Mhr": 23, "Kk": 30, "Mk": 31}
 PREC = {"fp64": 0, "mixed": 1}
+STATIC_SCRATCH_ENTRIES = 524288   # TMG_STATIC_SCRATCH_ENTRIES
 
 EXPORTED = ["tmg_create", "tmg_destroy", "tmg_last_error", "tmg_upload_sector", "tmg_assemble",
             "tmg_prepare", "tmg_projection", "tmg_symbolic", "tmg_solve_at_rpm", "tmg_result_info",
             "tmg_result_copy", "tmg_last_timing", "tmg_symbolic_stats",
-            "tmg_set_profiling", "tmg_profile_solve"]
+            "tmg_set_profiling", "tmg_profile_solve", "tmg_projection_harmonic_static"]
 
 
 class SectorDesc(C.Structure):
@@ -80,6 +81,7 @@ def load(build_if_missing: bool = True):
     L.tmg_last_timing.argtypes = [P, DP, C.c_int, I64P]
     L.tmg_set_profiling.argtypes = [P, C.c_int]
     L.tmg_profile_solve.argtypes = [P, DP]
+    L.tmg_projection_harmonic_static.argtypes = [P, C.c_int, C.c_int, I64P, I32P, I32P, I32P, DP]
     _lib = L
     return L
 

@@ -12,6 +12,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <random>
 #include <set>
@@ -1848,3 +1849,81 @@ int tmg_last_timing(tmg_context* c, double* phase_ms, int nphase, int64_t* kerne
 }
 
 }  // extern "C"
+
+// ---- per-harmonic K_k / M_k without device allocation ---------------------------------
+// tmg_projection forms K_k (or M_k) on the union pattern into a device buffer it allocates
+// per call, then copies it to the caller.  This variant forms it into one file-scope device
+// array instead, so the call performs no cudaMalloc / cudaFree and uploads nothing: the phase
+// e^{ik alpha} travels as kernel arguments.  The arithmetic is the same as k_form_csum.
+namespace {
+
+__device__ __align__(256) double g_harmonic_scratch[2 * TMG_STATIC_SCRATCH_ENTRIES];
+
+constexpr int kMaxScratchDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_addr[kMaxScratchDevices] = {};
+
+// Address of this device's copy of the scratch array, looked up once per device with the
+// device current (the caller made it current).
+zd* static_scratch(int device) {
+    if (device < 0 || device >= kMaxScratchDevices)
+        throw std::invalid_argument("device ordinal beyond the static-scratch table");
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_addr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_harmonic_scratch);
+        if (e != cudaSuccess)
+            throw cuda_error(std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(e));
+        g_scratch_addr[device] = p;
+    }
+    return reinterpret_cast<zd*>(g_scratch_addr[device]);
+}
+
+__global__ void k_form_csum_static(int64_t n, const int64_t* __restrict__ ic, const int64_t* __restrict__ ip,
+                                   const int64_t* __restrict__ ih, const double* __restrict__ c,
+                                   const double* __restrict__ pv, double pre, double pim, zd* __restrict__ out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const double a = ic[e] >= 0 ? c[ic[e]] : 0.0;
+    const double b = ip[e] >= 0 ? pv[ip[e]] : 0.0;
+    const double h = ih[e] >= 0 ? pv[ih[e]] : 0.0;
+    const zd P{pre, pim}, Pc{pre, -pim};
+    out[e] = (zd{a, 0.0} + P * zd{b, 0.0}) + Pc * zd{h, 0.0};
+}
+
+}  // namespace
+
+extern "C" int tmg_projection_harmonic_static(tmg_context* c, int which, int k, int64_t* nnz, int32_t* n,
+                                              int32_t* colptr, int32_t* rowidx, double* values) {
+    if (!c || !nnz) return TMG_ERR_ARG;
+    if (which != TMG_MAT_KK && which != TMG_MAT_MK)
+        return set_err(c, TMG_ERR_ARG, "tmg_projection_harmonic_static forms TMG_MAT_KK or TMG_MAT_MK only");
+    if (!c->prepared) return set_err(c, TMG_ERR_STATE, "call tmg_prepare first");
+    return guarded(c, [&]() {
+        Sector& S = *c->sec;
+        const UnionMaps& w = which == TMG_MAT_KK ? c->W0 : c->WM0;
+        const FreeMat& cc = which == TMG_MAT_KK ? c->Kcf : c->Mcf;
+        const FreeMat& pp = which == TMG_MAT_KK ? c->Kpf : c->Mpf;
+        const int64_t ne = w.U.nnz();
+        if (n) *n = S.n_free;
+        *nnz = ne;
+        if (ne > (int64_t)TMG_STATIC_SCRATCH_ENTRIES)
+            return set_err(c, TMG_ERR_ARG, "the harmonic matrix has " + std::to_string(ne) +
+                                               " entries; the static scratch holds at most " +
+                                               std::to_string((long long)TMG_STATIC_SCRATCH_ENTRIES) +
+                                               " (use tmg_projection)");
+        if (!colptr) return TMG_OK;
+        zd* out = static_scratch(c->device);
+        const double alpha = 2.0 * PI / S.ns;
+        if (ne)
+            TMG_LAUNCH(k_form_csum_static, nblk(ne), 256, 0, c->st, ne, w.maps[0].p, w.maps[1].p, w.maps[2].p, cc.v.p,
+                       pp.v.p, std::cos(k * alpha), std::sin(k * alpha), out);
+        TMG_CHECK_LAUNCH();
+        for (int32_t j = 0; j <= w.U.ncols; j++) colptr[j] = (int32_t)w.U.p[j];
+        if (rowidx) std::copy(w.U.i.begin(), w.U.i.end(), rowidx);
+        if (values && ne)
+            TMG_CUDA(cudaMemcpyAsync(values, out, (size_t)ne * sizeof(zd), cudaMemcpyDeviceToHost, c->st));
+        TMG_CUDA(cudaStreamSynchronize(c->st));
+        return TMG_OK;
+    });
+}
