@@ -139,8 +139,9 @@ int tmg_result_copy(tmg_context* ctx, int idx, double* freqs, double* shapes, in
 
 /* Time (ms) of the phases of the last tmg_solve_at_rpm: [0] prepare (assembly, prestress,
  * projections), [1] factorisations, [2] Lanczos, [3] post-processing, [4] the whole call
- * measured with CUDA events on the context's stream; and the number of this library's
- * kernel launches in it. */
+ * measured with CUDA events on the context's stream; counts: [5] batched triangular solves,
+ * [6] shift-invert applications, [7] most refinement iterations of one application; and the
+ * number of this library's kernel launches in it. */
 int tmg_last_timing(tmg_context* ctx, double* phase_ms, int nphase, int64_t* kernel_launches);
 
 /* Profiling mode (measurement only; it synchronises after every triangular solve): CUDA-event

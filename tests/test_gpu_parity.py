@@ -200,8 +200,9 @@ def test_leissa_clamped_disk_gpu(oracle):
 
 
 def test_full_size_sector_properties():
-    """Config-1 mesh (57,897 nodes) at one speed: mixed vs FP64 frequencies within 1e-6,
-    ascending, small residuals, finite modal masses (size-independent properties)."""
+    """Config-1 mesh (57,897 nodes) at one speed: mixed vs FP64 frequencies within 1e-6 and
+    mode MAC >= 0.999, ascending frequencies, bounded residuals, every refined solve at its
+    1e-10 target, finite positive modal masses (size-independent properties)."""
     from turbomodal_gb300.meshgen import TITANIUM, config_mesh
     from turbomodal_gb300.solver import CyclicSymmetrySolver, _modal_mass_from_M
 
@@ -214,8 +215,11 @@ def test_full_size_sector_properties():
         assert a.harmonic_index == b.harmonic_index
         assert np.all(np.diff(b.frequencies) >= -1e-9 * b.frequencies[1:])
         assert np.max(np.abs(a.frequencies - b.frequencies) / b.frequencies) <= FREQ_TOL
-        assert b.max_residual < 1e-6 and a.max_residual < 1e-4
-        assert a.refine_residual <= 1e-11
+        assert b.max_residual < 1e-6 and a.max_residual < 1e-3
+        assert a.refine_residual <= 1e-10
+        for q in range(len(a.frequencies)):
+            cluster = np.abs(b.frequencies - a.frequencies[q]) <= 1e-6 * a.frequencies[q]
+            assert subspace_mac(a.mode_shapes[:, q], b.mode_shapes[:, cluster]) >= MAC_MIN
     M = s.assemble("M")
     for mm in _modal_mass_from_M(M, fp64, m.num_sectors):
         assert np.all(np.isfinite(mm)) and np.all(mm > 0)

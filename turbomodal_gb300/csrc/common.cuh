@@ -69,6 +69,11 @@ template <> HD double zero_of<double>() { return 0.0; }
 template <> HD float zero_of<float>() { return 0.0f; }
 template <> HD zd zero_of<zd>() { return zd{0.0, 0.0}; }
 template <> HD zf zero_of<zf>() { return zf{0.0f, 0.0f}; }
+template <typename T> HD T one_of();
+template <> HD double one_of<double>() { return 1.0; }
+template <> HD float one_of<float>() { return 1.0f; }
+template <> HD zd one_of<zd>() { return zd{1.0, 0.0}; }
+template <> HD zf one_of<zf>() { return zf{1.0f, 0.0f}; }
 
 // conversion between precisions (used at the mixed-precision boundary)
 template <typename To, typename From> HD To conv(From a);

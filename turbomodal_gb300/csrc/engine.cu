@@ -11,6 +11,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <numeric>
@@ -1004,7 +1006,7 @@ struct ShiftInvertB {
     bool mixed = false;
     bool spd = false;             // every pivot positive: CG-accelerated refinement
     int max_iter = 30;            // refinement iterations per solve (mixed)
-    double rtol = 1e-12;          // relative residual target of a refined solve (mixed)
+    double rtol = 1e-10;          // relative residual target of a refined solve (mixed)
     DevCsr<Tv> A;                 // FP64 operator K - sigma M (CSR, per-problem values)
     DVec<Tf> L, U, tb, xw;
     DVec<Tv> gin, gout, r, d, z, pp, q, sc, bin;
@@ -1066,6 +1068,7 @@ struct ShiftInvertB {
         np.alloc((size_t)B * LZ_DOT_BLOCKS);
         nrm.alloc(B);
         ddone.alloc(B);
+        ddone.zero(c->st);
         worst.assign(B, 0.0);
     }
     Batch<Tf> batch() const { return Batch<Tf>{B, L.p, nullptr, D->l_entries, 0}; }
@@ -1079,7 +1082,7 @@ struct ShiftInvertB {
             cudaGraph_t g;
             TMG_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
             mf_permute_in<Tf, Tv>(c->st, *D, B, gin.p, n, xw.p, s);
-            mf_solve<Tf>(c->st, *D, batch(), xw.p, tb.p);
+            mf_solve<Tf>(c->st, *D, batch(), xw.p, tb.p, ddone.p);
             mf_permute_out<Tf, Tv>(c->st, *D, B, xw.p, gout.p, n, s);
             TMG_CUDA(cudaStreamEndCapture(c->st, &g));
             TMG_CUDA(cudaGraphInstantiate(&gexec, g, 0));
@@ -1125,7 +1128,11 @@ struct ShiftInvertB {
                                        cudaMemcpyDeviceToDevice, c->st));
             b = bin.p;
         }
-        if (!mixed) { solve1(b, x); return; }
+        if (!mixed) {   // finished problems are skipped by the solve kernels
+            TMG_CUDA(cudaMemcpyAsync(ddone.p, skip.data(), B * sizeof(int), cudaMemcpyHostToDevice, c->st));
+            solve1(b, x);
+            return;
+        }
         const std::vector<double> bn = norms(b);
         std::vector<int> done(skip);
         std::vector<double> rn;
@@ -1414,6 +1421,15 @@ void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os
     auto t2 = std::chrono::steady_clock::now();
     c->phase_ms[1] += std::chrono::duration<double, std::milli>(t1 - t0).count();
     c->phase_ms[2] += std::chrono::duration<double, std::milli>(t2 - t1).count();
+    c->phase_ms[5] += (double)op.solves;
+    c->phase_ms[6] += (double)op.applies;
+    c->phase_ms[7] = std::max(c->phase_ms[7], (double)op.max_its);
+    if (std::getenv("TMG_VERBOSE"))
+        std::fprintf(stderr, "[tmg] batch B=%d n=%d %s: factor %.1f ms, lanczos %.1f ms, %lld solves (%lld launches each), "
+                     "%lld applies, <=%lld refinement iterations\n", B, op.n, mixed ? "mixed" : "fp64",
+                     std::chrono::duration<double, std::milli>(t1 - t0).count(),
+                     std::chrono::duration<double, std::milli>(t2 - t1).count(), (long long)op.solves,
+                     (long long)op.launches_per_solve, (long long)op.applies, (long long)op.max_its);
     for (int p = 0; p < B; p++) {
         ResultHost& R = *probs[p].R;
         R.converged = eo[p].converged;

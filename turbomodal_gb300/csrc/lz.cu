@@ -8,27 +8,45 @@
 
 namespace tmg {
 
+// y = A x (or y -= A x) for CSR A; one warp per row, lanes stride the row's entries so the
+// value and column loads are coalesced; grid y = vector, z = problem.
 template <typename T>
-__global__ void k_spmv(int32_t nrows, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
-                       const T* __restrict__ av, int64_t vstride, const T* __restrict__ x, int64_t xs,
-                       T* __restrict__ y, int64_t ys, int64_t ld, int sub) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= nrows) return;
+__device__ __forceinline__ T lz_warp_sum(T v) {
+    using R = typename real_of<T>::type;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        R* q = reinterpret_cast<R*>(&v);
+        q[0] += __shfl_xor_sync(0xffffffff, q[0], o);
+        if constexpr (sizeof(T) == 2 * sizeof(R)) q[1] += __shfl_xor_sync(0xffffffff, q[1], o);
+    }
+    return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_spmv(int32_t nrows, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                              const T* __restrict__ av, int64_t vstride, const T* __restrict__ x,
+                                              int64_t xs, T* __restrict__ y, int64_t ys, int64_t ld, int sub) {
+    const int64_t i = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= nrows) return;                      // uniform per warp
     const int64_t v = blockIdx.y, p = blockIdx.z;
     const T* xv = x + p * xs + v * ld;
     const T* a = av + p * vstride;
     T s = zero_of<T>();
-    for (int64_t q = rp[i]; q < rp[i + 1]; q++) s += a[q] * xv[ci[q]];
-    T* yv = y + p * ys + v * ld;
-    if (sub) yv[i] -= s;
-    else yv[i] = s;
+    for (int64_t q = rp[i] + lane; q < rp[i + 1]; q += 32) s += a[q] * xv[ci[q]];
+    s = lz_warp_sum(s);
+    if (lane == 0) {
+        T* yv = y + p * ys + v * ld;
+        if (sub) yv[i] -= s;
+        else yv[i] = s;
+    }
 }
 
 template <typename T>
 void lz_spmv(cudaStream_t st, int B, const DevCsr<T>& A, const T* x, int64_t xs, T* y, int64_t ys, int nvec, int64_t ld,
              bool subtract) {
     if (A.nrows == 0 || nvec == 0 || B == 0) return;
-    TMG_LAUNCH(k_spmv<T>, dim3((unsigned)ceil_div(A.nrows, 128), nvec, B), 128, 0, st, A.nrows, A.rowptr, A.col, A.val,
+    TMG_LAUNCH(k_spmv<T>, dim3((unsigned)ceil_div(A.nrows, 8), nvec, B), 256, 0, st, A.nrows, A.rowptr, A.col, A.val,
                A.vstride, x, xs, y, ys, ld, subtract ? 1 : 0);
     TMG_CHECK_LAUNCH();
 }

@@ -4,8 +4,11 @@
 // level's update blocks are zeroed, children's update blocks are added into their parents
 // (one launch per child rank, so no two writers touch one entry and the sums run in a fixed
 // order), then each front is partially factorised by 32-wide pivot blocks: diagonal block
-// (one CTA per front), panel rows (CTA per 64 rows), and the Schur update of the trailing
-// lower triangle (CTA per 64x64 tile).  Every launch covers all problems of the batch
+// (one CTA per front), panel rows (CTA per 64 rows), and the Schur update (CTA per 64x64
+// tile) in two levels: a pivot block updates only the rest of its 256-column super-block,
+// and when a super-block is complete one update with K = 256 covers everything right of it
+// (remaining panel columns and the update block), so the large trailing matrices are read
+// and written once per super-block.  Every launch covers all problems of the batch
 // (grid y or z = problem).  The reference factorises the same operator with Eigen's
 // simplicial up-looking LDL^T (src/hermitian_lanczos.cpp:12-56); the supernodal form has the
 // same L and D in exact arithmetic.
@@ -163,63 +166,71 @@ __global__ void __launch_bounds__(64) k_panel(const int32_t* __restrict__ items,
         if (j < nb) Fs[(int64_t)(k0 + j) * m + i] = x[j];
 }
 
-// Trailing lower-triangle update: C(i,j) -= sum_l L(i,l) d_l conj(L(j,l)) over the pivot block
+// Lower-triangle update of one 64x64 tile at front rows [i0, i0+64), columns [j0, j0+64):
+//   C(i, j) -= sum_{l in [kl, kh)} L(i, l) d_l conj(L(j, l)),  i >= j, j < jmax,
+// with kh = min(kl + kw, w), the K range staged through shared memory 32 columns at a time.
+// Pivot mode (trail == 0): kl is one pivot block and jmax ends the block's 256-column
+// super-block (updates stay inside it).  Trail mode: [kl, kh) is a whole super-block and
+// the tile lies right of it (panel columns beyond it and the update block).
 template <typename T>
-__global__ void __launch_bounds__(256) k_update(const int32_t* __restrict__ items, int kb, SnDev S, T* __restrict__ L,
-                                                T* __restrict__ U, int64_t lstride, int64_t ustride) {
+__global__ void __launch_bounds__(256) k_update(const int32_t* __restrict__ items, int kl, int kw, int trail, SnDev S,
+                                                T* __restrict__ L, T* __restrict__ U, int64_t lstride,
+                                                int64_t ustride) {
     using R = typename real_of<T>::type;
     extern __shared__ unsigned char smem_raw[];
     T* Li = reinterpret_cast<T*>(smem_raw);                  // [MF_NB][MF_TILE]
     T* Lj = Li + MF_NB * MF_TILE;                            // [MF_NB][MF_TILE], scaled by d
     const int64_t p = blockIdx.y;
     const int s = items[3 * blockIdx.x];
-    const int ti = items[3 * blockIdx.x + 1], tj = items[3 * blockIdx.x + 2];
+    const int64_t i0 = items[3 * blockIdx.x + 1], j0 = items[3 * blockIdx.x + 2];
     const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
     const int w = S.first[s + 1] - S.first[s];
-    const int k0 = kb * MF_NB;
-    const int nb = min(MF_NB, w - k0);
-    const int64_t t0 = k0 + nb;
-    const int64_t i0 = t0 + (int64_t)ti * MF_TILE, j0 = t0 + (int64_t)tj * MF_TILE;
+    const int kh = min(kl + kw, w);
+    const int64_t jmax = trail ? m : (int64_t)min((kl / MF_SB + 1) * MF_SB, w);
     T* Lp = L + p * lstride;
     T* Up = U + p * ustride;
     const T* Fs = Lp + S.loff[s];
-    for (int q = threadIdx.x; q < MF_NB * MF_TILE; q += blockDim.x) {
-        const int r = q % MF_TILE, l = q / MF_TILE;
-        T a = zero_of<T>(), b = zero_of<T>();
-        if (l < nb) {
-            if (i0 + r < m) a = Fs[(int64_t)(k0 + l) * m + i0 + r];
-            if (j0 + r < m) {
-                const R d = re(Fs[(int64_t)(k0 + l) * m + k0 + l]);
-                b = d * Fs[(int64_t)(k0 + l) * m + j0 + r];
-            }
-        }
-        Li[l * MF_TILE + r] = a;
-        Lj[l * MF_TILE + r] = b;
-    }
-    __syncthreads();
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     T acc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; a++)
 #pragma unroll
         for (int b = 0; b < 4; b++) acc[a][b] = zero_of<T>();
-    for (int l = 0; l < nb; l++) {
-        T av[4], bv[4];
+    for (int k0 = kl; k0 < kh; k0 += MF_NB) {
+        const int nb = min(MF_NB, kh - k0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < MF_NB * MF_TILE; q += blockDim.x) {
+            const int r = q % MF_TILE, l = q / MF_TILE;
+            T a = zero_of<T>(), b = zero_of<T>();
+            if (l < nb) {
+                if (i0 + r < m) a = Fs[(int64_t)(k0 + l) * m + i0 + r];
+                if (j0 + r < m) {
+                    const R d = re(Fs[(int64_t)(k0 + l) * m + k0 + l]);
+                    b = d * Fs[(int64_t)(k0 + l) * m + j0 + r];
+                }
+            }
+            Li[l * MF_TILE + r] = a;
+            Lj[l * MF_TILE + r] = b;
+        }
+        __syncthreads();
+        for (int l = 0; l < nb; l++) {
+            T av[4], bv[4];
 #pragma unroll
-        for (int a = 0; a < 4; a++) av[a] = Li[l * MF_TILE + ty + 16 * a];
+            for (int a = 0; a < 4; a++) av[a] = Li[l * MF_TILE + ty + 16 * a];
 #pragma unroll
-        for (int b = 0; b < 4; b++) bv[b] = conj(Lj[l * MF_TILE + tx + 16 * b]);
+            for (int b = 0; b < 4; b++) bv[b] = conj(Lj[l * MF_TILE + tx + 16 * b]);
 #pragma unroll
-        for (int a = 0; a < 4; a++)
+            for (int a = 0; a < 4; a++)
 #pragma unroll
-            for (int b = 0; b < 4; b++) acc[a][b] += av[a] * bv[b];
+                for (int b = 0; b < 4; b++) acc[a][b] += av[a] * bv[b];
+        }
     }
 #pragma unroll
     for (int a = 0; a < 4; a++)
 #pragma unroll
         for (int b = 0; b < 4; b++) {
             const int64_t i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
-            if (i < m && j < m && i >= j) *fent(S, Lp, Up, s, m, w, i, j) -= acc[a][b];
+            if (i < m && j < jmax && i >= j) *fent(S, Lp, Up, s, m, w, i, j) -= acc[a][b];
         }
 }
 
@@ -238,14 +249,12 @@ __global__ void k_count_nonpos(int32_t ns, SnDev S, const T* __restrict__ L, int
 }
 
 // ------------------------------------------------------------------------------------
-// Triangular solves, level by level.  Forward: gather the front vector (own entries +
-// children's update vectors, children in fixed order), then sweep 64-wide column blocks:
-// every CTA of a front re-solves the small diagonal block (staged in shared memory) from
-// the final block entries and updates its own 256 rows below it, so a large front is spread
-// over many CTAs and the only sequential chain is the column-block loop.  Backward:
-// off-diagonal products with the ancestors' solution (warp per column), then column blocks
-// from the last one, each CTA re-solving the diagonal block and updating its own columns to
-// the left.  grid y = problem.
+// Diagonal-block inverses.  After the numeric factorisation, every diagonal block of width
+// NB (the block of columns [b*NB, b*NB + nbb) and the same rows) is replaced below its
+// diagonal by the strict lower part of its unit-lower inverse X = L_bb^-1, computed by
+// forward substitution on the columns of the identity (lanes hold rows, warp shuffles carry
+// the solved entry).  The triangular solves then apply a block as one dense product, with
+// no sequential dependency inside it.
 template <typename T>
 __device__ __forceinline__ T shfl_t(T v, int src) {
     using R = typename real_of<T>::type;
@@ -268,20 +277,155 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
+// warps (items) per CTA of k_inv_small: its shared block copies stay under 48 KB
+template <typename T>
+constexpr int inv_wpc() { return sizeof(T) >= 16 ? 2 : 4; }
+
+// item = (s, b) with a block of at most 32 columns; one warp per item
+template <typename T, int NB>
+__global__ void __launch_bounds__(128) k_inv_small(const int32_t* __restrict__ items, int cnt, SnDev S,
+                                                   T* __restrict__ L, int64_t lstride) {
+    __shared__ T Lb[inv_wpc<T>()][32][33];
+    const int64_t p = blockIdx.y;
+    const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int it = blockIdx.x * inv_wpc<T>() + wi;
+    if (it >= cnt) return;                       // uniform per warp; only warp-level sync below
+    const int s = items[2 * it], b = items[2 * it + 1];
+    const int w = S.first[s + 1] - S.first[s];
+    const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
+    const int b0 = b * NB;
+    const int nbb = min(NB, w - b0);             // <= 32 by construction of the item list
+    T* Fs = L + p * lstride + S.loff[s];
+    for (int k = 0; k < nbb; k++)
+        if (lane > k && lane < nbb) Lb[wi][lane][k] = Fs[(int64_t)(b0 + k) * m + b0 + lane];
+    __syncwarp();
+    for (int j = 0; j < nbb - 1; j++) {
+        T v = lane == j ? one_of<T>() : zero_of<T>();
+        for (int k = j; k < nbb - 1; k++) {
+            const T xk = shfl_t(v, k);
+            if (lane > k && lane < nbb) v -= Lb[wi][lane][k] * xk;
+        }
+        if (lane > j && lane < nbb) Fs[(int64_t)(b0 + j) * m + b0 + lane] = v;
+    }
+}
+
+// item = (s, b) with a block wider than 32 columns; one CTA per item, warp per column
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) k_inv_large(const int32_t* __restrict__ items, SnDev S, T* __restrict__ L,
+                                                   int64_t lstride) {
+    extern __shared__ unsigned char inv_smem[];
+    T* Lb = reinterpret_cast<T*>(inv_smem);      // Lb[i * (NB + 1) + k] = L(b0 + i, b0 + k)
+    constexpr int R = NB / 32;                   // rows per lane
+    const int64_t p = blockIdx.y;
+    const int s = items[2 * blockIdx.x], b = items[2 * blockIdx.x + 1];
+    const int w = S.first[s + 1] - S.first[s];
+    const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
+    const int b0 = b * NB;
+    const int nbb = min(NB, w - b0);
+    T* Fs = L + p * lstride + S.loff[s];
+    for (int q = threadIdx.x; q < NB * NB; q += blockDim.x) {
+        const int i = q % NB, k = q / NB;
+        if (i < nbb && k < i) Lb[i * (NB + 1) + k] = Fs[(int64_t)(b0 + k) * m + b0 + i];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int j = warp; j < nbb - 1; j += 8) {
+        T v[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) v[r] = lane + 32 * r == j ? one_of<T>() : zero_of<T>();
+        for (int k = j; k < nbb - 1; k++) {
+            T src = v[0];
+#pragma unroll
+            for (int r = 1; r < R; r++)
+                if ((k >> 5) == r) src = v[r];   // uniform across the warp
+            const T xk = shfl_t(src, k & 31);
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const int i = lane + 32 * r;
+                if (i > k && i < nbb) v[r] -= Lb[i * (NB + 1) + k] * xk;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int i = lane + 32 * r;
+            if (i > j && i < nbb) Fs[(int64_t)(b0 + j) * m + b0 + i] = v[r];
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Triangular solves, level by level (grid y = problem).  Front s has w pivot columns and m
+// rows; its panel is L(r, j) = Fs[j * m + r] and its solve vector t (m entries) holds the
+// pivot part first and the update for the parent after it.
+//
+// Forward, per level: gather assembles t from x and the children's updates and applies the
+// first diagonal block (y_0 = X_0 t_0); each triangle launch b subtracts block b's product
+// from the triangle rows below it, and the CTA holding block b+1's rows then applies X_{b+1}
+// (look-ahead), so the next launch finds y_{b+1} ready; one rectangle launch then forms the
+// parent update t[w..m) -= L21 y.  x receives D^-1 y.
+// Backward, per level (top first): one rectangle launch forms z = x - L21^H x(rows) per
+// column chunk and applies X^H to the last block; each triangle launch b subtracts block b's
+// contribution from the columns left of it, and the CTA holding block b-1 applies X_{b-1}^H.
 struct SolveArgs {
     int64_t lstride, xstride, tstride;
+    const int* skip;   // per problem: nonzero = leave this problem's vectors alone (may be null)
 };
+
+constexpr int XS_LD = 65;                        // padded leading dimension of a staged 64x64 block
+
+// Stage the strict lower part of the inverse block at column c0 (nbk <= 64 columns) into
+// Xs[k * XS_LD + i] = X(i, k); every thread issues its loads at once.
+template <typename T>
+__device__ __forceinline__ void stage_x(const T* Fs, int64_t m, int c0, int nbk, T* Xs) {
+#pragma unroll 4
+    for (int q = threadIdx.x; q < 64 * 64; q += 256) {
+        const int i = q & 63, k = q >> 6;
+        if (k < nbk && i > k && i < nbk) Xs[k * XS_LD + i] = Fs[(int64_t)(c0 + k) * m + c0 + i];
+    }
+}
+
+// v = X u (unit lower X staged in Xs, u in shared memory, nbk entries); four threads per row,
+// red: 256 shared scratch entries.  Result for row i in v[i].  Called by all 256 threads.
+template <typename T>
+__device__ __forceinline__ void apply_x(const T* Xs, const T* u, int nbk, T* red, T* v) {
+    const int i = threadIdx.x & 63, pi = threadIdx.x >> 6;
+    T a = zero_of<T>();
+    if (i < nbk)
+        for (int k = pi; k < i; k += 4) a += Xs[k * XS_LD + i] * u[k];
+    red[threadIdx.x] = a;
+    __syncthreads();
+    if (threadIdx.x < nbk) v[i] = u[i] + ((red[i] + red[i + 64]) + (red[i + 128] + red[i + 192]));
+}
+
+// v = X^H u, same layout
+template <typename T>
+__device__ __forceinline__ void apply_xh(const T* Xs, const T* u, int nbk, T* red, T* v) {
+    const int i = threadIdx.x & 63, pi = threadIdx.x >> 6;
+    T a = zero_of<T>();
+    if (i < nbk)
+        for (int k = i + 1 + pi; k < nbk; k += 4) a += conj(Xs[i * XS_LD + k]) * u[k];
+    red[threadIdx.x] = a;
+    __syncthreads();
+    if (threadIdx.x < nbk) v[i] = u[i] + ((red[i] + red[i + 64]) + (red[i + 128] + red[i + 192]));
+}
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_fwd_gather(const int32_t* __restrict__ lvl, SnDev S, SolveArgs A,
-                                                    const T* __restrict__ x, T* __restrict__ tbuf) {
+                                                    const T* __restrict__ L, T* __restrict__ x, T* __restrict__ tbuf) {
+    extern __shared__ unsigned char sv_smem[];
+    T* Xs = reinterpret_cast<T*>(sv_smem);
+    __shared__ T tv[64], yv[64], red[256];
     const int64_t p = blockIdx.y;
+    if (A.skip && A.skip[p]) return;
     x += p * A.xstride;
     tbuf += p * A.tstride;
     const int s = lvl[blockIdx.x];
     const int f = S.first[s];
     const int w = S.first[s + 1] - f;
     const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
+    const T* Fs = L + p * A.lstride + S.loff[s];
+    const int nb0 = min(64, w);
+    stage_x(Fs, m, 0, nb0, Xs);                  // independent of t: its loads overlap the gather
     T* t = tbuf + S.row_ptr[s];
     for (int64_t r = threadIdx.x; r < m; r += blockDim.x) t[r] = r < w ? x[f + r] : zero_of<T>();
     __syncthreads();
@@ -294,132 +438,221 @@ __global__ void __launch_bounds__(256) k_fwd_gather(const int32_t* __restrict__ 
         for (int64_t a = threadIdx.x; a < mc - wc; a += blockDim.x) t[rl[a]] += tc[a];
         __syncthreads();
     }
+    if (threadIdx.x < nb0) tv[threadIdx.x] = t[threadIdx.x];
+    __syncthreads();
+    apply_x(Xs, tv, nb0, red, yv);
+    if (threadIdx.x < nb0) {
+        const T y = yv[threadIdx.x];
+        t[threadIdx.x] = y;
+        x[f + threadIdx.x] = dev_div(y, re(Fs[(int64_t)threadIdx.x * m + threadIdx.x]));
+    }
 }
 
-// item = (s, row0): rows [row0, row0 + SV_RC) below the diagonal block of column block b
+// item = (s, r0): triangle rows [r0, min(r0 + 64, w)) below full block b (r0 >= b*64 + 64)
 template <typename T>
-__global__ void __launch_bounds__(256) k_fwd_block(const int32_t* __restrict__ items, int b, SnDev S, SolveArgs A,
-                                                   const T* __restrict__ L, T* __restrict__ x, T* __restrict__ tbuf) {
-    __shared__ T y[SV_B];
+__global__ void __launch_bounds__(256) k_fwd_tri(const int32_t* __restrict__ items, int b, SnDev S, SolveArgs A,
+                                                 const T* __restrict__ L, T* __restrict__ x, T* __restrict__ tbuf) {
     extern __shared__ unsigned char sv_smem[];
-    T (*Lb)[SV_B + 1] = reinterpret_cast<T (*)[SV_B + 1]>(sv_smem);
+    T* Xs = reinterpret_cast<T*>(sv_smem);
+    __shared__ T ys[64], tn[64], yn[64], red[256];
     const int64_t p = blockIdx.y;
+    if (A.skip && A.skip[p]) return;
     x += p * A.xstride;
     tbuf += p * A.tstride;
     const int s = items[2 * blockIdx.x];
-    const int64_t row0 = items[2 * blockIdx.x + 1];
+    const int r0 = items[2 * blockIdx.x + 1];
     const int f = S.first[s];
     const int w = S.first[s + 1] - f;
     const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
-    const int b0 = b * SV_B;
-    const int nbb = min(SV_B, w - b0);
+    const int b0 = b * 64;
     const T* Fs = L + p * A.lstride + S.loff[s];
     T* t = tbuf + S.row_ptr[s];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int q = threadIdx.x; q < SV_B * SV_B; q += blockDim.x) {
-        const int i = q % SV_B, j = q / SV_B;
-        if (i < nbb && j < i) Lb[i][j] = Fs[(int64_t)(b0 + j) * m + b0 + i];
-    }
-    if (threadIdx.x < nbb) y[threadIdx.x] = t[b0 + threadIdx.x];
+    const int rend = min(r0 + 64, w);
+    const bool la = r0 == b0 + 64;               // this CTA holds block b+1: look-ahead
+    if (la) stage_x(Fs, m, r0, rend - r0, Xs);
+    if (threadIdx.x < 64) ys[threadIdx.x] = t[b0 + threadIdx.x];
     __syncthreads();
-    if (warp == 0) {
-        T v0 = lane < nbb ? y[lane] : zero_of<T>();
-        T v1 = lane + 32 < nbb ? y[lane + 32] : zero_of<T>();
-        for (int j = 0; j < nbb; j++) {
-            const T yj = j < 32 ? shfl_t(v0, j) : shfl_t(v1, j - 32);
-            if (lane > j && lane < nbb) v0 -= Lb[lane][j] * yj;
-            if (lane + 32 > j && lane + 32 < nbb) v1 -= Lb[lane + 32][j] * yj;
+    const int rl = threadIdx.x & 63, pi = threadIdx.x >> 6;
+    const int r = r0 + rl;
+    T a = zero_of<T>();
+    if (r < rend) {
+        const T* col = Fs + (int64_t)b0 * m + r;
+#pragma unroll
+        for (int u = 0; u < 16; u++) a += col[(int64_t)(pi + 4 * u) * m] * ys[pi + 4 * u];
+    }
+    red[threadIdx.x] = a;
+    __syncthreads();
+    if (threadIdx.x < 64 && r < rend) {
+        const T v = t[r] - ((red[rl] + red[rl + 64]) + (red[rl + 128] + red[rl + 192]));
+        t[r] = v;
+        tn[rl] = v;
+    }
+    if (la) {
+        __syncthreads();
+        apply_x(Xs, tn, rend - r0, red, yn);
+        if (threadIdx.x < rend - r0) {
+            const T y = yn[threadIdx.x];
+            t[r0 + threadIdx.x] = y;
+            x[f + r0 + threadIdx.x] = dev_div(y, re(Fs[(int64_t)(r0 + threadIdx.x) * m + r0 + threadIdx.x]));
         }
-        if (lane < nbb) y[lane] = v0;
-        if (lane + 32 < nbb) y[lane + 32] = v1;
-    }
-    __syncthreads();
-    if (row0 == b0 + nbb)   // the first chunk of this front stores the scaled block solution
-        for (int j = threadIdx.x; j < nbb; j += blockDim.x)
-            x[f + b0 + j] = dev_div(y[j], re(Fs[(int64_t)(b0 + j) * m + b0 + j]));
-    const int64_t r = row0 + threadIdx.x;
-    if (r < m && r < row0 + SV_RC) {
-        T a = t[r];
-        for (int j = 0; j < nbb; j++) a -= Fs[(int64_t)(b0 + j) * m + r] * y[j];
-        t[r] = a;
     }
 }
 
-// item = (s, col0): z_j = x[f + j] - sum_{r >= w} conj(L(r, j)) x[rows[r]], j in [col0, col0+32)
+// item = (s, r0): rows [r0, min(r0 + SV_RR, m)) below the triangle (r0 >= w): t -= L21 y
 template <typename T>
-__global__ void __launch_bounds__(256) k_bwd_offdiag(const int32_t* __restrict__ items, SnDev S, SolveArgs A,
-                                                     const T* __restrict__ L, const T* __restrict__ x,
-                                                     T* __restrict__ tbuf) {
+__global__ void __launch_bounds__(256) k_fwd_rect(const int32_t* __restrict__ items, SnDev S, SolveArgs A,
+                                                  const T* __restrict__ L, T* __restrict__ tbuf) {
+    constexpr int G = 256 / SV_RR;               // column groups
+    __shared__ T part[256];
     const int64_t p = blockIdx.y;
+    if (A.skip && A.skip[p]) return;
+    tbuf += p * A.tstride;
+    const int s = items[2 * blockIdx.x];
+    const int r0 = items[2 * blockIdx.x + 1];
+    const int w = S.first[s + 1] - S.first[s];
+    const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
+    const T* Fs = L + p * A.lstride + S.loff[s];
+    T* t = tbuf + S.row_ptr[s];
+    const int rl = threadIdx.x % SV_RR, pi = threadIdx.x / SV_RR;
+    const int64_t r = r0 + rl;
+    T a = zero_of<T>();
+    if (r < m) {
+        const T* col = Fs + r;
+        int j = pi;
+        for (; j + 7 * G < w; j += 8 * G) {      // eight independent loads in flight per thread
+            T lv[8], yv[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) { lv[u] = col[(int64_t)(j + u * G) * m]; yv[u] = t[j + u * G]; }
+#pragma unroll
+            for (int u = 0; u < 8; u++) a += lv[u] * yv[u];
+        }
+        for (; j < w; j += G) a += col[(int64_t)j * m] * t[j];
+    }
+    part[threadIdx.x] = a;
+    __syncthreads();
+    if (threadIdx.x < SV_RR && r < m) {
+        T sum = part[threadIdx.x];
+#pragma unroll
+        for (int q = 1; q < G; q++) sum += part[threadIdx.x + q * SV_RR];
+        t[r] -= sum;
+    }
+}
+
+// item = (s, c0): columns [c0, min(c0 + 64, w)); z_j = x_j - sum_{r >= w} conj(L(r, j)) x(rows[r]);
+// each warp carries eight columns through the row loop; the CTA holding the front's last
+// block then applies X^H
+template <typename T>
+__global__ void __launch_bounds__(256) k_bwd_rect(const int32_t* __restrict__ items, SnDev S, SolveArgs A,
+                                                  const T* __restrict__ L, T* __restrict__ x, T* __restrict__ tbuf) {
+    extern __shared__ unsigned char sv_smem[];
+    T* Xs = reinterpret_cast<T*>(sv_smem);
+    __shared__ T xs[SV_CH];
+    __shared__ T zs[64], xo[64], red[256];
+    const int64_t p = blockIdx.y;
+    if (A.skip && A.skip[p]) return;
     x += p * A.xstride;
     tbuf += p * A.tstride;
     const int s = items[2 * blockIdx.x];
-    const int col0 = items[2 * blockIdx.x + 1];
+    const int c0 = items[2 * blockIdx.x + 1];
     const int f = S.first[s];
     const int w = S.first[s + 1] - f;
     const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
     const T* Fs = L + p * A.lstride + S.loff[s];
     const int32_t* rows = S.rows + S.row_ptr[s];
     T* t = tbuf + S.row_ptr[s];
+    const int nc = min(64, w - c0);
+    const bool last = c0 + nc == w;
+    if (last) stage_x(Fs, m, c0, nc, Xs);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int jj = warp; jj < SV_CC; jj += 8) {
-        const int j = col0 + jj;
-        if (j >= w) break;
-        T a = zero_of<T>();
-        for (int64_t r = w + lane; r < m; r += 32) a += conj(Fs[(int64_t)j * m + r]) * x[rows[r]];
-        a = warp_sum(a);
-        if (lane == 0) t[j] = x[f + j] - a;
+    const int j0 = warp * 8;                     // this warp's columns: c0 + j0 .. c0 + j0 + 7
+    T acc[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) acc[c] = zero_of<T>();
+    for (int64_t q0 = w; q0 < m; q0 += SV_CH) {
+        const int len = (int)(m - q0 < SV_CH ? m - q0 : SV_CH);
+        __syncthreads();
+        for (int q = threadIdx.x; q < len; q += blockDim.x) xs[q] = x[rows[q0 + q]];
+        __syncthreads();
+        if (j0 < nc) {
+            const T* col = Fs + (int64_t)(c0 + j0) * m + q0;
+            for (int q = lane; q < len; q += 32) {
+                const T xv = xs[q];
+#pragma unroll
+                for (int c = 0; c < 8; c++)
+                    if (j0 + c < nc) acc[c] += conj(col[(int64_t)c * m + q]) * xv;
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; c++) acc[c] = warp_sum(acc[c]);
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < 8; c++)
+            if (j0 + c < nc) {
+                const T z = x[f + c0 + j0 + c] - acc[c];
+                t[c0 + j0 + c] = z;
+                zs[j0 + c] = z;
+            }
+    if (last) {
+        __syncthreads();
+        apply_xh(Xs, zs, nc, red, xo);
+        if (threadIdx.x < nc) x[f + c0 + threadIdx.x] = xo[threadIdx.x];
     }
 }
 
-// item = (s, col0): solve L_bb^H x_b = z_b, then z_j -= sum_{r in b} conj(L(r, j)) x_r for
-// the CTA's columns j in [col0, col0+32), j < b0
+// item = (s, c0): columns [c0, c0 + 64) left of block b (c0 + 64 <= b*64):
+// z_j -= sum_{r in block b} conj(L(r, j)) x_r; the CTA holding block b-1 then applies X^H
 template <typename T>
-__global__ void __launch_bounds__(256) k_bwd_block(const int32_t* __restrict__ items, int b, SnDev S, SolveArgs A,
-                                                   const T* __restrict__ L, T* __restrict__ x, T* __restrict__ tbuf) {
-    __shared__ T xb[SV_B];
+__global__ void __launch_bounds__(256) k_bwd_tri(const int32_t* __restrict__ items, int b, SnDev S, SolveArgs A,
+                                                 const T* __restrict__ L, T* __restrict__ x, T* __restrict__ tbuf) {
     extern __shared__ unsigned char sv_smem[];
-    T (*Lb)[SV_B + 1] = reinterpret_cast<T (*)[SV_B + 1]>(sv_smem);
+    T* Xs = reinterpret_cast<T*>(sv_smem);
+    __shared__ T xb[64], zs[64], xo[64], red[256];
     const int64_t p = blockIdx.y;
+    if (A.skip && A.skip[p]) return;
     x += p * A.xstride;
     tbuf += p * A.tstride;
     const int s = items[2 * blockIdx.x];
-    const int col0 = items[2 * blockIdx.x + 1];
+    const int c0 = items[2 * blockIdx.x + 1];
     const int f = S.first[s];
     const int w = S.first[s + 1] - f;
     const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
-    const int b0 = b * SV_B;
-    const int nbb = min(SV_B, w - b0);
+    const int b0 = b * 64;
+    const int nbb = min(64, w - b0);
     const T* Fs = L + p * A.lstride + S.loff[s];
     T* t = tbuf + S.row_ptr[s];
+    const bool la = c0 + 64 == b0;
+    if (la) stage_x(Fs, m, c0, 64, Xs);
+    if (threadIdx.x < nbb) xb[threadIdx.x] = x[f + b0 + threadIdx.x];
+    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int q = threadIdx.x; q < SV_B * SV_B; q += blockDim.x) {
-        const int i = q % SV_B, j = q / SV_B;
-        if (i < nbb && j < i) Lb[i][j] = Fs[(int64_t)(b0 + j) * m + b0 + i];
-    }
-    if (threadIdx.x < nbb) xb[threadIdx.x] = t[b0 + threadIdx.x];
-    __syncthreads();
-    if (warp == 0) {
-        T v0 = lane < nbb ? xb[lane] : zero_of<T>();
-        T v1 = lane + 32 < nbb ? xb[lane + 32] : zero_of<T>();
-        for (int j = nbb - 1; j >= 0; j--) {
-            const T yj = j < 32 ? shfl_t(v0, j) : shfl_t(v1, j - 32);
-            if (lane < j) v0 -= conj(Lb[j][lane]) * yj;
-            if (lane + 32 < j) v1 -= conj(Lb[j][lane + 32]) * yj;
+    const int j0 = warp * 8;
+    T acc[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) acc[c] = zero_of<T>();
+    const T* col = Fs + (int64_t)(c0 + j0) * m + b0;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int r = lane + 32 * h;
+        if (r < nbb) {
+            const T xv = xb[r];
+#pragma unroll
+            for (int c = 0; c < 8; c++) acc[c] += conj(col[(int64_t)c * m + r]) * xv;
         }
-        if (lane < nbb) xb[lane] = v0;
-        if (lane + 32 < nbb) xb[lane + 32] = v1;
     }
-    __syncthreads();
-    if (col0 == 0)
-        for (int j = threadIdx.x; j < nbb; j += blockDim.x) x[f + b0 + j] = xb[j];
-    for (int jj = warp; jj < SV_CC; jj += 8) {
-        const int j = col0 + jj;
-        if (j >= b0) break;
-        T a = zero_of<T>();
-        for (int r = lane; r < nbb; r += 32) a += conj(Fs[(int64_t)j * m + b0 + r]) * xb[r];
-        a = warp_sum(a);
-        if (lane == 0) t[j] -= a;
+#pragma unroll
+    for (int c = 0; c < 8; c++) acc[c] = warp_sum(acc[c]);
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const T z = t[c0 + j0 + c] - acc[c];
+            t[c0 + j0 + c] = z;
+            zs[j0 + c] = z;
+        }
+    if (la) {
+        __syncthreads();
+        apply_xh(Xs, zs, 64, red, xo);
+        if (threadIdx.x < 64) x[f + c0 + threadIdx.x] = xo[threadIdx.x];
     }
 }
 
@@ -599,59 +832,96 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
                 if (w <= kb * MF_NB) continue;
                 const int64_t m = S.sn_row_ptr[s + 1] - S.sn_row_ptr[s];
                 const int64_t t0 = kb * MF_NB + std::min(MF_NB, w - kb * MF_NB);
-                const int64_t T = (m - t0 + MF_TILE - 1) / MF_TILE;
-                for (int64_t a = 0; a < T; a++)
-                    for (int64_t b = 0; b <= a; b++) {
-                        it.push_back(s); it.push_back((int32_t)a); it.push_back((int32_t)b);
+                const int64_t s1 = std::min<int64_t>((kb * MF_NB / MF_SB + 1) * MF_SB, w);
+                for (int64_t j0 = t0; j0 < s1; j0 += MF_TILE)
+                    for (int64_t i0 = j0; i0 < m; i0 += MF_TILE) {
+                        it.push_back(s); it.push_back((int32_t)i0); it.push_back((int32_t)j0);
                         st.upd_cnt++;
+                    }
+            }
+            st.trail_off = (int64_t)it.size();
+            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                const int s = S.level_sn[q];
+                const int w = S.sn_first[s + 1] - S.sn_first[s];
+                if (w <= kb * MF_NB) continue;
+                const int64_t m = S.sn_row_ptr[s + 1] - S.sn_row_ptr[s];
+                const int64_t kend = std::min<int64_t>((int64_t)(kb + 1) * MF_NB, w);
+                const bool sb_end = kend == w || kend % MF_SB == 0;   // this pivot block closes a super-block
+                if (!sb_end) continue;
+                for (int64_t j0 = kend; j0 < m; j0 += MF_TILE)
+                    for (int64_t i0 = j0; i0 < m; i0 += MF_TILE) {
+                        it.push_back(s); it.push_back((int32_t)i0); it.push_back((int32_t)j0);
+                        st.trail_cnt++;
                     }
             }
             steps.push_back(st);
         }
     }
     put(items, it);
-    // triangular-solve schedule
+    // triangular-solve schedules (diagonal-block widths 64 and 128)
     std::vector<int32_t> si;
-    solve_levels.assign(nlev, SolveLevel{});
-    for (int l = 0; l < nlev; l++) {
-        SolveLevel& L = solve_levels[l];
-        int maxw = 0;
-        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-            const int s = S.level_sn[q];
-            maxw = std::max(maxw, S.sn_first[s + 1] - S.sn_first[s]);
-        }
-        const int nbk = (maxw + SV_B - 1) / SV_B;
-        for (int b = 0; b < nbk; b++) {
-            L.fwd_off.push_back((int64_t)si.size());
-            int cnt = 0;
+    for (int pl = 0; pl < 2; pl++) {
+        SolvePlan& P = plans[pl];
+        const int nb = pl == 0 ? 64 : 128;
+        P.nb = nb;
+        P.levels.assign(nlev, SolveLevel{});
+        for (int l = 0; l < nlev; l++) {
+            SolveLevel& L = P.levels[l];
+            int maxw = 0;
+            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                const int s = S.level_sn[q];
+                maxw = std::max(maxw, S.sn_first[s + 1] - S.sn_first[s]);
+            }
+            const int nbk = (maxw + nb - 1) / nb;
+            L.ftri_off.assign(std::max(nbk, 1), 0);
+            L.ftri_cnt.assign(std::max(nbk, 1), 0);
+            L.btri_off.assign(std::max(nbk, 1), 0);
+            L.btri_cnt.assign(std::max(nbk, 1), 0);
+            for (int b = 0; b + 1 < nbk; b++) {          // forward triangle launches
+                L.ftri_off[b] = (int64_t)si.size();
+                for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                    const int s = S.level_sn[q];
+                    const int w = S.sn_first[s + 1] - S.sn_first[s];
+                    for (int r0 = (b + 1) * nb; r0 < w; r0 += nb) { si.push_back(s); si.push_back(r0); L.ftri_cnt[b]++; }
+                }
+            }
+            L.frect_off = (int64_t)si.size();
             for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
                 const int s = S.level_sn[q];
                 const int w = S.sn_first[s + 1] - S.sn_first[s];
-                if (w <= b * SV_B) continue;
                 const int64_t m = S.sn_row_ptr[s + 1] - S.sn_row_ptr[s];
-                const int64_t r0 = b * SV_B + std::min(SV_B, w - b * SV_B);
-                if (r0 >= m) { si.push_back(s); si.push_back((int32_t)r0); cnt++; continue; }
-                for (int64_t r = r0; r < m; r += SV_RC) { si.push_back(s); si.push_back((int32_t)r); cnt++; }
+                for (int64_t r0 = w; r0 < m; r0 += SV_RR) { si.push_back(s); si.push_back((int32_t)r0); L.frect_cnt++; }
             }
-            L.fwd_cnt.push_back(cnt);
-        }
-        L.off_items = (int64_t)si.size();
-        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-            const int s = S.level_sn[q];
-            const int w = S.sn_first[s + 1] - S.sn_first[s];
-            for (int c0 = 0; c0 < w; c0 += SV_CC) { si.push_back(s); si.push_back(c0); L.off_cnt++; }
-        }
-        for (int b = 0; b < nbk; b++) {
-            L.bwd_off.push_back((int64_t)si.size());
-            int cnt = 0;
+            L.brect_off = (int64_t)si.size();
             for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
                 const int s = S.level_sn[q];
                 const int w = S.sn_first[s + 1] - S.sn_first[s];
-                if (w <= b * SV_B) continue;
-                si.push_back(s); si.push_back(0); cnt++;
-                for (int c0 = SV_CC; c0 < b * SV_B; c0 += SV_CC) { si.push_back(s); si.push_back(c0); cnt++; }
+                for (int c0 = 0; c0 < w; c0 += nb) { si.push_back(s); si.push_back(c0); L.brect_cnt++; }
             }
-            L.bwd_cnt.push_back(cnt);
+            for (int b = 1; b < nbk; b++) {              // backward triangle launches
+                L.btri_off[b] = (int64_t)si.size();
+                for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                    const int s = S.level_sn[q];
+                    const int w = S.sn_first[s + 1] - S.sn_first[s];
+                    if (w <= b * nb) continue;
+                    for (int c0 = 0; c0 < b * nb; c0 += nb) { si.push_back(s); si.push_back(c0); L.btri_cnt[b]++; }
+                }
+            }
+        }
+        // diagonal blocks to invert after the factorisation
+        P.inv_small_off = (int64_t)si.size();
+        for (int s = 0; s < ns; s++) {
+            const int w = S.sn_first[s + 1] - S.sn_first[s];
+            for (int b = 0; b * nb < w; b++)
+                if (std::min(nb, w - b * nb) <= 32 && std::min(nb, w - b * nb) > 1) {
+                    si.push_back(s); si.push_back(b); P.inv_small_cnt++;
+                }
+        }
+        P.inv_large_off = (int64_t)si.size();
+        for (int s = 0; s < ns; s++) {
+            const int w = S.sn_first[s + 1] - S.sn_first[s];
+            for (int b = 0; b * nb < w; b++)
+                if (std::min(nb, w - b * nb) > 32) { si.push_back(s); si.push_back(b); P.inv_large_cnt++; }
         }
     }
     put(sitems, si);
@@ -675,6 +945,9 @@ void mf_scatter(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, const
                bt.L, bt.lstride);
     TMG_CHECK_LAUNCH();
 }
+
+template <typename T>
+void mf_invert_diag(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt);
 
 template <typename T>
 void mf_factor(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, int* status) {
@@ -708,43 +981,76 @@ void mf_factor(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, int* s
             TMG_LAUNCH(k_panel<T>, dim3(stp.panel_cnt, B), 64, 0, st, S.items + stp.panel_off, stp.kb, sn, bt.L,
                        bt.lstride);
         if (stp.upd_cnt)
-            TMG_LAUNCH(k_update<T>, dim3(stp.upd_cnt, B), 256, upd_smem, st, S.items + stp.upd_off, stp.kb, sn, bt.L, bt.U,
-                       bt.lstride, bt.ustride);
+            TMG_LAUNCH(k_update<T>, dim3(stp.upd_cnt, B), 256, upd_smem, st, S.items + stp.upd_off, stp.kb * MF_NB, MF_NB,
+                       0, sn, bt.L, bt.U, bt.lstride, bt.ustride);
+        if (stp.trail_cnt)
+            TMG_LAUNCH(k_update<T>, dim3(stp.trail_cnt, B), 256, upd_smem, st, S.items + stp.trail_off,
+                       (stp.kb * MF_NB / MF_SB) * MF_SB, MF_SB, 1, sn, bt.L, bt.U, bt.lstride, bt.ustride);
+    }
+    TMG_CHECK_LAUNCH();
+    mf_invert_diag<T>(st, S, bt);
+}
+
+template <typename T>
+void mf_invert_diag(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt) {
+    constexpr int NB = sv_nb<T>();
+    const auto& P = S.plan(NB);
+    const SnDev sn = S.sn();
+    const unsigned B = bt.B;
+    if (P.inv_small_cnt)
+        TMG_LAUNCH((k_inv_small<T, NB>), dim3((unsigned)ceil_div(P.inv_small_cnt, inv_wpc<T>()), B),
+                   32 * inv_wpc<T>(), 0, st,
+                   S.sitems + P.inv_small_off, P.inv_small_cnt, sn, bt.L, bt.lstride);
+    if (P.inv_large_cnt) {
+        const size_t smem = (size_t)NB * (NB + 1) * sizeof(T);
+        static bool attr_set = false;
+        if (!attr_set) {
+            TMG_CUDA(cudaFuncSetAttribute(k_inv_large<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            attr_set = true;
+        }
+        TMG_LAUNCH((k_inv_large<T, NB>), dim3(P.inv_large_cnt, B), 256, smem, st, S.sitems + P.inv_large_off, sn, bt.L,
+                   bt.lstride);
     }
     TMG_CHECK_LAUNCH();
 }
 
 template <typename T>
-void mf_solve(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, T* x, T* tbuf) {
+void mf_solve(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, T* x, T* tbuf, const int* skip) {
+    static_assert(sv_nb<T>() == 64, "the solve kernels work on 64-wide diagonal blocks");
+    const auto& P = S.plan(64);
     const int nlev = (int)S.level_ptr.size() - 1;
+    const SnDev sn = S.sn();
+    const SolveArgs A{bt.lstride, (int64_t)S.n, S.t_entries, skip};
+    const unsigned B = bt.B;
+    const size_t xs = (size_t)64 * XS_LD * sizeof(T);
     static bool attr_set = false;
-    const size_t sv_smem = (size_t)SV_B * (SV_B + 1) * sizeof(T);
     if (!attr_set) {
-        TMG_CUDA(cudaFuncSetAttribute(k_fwd_block<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sv_smem));
-        TMG_CUDA(cudaFuncSetAttribute(k_bwd_block<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sv_smem));
+        TMG_CUDA(cudaFuncSetAttribute(k_fwd_gather<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
+        TMG_CUDA(cudaFuncSetAttribute(k_fwd_tri<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
+        TMG_CUDA(cudaFuncSetAttribute(k_bwd_rect<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
+        TMG_CUDA(cudaFuncSetAttribute(k_bwd_tri<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
         attr_set = true;
     }
-    const SnDev sn = S.sn();
-    const SolveArgs A{bt.lstride, (int64_t)S.n, S.t_entries};
-    const unsigned B = bt.B;
     for (int l = 0; l < nlev; l++) {
         const int cnt = S.level_ptr[l + 1] - S.level_ptr[l];
         if (!cnt) continue;
-        TMG_LAUNCH(k_fwd_gather<T>, dim3(cnt, B), 256, 0, st, S.level_sn + S.level_ptr[l], sn, A, x, tbuf);
-        const auto& L = S.solve_levels[l];
-        for (size_t b = 0; b < L.fwd_off.size(); b++)
-            if (L.fwd_cnt[b])
-                TMG_LAUNCH(k_fwd_block<T>, dim3(L.fwd_cnt[b], B), 256, sv_smem, st, S.sitems + L.fwd_off[b], (int)b, sn, A,
+        const auto& L = P.levels[l];
+        TMG_LAUNCH(k_fwd_gather<T>, dim3(cnt, B), 256, xs, st, S.level_sn + S.level_ptr[l], sn, A, bt.L, x, tbuf);
+        for (size_t b = 0; b < L.ftri_cnt.size(); b++)
+            if (L.ftri_cnt[b])
+                TMG_LAUNCH(k_fwd_tri<T>, dim3(L.ftri_cnt[b], B), 256, xs, st, S.sitems + L.ftri_off[b], (int)b, sn, A,
                            bt.L, x, tbuf);
+        if (L.frect_cnt)
+            TMG_LAUNCH(k_fwd_rect<T>, dim3(L.frect_cnt, B), 256, 0, st, S.sitems + L.frect_off, sn, A, bt.L, tbuf);
     }
     for (int l = nlev - 1; l >= 0; l--) {
-        const auto& L = S.solve_levels[l];
-        if (L.off_cnt)
-            TMG_LAUNCH(k_bwd_offdiag<T>, dim3(L.off_cnt, B), 256, 0, st, S.sitems + L.off_items, sn, A, bt.L, x, tbuf);
-        for (int b = (int)L.bwd_off.size() - 1; b >= 0; b--)
-            if (L.bwd_cnt[b])
-                TMG_LAUNCH(k_bwd_block<T>, dim3(L.bwd_cnt[b], B), 256, sv_smem, st, S.sitems + L.bwd_off[b], b, sn, A,
-                           bt.L, x, tbuf);
+        const auto& L = P.levels[l];
+        if (L.brect_cnt)
+            TMG_LAUNCH(k_bwd_rect<T>, dim3(L.brect_cnt, B), 256, xs, st, S.sitems + L.brect_off, sn, A, bt.L, x, tbuf);
+        for (int b = (int)L.btri_cnt.size() - 1; b >= 1; b--)
+            if (L.btri_cnt[b])
+                TMG_LAUNCH(k_bwd_tri<T>, dim3(L.btri_cnt[b], B), 256, xs, st, S.sitems + L.btri_off[b], b, sn, A, bt.L,
+                           x, tbuf);
     }
     TMG_CHECK_LAUNCH();
 }
@@ -772,7 +1078,7 @@ void mf_count_nonpos(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, 
 #define TMG_INST(T)                                                                          \
     template void mf_factor<T>(cudaStream_t, const DevSymbolic&, const Batch<T>&, int*);     \
     template void mf_scatter<T>(cudaStream_t, const DevSymbolic&, const Batch<T>&, const T*); \
-    template void mf_solve<T>(cudaStream_t, const DevSymbolic&, const Batch<T>&, T*, T*);    \
+    template void mf_solve<T>(cudaStream_t, const DevSymbolic&, const Batch<T>&, T*, T*, const int*); \
     template void mf_count_nonpos<T>(cudaStream_t, const DevSymbolic&, const Batch<T>&, int*);
 TMG_INST(double)
 TMG_INST(float)

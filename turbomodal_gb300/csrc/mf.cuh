@@ -17,9 +17,14 @@ namespace tmg {
 
 constexpr int MF_NB = 32;      // pivot block width
 constexpr int MF_TILE = 64;    // Schur-update tile
-constexpr int SV_B = 64;       // triangular-solve column block
-constexpr int SV_RC = 256;     // rows per CTA in the forward sweep
-constexpr int SV_CC = 32;      // columns per CTA (four per warp) in the backward sweeps
+constexpr int MF_SB = 256;     // super-block: pivot blocks update inside it, one trailing update after it
+constexpr int SV_RR = 64;      // rows per CTA of the forward rectangle products
+constexpr int SV_CH = 2048;    // gathered solution entries staged per pass (backward rectangles)
+
+// Width of the diagonal blocks that the triangular solves treat as dense units (the factor
+// stores each block's explicit unit-lower inverse).
+template <typename T>
+constexpr int sv_nb() { return 64; }
 
 // Per-supernode geometry shared by the kernels.
 struct SnDev {
@@ -59,17 +64,30 @@ struct DevSymbolic {
         int64_t uzero_max = 0;
         std::vector<int64_t> ext_off;          // extend-add lists (parent, child), one per child rank
         std::vector<int32_t> ext_cnt, ext_max;
-        int64_t diag_off = 0, panel_off = 0, upd_off = 0;
-        int32_t diag_cnt = 0, panel_cnt = 0, upd_cnt = 0;
+        int64_t diag_off = 0, panel_off = 0, upd_off = 0, trail_off = 0;
+        int32_t diag_cnt = 0, panel_cnt = 0, upd_cnt = 0, trail_cnt = 0;
     };
     std::vector<Step> steps;
+    // Triangular-solve schedule for one diagonal-block width nb, per tree level:
+    //   forward:  gather (level supernodes), triangle launches b = 0 .. (items (s, r0): rows
+    //             [r0, r0 + nb) of the triangle below block b), one rectangle launch
+    //             (items (s, r0): rows [r0, r0 + SV_RR) below the triangle);
+    //   backward: one rectangle launch (items (s, c0): columns [c0, c0 + nb)), triangle
+    //             launches b = last .. 1 (items (s, c0): columns [c0, c0 + nb) left of block b).
     struct SolveLevel {
-        int64_t off_items = 0;
-        int32_t off_cnt = 0;
-        std::vector<int64_t> fwd_off, bwd_off;
-        std::vector<int32_t> fwd_cnt, bwd_cnt;
+        std::vector<int64_t> ftri_off, btri_off;   // index b
+        std::vector<int32_t> ftri_cnt, btri_cnt;
+        int64_t frect_off = 0, brect_off = 0;
+        int32_t frect_cnt = 0, brect_cnt = 0;
     };
-    std::vector<SolveLevel> solve_levels;
+    struct SolvePlan {
+        int nb = 0;
+        std::vector<SolveLevel> levels;
+        int64_t inv_small_off = 0, inv_large_off = 0;   // items (s, b): diagonal blocks to invert
+        int32_t inv_small_cnt = 0, inv_large_cnt = 0;   // small: width <= 32
+    };
+    SolvePlan plans[2];        // nb = 64, nb = 128
+    const SolvePlan& plan(int nb) const { return plans[nb == 64 ? 0 : 1]; }
     std::vector<int32_t> level_ptr;
     SnDev sn() const {
         return SnDev{sn_first, sn_row_ptr, sn_rows, loff, uoff, child_ptr, child_list, rel_ptr, rel};
@@ -96,12 +114,16 @@ template <typename T>
 void mf_scatter(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, const T* vals);
 
 // Numeric factorisation; status[p] receives 1 + the first zero-pivot column of problem p.
+// On return every diagonal block of width sv_nb<T>() of every panel holds, below its
+// diagonal, the strict lower part of the block's unit-lower inverse (the diagonal keeps D),
+// which is the form mf_solve reads.
 template <typename T>
 void mf_factor(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, int* status);
 
-// x (B x n, factor numbering, factor precision) <- L^-H D^-1 L^-1 x ; tbuf: B x t_entries
+// x (B x n, factor numbering, factor precision) <- L^-H D^-1 L^-1 x ; tbuf: B x t_entries.
+// skip (device, B flags, may be null): problems with a nonzero flag are left untouched.
 template <typename T>
-void mf_solve(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, T* x, T* tbuf);
+void mf_solve(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, T* x, T* tbuf, const int* skip = nullptr);
 
 // Permutation with precision conversion between user vectors (problem stride ld) and the
 // factor-numbering work vectors (problem stride n); optional per-problem diagonal scaling

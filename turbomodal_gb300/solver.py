@@ -128,7 +128,8 @@ class CyclicSymmetrySolver:
         ph = np.zeros(8)
         nl = C.c_int64()
         self.ctx.L.tmg_last_timing(self.ctx.h, _lib.ptr(ph, C.c_double), 8, C.byref(nl))
-        return dict(prepare_ms=ph[0], factor_ms=ph[1], lanczos_ms=ph[2], post_ms=ph[3], device_ms=ph[4],
+        return dict(prepare_ms=float(ph[0]), factor_ms=float(ph[1]), lanczos_ms=float(ph[2]), post_ms=float(ph[3]),
+                    device_ms=float(ph[4]), solves=int(ph[5]), applies=int(ph[6]), max_refine_iters=int(ph[7]),
                     kernel_launches=nl.value)
 
     def set_profiling(self, on: bool) -> None:
