@@ -33,6 +33,32 @@ extern int64_t g_kernel_launches;
     } while (0)
 #define TMG_CHECK_LAUNCH() TMG_CUDA(cudaGetLastError())
 
+// Programmatic dependent launch: the kernel may start while its predecessor in the stream is
+// still running.  Such kernels call pdl_trigger() on entry (letting their own successor
+// launch early), load only data no earlier kernel of the sequence writes, then call
+// pdl_wait(), which returns once the predecessor has completed and its writes are visible.
+// Every CTA of such a kernel executes pdl_wait(), so completion is transitive along the chain.
+#define TMG_LAUNCH_PDL(kern_, grid_, block_, smem_, strm_, ...)                              \
+    do {                                                                                      \
+        cudaLaunchConfig_t cfg_{};                                                            \
+        cfg_.gridDim = (grid_);                                                               \
+        cfg_.blockDim = (block_);                                                             \
+        cfg_.dynamicSmemBytes = (smem_);                                                      \
+        cfg_.stream = (strm_);                                                                \
+        cudaLaunchAttribute at_[1];                                                           \
+        at_[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;                      \
+        at_[0].val.programmaticStreamSerializationAllowed = 1;                               \
+        cfg_.attrs = at_;                                                                     \
+        cfg_.numAttrs = 1;                                                                    \
+        TMG_CUDA(cudaLaunchKernelEx(&cfg_, kern_, __VA_ARGS__));                              \
+        ::tmg::g_kernel_launches++;                                                           \
+    } while (0)
+
+#ifdef __CUDACC__
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+#endif
+
 // Minimal complex types (interleaved re/im), usable on host and device.
 template <typename R>
 struct cpx {

@@ -415,8 +415,9 @@ __global__ void __launch_bounds__(256) k_fwd_gather(const int32_t* __restrict__ 
     extern __shared__ unsigned char sv_smem[];
     T* Xs = reinterpret_cast<T*>(sv_smem);
     __shared__ T tv[64], yv[64], red[256];
+    pdl_trigger();
     const int64_t p = blockIdx.y;
-    if (A.skip && A.skip[p]) return;
+    const bool skp = A.skip && A.skip[p];
     x += p * A.xstride;
     tbuf += p * A.tstride;
     const int s = lvl[blockIdx.x];
@@ -425,7 +426,9 @@ __global__ void __launch_bounds__(256) k_fwd_gather(const int32_t* __restrict__ 
     const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
     const T* Fs = L + p * A.lstride + S.loff[s];
     const int nb0 = min(64, w);
-    stage_x(Fs, m, 0, nb0, Xs);                  // independent of t: its loads overlap the gather
+    if (!skp) stage_x(Fs, m, 0, nb0, Xs);        // factor data: staged before the predecessor ends
+    pdl_wait();
+    if (skp) return;
     T* t = tbuf + S.row_ptr[s];
     for (int64_t r = threadIdx.x; r < m; r += blockDim.x) t[r] = r < w ? x[f + r] : zero_of<T>();
     __syncthreads();
@@ -455,8 +458,9 @@ __global__ void __launch_bounds__(256) k_fwd_tri(const int32_t* __restrict__ ite
     extern __shared__ unsigned char sv_smem[];
     T* Xs = reinterpret_cast<T*>(sv_smem);
     __shared__ T ys[64], tn[64], yn[64], red[256];
+    pdl_trigger();
     const int64_t p = blockIdx.y;
-    if (A.skip && A.skip[p]) return;
+    const bool skp = A.skip && A.skip[p];
     x += p * A.xstride;
     tbuf += p * A.tstride;
     const int s = items[2 * blockIdx.x];
@@ -469,17 +473,26 @@ __global__ void __launch_bounds__(256) k_fwd_tri(const int32_t* __restrict__ ite
     T* t = tbuf + S.row_ptr[s];
     const int rend = min(r0 + 64, w);
     const bool la = r0 == b0 + 64;               // this CTA holds block b+1: look-ahead
-    if (la) stage_x(Fs, m, r0, rend - r0, Xs);
-    if (threadIdx.x < 64) ys[threadIdx.x] = t[b0 + threadIdx.x];
-    __syncthreads();
     const int rl = threadIdx.x & 63, pi = threadIdx.x >> 6;
     const int r = r0 + rl;
-    T a = zero_of<T>();
-    if (r < rend) {
-        const T* col = Fs + (int64_t)b0 * m + r;
+    T lv[16];                                    // factor entries of this thread's product
 #pragma unroll
-        for (int u = 0; u < 16; u++) a += col[(int64_t)(pi + 4 * u) * m] * ys[pi + 4 * u];
+    for (int u = 0; u < 16; u++) lv[u] = zero_of<T>();
+    if (!skp) {
+        if (la) stage_x(Fs, m, r0, rend - r0, Xs);
+        if (r < rend) {
+            const T* col = Fs + (int64_t)b0 * m + r;
+#pragma unroll
+            for (int u = 0; u < 16; u++) lv[u] = col[(int64_t)(pi + 4 * u) * m];
+        }
     }
+    pdl_wait();
+    if (skp) return;
+    if (threadIdx.x < 64) ys[threadIdx.x] = t[b0 + threadIdx.x];
+    __syncthreads();
+    T a = zero_of<T>();
+#pragma unroll
+    for (int u = 0; u < 16; u++) a += lv[u] * ys[pi + 4 * u];
     red[threadIdx.x] = a;
     __syncthreads();
     if (threadIdx.x < 64 && r < rend) {
@@ -504,8 +517,9 @@ __global__ void __launch_bounds__(256) k_fwd_rect(const int32_t* __restrict__ it
                                                   const T* __restrict__ L, T* __restrict__ tbuf) {
     constexpr int G = 256 / SV_RR;               // column groups
     __shared__ T part[256];
+    pdl_trigger();
     const int64_t p = blockIdx.y;
-    if (A.skip && A.skip[p]) return;
+    const bool skp = A.skip && A.skip[p];
     tbuf += p * A.tstride;
     const int s = items[2 * blockIdx.x];
     const int r0 = items[2 * blockIdx.x + 1];
@@ -513,6 +527,8 @@ __global__ void __launch_bounds__(256) k_fwd_rect(const int32_t* __restrict__ it
     const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
     const T* Fs = L + p * A.lstride + S.loff[s];
     T* t = tbuf + S.row_ptr[s];
+    pdl_wait();
+    if (skp) return;
     const int rl = threadIdx.x % SV_RR, pi = threadIdx.x / SV_RR;
     const int64_t r = r0 + rl;
     T a = zero_of<T>();
@@ -548,8 +564,9 @@ __global__ void __launch_bounds__(256) k_bwd_rect(const int32_t* __restrict__ it
     T* Xs = reinterpret_cast<T*>(sv_smem);
     __shared__ T xs[SV_CH];
     __shared__ T zs[64], xo[64], red[256];
+    pdl_trigger();
     const int64_t p = blockIdx.y;
-    if (A.skip && A.skip[p]) return;
+    const bool skp = A.skip && A.skip[p];
     x += p * A.xstride;
     tbuf += p * A.tstride;
     const int s = items[2 * blockIdx.x];
@@ -562,7 +579,9 @@ __global__ void __launch_bounds__(256) k_bwd_rect(const int32_t* __restrict__ it
     T* t = tbuf + S.row_ptr[s];
     const int nc = min(64, w - c0);
     const bool last = c0 + nc == w;
-    if (last) stage_x(Fs, m, c0, nc, Xs);
+    if (last && !skp) stage_x(Fs, m, c0, nc, Xs);
+    pdl_wait();
+    if (skp) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int j0 = warp * 8;                     // this warp's columns: c0 + j0 .. c0 + j0 + 7
     T acc[8];
@@ -575,11 +594,21 @@ __global__ void __launch_bounds__(256) k_bwd_rect(const int32_t* __restrict__ it
         __syncthreads();
         if (j0 < nc) {
             const T* col = Fs + (int64_t)(c0 + j0) * m + q0;
-            for (int q = lane; q < len; q += 32) {
-                const T xv = xs[q];
+            const int ncw = min(8, nc - j0);
+            for (int q = lane; q < len; q += 64) {     // two rows per lane and step: 16 loads in flight
+                const bool h1 = q + 32 < len;
+                T l0[8], l1[8];
 #pragma unroll
-                for (int c = 0; c < 8; c++)
-                    if (j0 + c < nc) acc[c] += conj(col[(int64_t)c * m + q]) * xv;
+                for (int c = 0; c < 8; c++) {
+                    l0[c] = c < ncw ? col[(int64_t)c * m + q] : zero_of<T>();
+                    l1[c] = c < ncw && h1 ? col[(int64_t)c * m + q + 32] : zero_of<T>();
+                }
+                const T x0 = xs[q], x1 = h1 ? xs[q + 32] : zero_of<T>();
+#pragma unroll
+                for (int c = 0; c < 8; c++) {
+                    acc[c] += conj(l0[c]) * x0;
+                    acc[c] += conj(l1[c]) * x1;
+                }
             }
         }
     }
@@ -608,8 +637,9 @@ __global__ void __launch_bounds__(256) k_bwd_tri(const int32_t* __restrict__ ite
     extern __shared__ unsigned char sv_smem[];
     T* Xs = reinterpret_cast<T*>(sv_smem);
     __shared__ T xb[64], zs[64], xo[64], red[256];
+    pdl_trigger();
     const int64_t p = blockIdx.y;
-    if (A.skip && A.skip[p]) return;
+    const bool skp = A.skip && A.skip[p];
     x += p * A.xstride;
     tbuf += p * A.tstride;
     const int s = items[2 * blockIdx.x];
@@ -622,22 +652,36 @@ __global__ void __launch_bounds__(256) k_bwd_tri(const int32_t* __restrict__ ite
     const T* Fs = L + p * A.lstride + S.loff[s];
     T* t = tbuf + S.row_ptr[s];
     const bool la = c0 + 64 == b0;
-    if (la) stage_x(Fs, m, c0, 64, Xs);
-    if (threadIdx.x < nbb) xb[threadIdx.x] = x[f + b0 + threadIdx.x];
-    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int j0 = warp * 8;
+    T lv[2][8];                                  // factor entries of this lane's products
+#pragma unroll
+    for (int h = 0; h < 2; h++)
+#pragma unroll
+        for (int c = 0; c < 8; c++) lv[h][c] = zero_of<T>();
+    if (!skp) {
+        if (la) stage_x(Fs, m, c0, 64, Xs);
+        const T* col = Fs + (int64_t)(c0 + j0) * m + b0;
+#pragma unroll
+        for (int h = 0; h < 2; h++)
+            if (lane + 32 * h < nbb)
+#pragma unroll
+                for (int c = 0; c < 8; c++) lv[h][c] = col[(int64_t)c * m + lane + 32 * h];
+    }
+    pdl_wait();
+    if (skp) return;
+    if (threadIdx.x < nbb) xb[threadIdx.x] = x[f + b0 + threadIdx.x];
+    __syncthreads();
     T acc[8];
 #pragma unroll
     for (int c = 0; c < 8; c++) acc[c] = zero_of<T>();
-    const T* col = Fs + (int64_t)(c0 + j0) * m + b0;
 #pragma unroll
     for (int h = 0; h < 2; h++) {
         const int r = lane + 32 * h;
         if (r < nbb) {
             const T xv = xb[r];
 #pragma unroll
-            for (int c = 0; c < 8; c++) acc[c] += conj(col[(int64_t)c * m + r]) * xv;
+            for (int c = 0; c < 8; c++) acc[c] += conj(lv[h][c]) * xv;
         }
     }
 #pragma unroll
@@ -1035,21 +1079,21 @@ void mf_solve(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, T* x, T
         const int cnt = S.level_ptr[l + 1] - S.level_ptr[l];
         if (!cnt) continue;
         const auto& L = P.levels[l];
-        TMG_LAUNCH(k_fwd_gather<T>, dim3(cnt, B), 256, xs, st, S.level_sn + S.level_ptr[l], sn, A, bt.L, x, tbuf);
+        TMG_LAUNCH_PDL(k_fwd_gather<T>, dim3(cnt, B), 256, xs, st, S.level_sn + S.level_ptr[l], sn, A, bt.L, x, tbuf);
         for (size_t b = 0; b < L.ftri_cnt.size(); b++)
             if (L.ftri_cnt[b])
-                TMG_LAUNCH(k_fwd_tri<T>, dim3(L.ftri_cnt[b], B), 256, xs, st, S.sitems + L.ftri_off[b], (int)b, sn, A,
+                TMG_LAUNCH_PDL(k_fwd_tri<T>, dim3(L.ftri_cnt[b], B), 256, xs, st, S.sitems + L.ftri_off[b], (int)b, sn, A,
                            bt.L, x, tbuf);
         if (L.frect_cnt)
-            TMG_LAUNCH(k_fwd_rect<T>, dim3(L.frect_cnt, B), 256, 0, st, S.sitems + L.frect_off, sn, A, bt.L, tbuf);
+            TMG_LAUNCH_PDL(k_fwd_rect<T>, dim3(L.frect_cnt, B), 256, 0, st, S.sitems + L.frect_off, sn, A, bt.L, tbuf);
     }
     for (int l = nlev - 1; l >= 0; l--) {
         const auto& L = P.levels[l];
         if (L.brect_cnt)
-            TMG_LAUNCH(k_bwd_rect<T>, dim3(L.brect_cnt, B), 256, xs, st, S.sitems + L.brect_off, sn, A, bt.L, x, tbuf);
+            TMG_LAUNCH_PDL(k_bwd_rect<T>, dim3(L.brect_cnt, B), 256, xs, st, S.sitems + L.brect_off, sn, A, bt.L, x, tbuf);
         for (int b = (int)L.btri_cnt.size() - 1; b >= 1; b--)
             if (L.btri_cnt[b])
-                TMG_LAUNCH(k_bwd_tri<T>, dim3(L.btri_cnt[b], B), 256, xs, st, S.sitems + L.btri_off[b], b, sn, A, bt.L,
+                TMG_LAUNCH_PDL(k_bwd_tri<T>, dim3(L.btri_cnt[b], B), 256, xs, st, S.sitems + L.btri_off[b], b, sn, A, bt.L,
                            x, tbuf);
     }
     TMG_CHECK_LAUNCH();
