@@ -50,6 +50,10 @@ def parse():
     ap.add_argument("--num-modes", type=int, default=10)
     ap.add_argument("--no-verify", action="store_true", help="skip the FP64 verification pass")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served request-stream sample")
+    ap.add_argument("--serve-requests", type=int, default=12)
+    ap.add_argument("--serve-max-nodes", type=int, default=30000,
+                    help="largest sector of the request-stream sample (the full stream goes to 200000)")
     return ap.parse_args()
 
 
@@ -241,6 +245,7 @@ def main():
     clocks.start()
     dev_ms, wall_s, results, launches, d2h = [], [], [], 0, 0
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("timed")
     for rpm in timed:
         t0 = time.perf_counter()
         res = solver.solve_at_rpm(rpm, args.num_modes, hi, precision="mixed")
@@ -251,6 +256,7 @@ def main():
         d2h += sum(r.frequencies.nbytes + r.mode_shapes.nbytes + r.whirl_direction.nbytes for r in res)
         results.append(res)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     clk = clocks.stop()
     barrier(pg)
     # verification against the plain FP64 GPU path (untimed) and its own throughput
@@ -269,10 +275,11 @@ def main():
             worst = max(worst, w)
     else:
         n_ok = n_all = sum(len(r.frequencies) for res in results for r in res)
-    # roofline of the dominant kernel: the shift-invert triangular-solve graph (HBM bound),
-    # timed live with CUDA events in one extra profiled step
+    # roofline of the dominant kernel: the shift-invert triangular-solve graph of the batch of
+    # complex harmonics (HBM bound), timed live with CUDA events in one extra profiled solve
+    mesh_k = [k for k in (hi or range(mesh.num_sectors // 2 + 1)) if 0 < k < mesh.num_sectors / 2]
     solver.set_profiling(True)
-    solver.solve_at_rpm(timed[0], args.num_modes, hi, precision="mixed")
+    solver.solve_at_rpm(timed[0], args.num_modes, mesh_k, precision="mixed")
     prof = solver.profile_solve()
     solver.set_profiling(False)
     peaks = {}
@@ -285,14 +292,28 @@ def main():
     per_launch_bytes = prof["bytes"] / max(prof["count"], 1)
     per_launch_s = prof["ms"] / max(prof["count"], 1) / 1e3
     achieved = per_launch_bytes / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
-    traffic = None
-    tr_path = os.path.join(ROOT, "profiles", "trisolve_traffic.json")
+    traffic = None   # DRAM bytes of one batched solve from an ncu capture of this workload
+    tr_path = os.path.join(ROOT, "profiles", "trisolve_cfg1_traffic.txt")
     if os.path.exists(tr_path):
         with open(tr_path) as fh:
-            traffic = json.load(fh).get("bytes_per_solve")
+            for line in fh:
+                if line.startswith("dram_bytes_per_solve"):
+                    traffic = float(line.split("=")[1])
     t_dev = max_over_ranks(pg, sum(dev_ms) / 1e3)
     t_wall = max_over_ranks(pg, sum(wall_s))
     tot_ok = sum_over_ranks(pg, n_ok)
+    serving = None
+    if rank == 0 and not args.no_serve:
+        # served request stream (Poisson arrivals, mixed sizes, admission by memory budget)
+        from turbomodal_gb300.serve import ModalServer, latency_summary, request_stream
+
+        reqs = request_stream(args.serve_requests, seed=2024, rate_hz=20.0, min_nodes=2000,
+                              max_nodes=args.serve_max_nodes)
+        done = ModalServer(device=local, budget_bytes=150 << 30, max_inflight=4).serve(reqs)
+        serving = latency_summary(done)
+        serving["sample"] = (f"{len(reqs)} requests, Poisson 20 req/s, config-0/1-style sectors of 2000-"
+                             f"{args.serve_max_nodes} nodes (log-uniform), 24/36/48 sectors, rpm U(0,15000), "
+                             "5-20 modes, 1-19 random harmonics, mixed precision, 150 GB budget, 4 in flight")
     if rank == 0:
         cpu = None
         if ws == 1 and not args.no_cpu_baseline:
@@ -312,12 +333,14 @@ def main():
             "e2e": {"value": tot_ok / t_wall if t_wall > 0 else 0.0, "unit": UNIT,
                     "h2d_bytes_per_step": 8 + 4 * max(len(hi), 19), "d2h_bytes_per_step": int(d2h / max(len(timed), 1))},
             "gpu_launches": launches,
-            "roofline": {"kernel": "shift-invert triangular solve (supernodal sweeps, one CUDA graph)",
+            "roofline": {"kernel": f"shift-invert triangular solve of the {len(mesh_k)} complex harmonics "
+                                   "(supernodal sweeps, one CUDA graph per batched solve)",
                          "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak if hbm_peak else None, "traffic": traffic,
                          "per_launch_bytes": per_launch_bytes, "launches": prof["count"],
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
             "cpu_baseline": cpu,
+            "serving": serving,
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)

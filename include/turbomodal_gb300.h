@@ -89,6 +89,12 @@ typedef struct {
 /* Context on one device with a device-memory budget (0 = 90% of free memory).
  * Replaces the per-solver thread pool + memory cap (cyclic_solver.cpp:1226-1273). */
 int tmg_create(int device, size_t mem_budget_bytes, tmg_context** out);
+
+/* Change the device-memory budget of later solves (0 = 90% of the memory free now); the
+ * number of problems factorised together is chosen to fit it.  Replaces the
+ * memory_reserve_fraction argument of solve_at_rpm (python_bindings.cpp:340-360,
+ * cyclic_solver.cpp:1226-1273). */
+int tmg_set_memory_budget(tmg_context* ctx, size_t mem_budget_bytes);
 int tmg_destroy(tmg_context* ctx);
 const char* tmg_last_error(const tmg_context* ctx);
 
@@ -108,7 +114,10 @@ int tmg_assemble(tmg_context* ctx, int which, double rpm, int64_t* nnz,
 int tmg_prepare(tmg_context* ctx, double rpm, int coriolis);
 
 /* Copy a projected matrix (complex interleaved values) after tmg_prepare.
- * k selects the harmonic for TMG_MAT_KK / TMG_MAT_MK.  Pass NULL arrays to query. */
+ * k selects the harmonic for TMG_MAT_KK / TMG_MAT_MK, which are returned on the union of the
+ * projections' structural patterns (the operator the solver factorises): entries that the
+ * reference's pruning removes as roundoff are present as exact zeros.  Pass NULL arrays to
+ * query. */
 int tmg_projection(tmg_context* ctx, int which, int k, int64_t* nnz, int32_t* n,
                    int32_t* colptr, int32_t* rowidx, double* values);
 

@@ -258,9 +258,15 @@ EigResult<T> solve_dense(const Csc<T>& K, const Csc<T>& M, int nev) {
             for (int k = i + 1; k < n; k++) s -= std::conj(L[(size_t)k * n + i]) * x[k];
             x[i] = s / L[(size_t)i * n + i];
         }
-        for (int i = 0; i < n; i++) {
-            if constexpr (std::is_same<T, double>::value) res.vectors[(size_t)t * n + i] = x[i].real();
-            else res.vectors[(size_t)t * n + i] = x[i];
+        if constexpr (std::is_same<T, double>::value) {
+            // a real problem's eigenvector comes out of the complex embedding with an arbitrary
+            // phase (possibly purely imaginary): rotate its largest entry onto the real axis
+            int im = 0;
+            for (int i = 1; i < n; i++) if (std::abs(x[i]) > std::abs(x[im])) im = i;
+            const cd ph = std::abs(x[im]) > 0.0 ? std::conj(x[im]) / std::abs(x[im]) : cd(1.0);
+            for (int i = 0; i < n; i++) res.vectors[(size_t)t * n + i] = (x[i] * ph).real();
+        } else {
+            for (int i = 0; i < n; i++) res.vectors[(size_t)t * n + i] = x[i];
         }
     }
     res.nconv = nev;

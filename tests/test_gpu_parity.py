@@ -180,6 +180,39 @@ def test_batch_same_alone_and_in_the_mix(gpu_solvers):
         np.testing.assert_allclose(alone.frequencies, full[k].frequencies, rtol=1e-9)
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_speed_sequence_same_as_fresh(cfg0, precision):
+    """A solver that has already solved at rest (a different sparsity pattern, so the symbolic
+    analysis is redone) gives the result a fresh solver gives at speed."""
+    from turbomodal_gb300.meshgen import TITANIUM
+    from turbomodal_gb300.solver import CyclicSymmetrySolver
+
+    s = CyclicSymmetrySolver(cfg0, TITANIUM)
+    s.solve_at_rpm(0.0, 5, precision=precision)
+    s.solve_at_rpm(5000.0, 5, precision=precision)
+    seq = {r.harmonic_index: r for r in s.solve_at_rpm(10000.0, 5, precision=precision)}
+    fresh = {r.harmonic_index: r for r in CyclicSymmetrySolver(cfg0, TITANIUM).solve_at_rpm(10000.0, 5,
+                                                                                             precision=precision)}
+    assert sorted(seq) == sorted(fresh)
+    for k in fresh:
+        np.testing.assert_allclose(seq[k].frequencies, fresh[k].frequencies, rtol=1e-9)
+
+
+@pytest.mark.parametrize("rpm", [0.0, 6000.0])
+def test_dense_path_small_sector(oracle, rpm):
+    """n <= 200 (the reference's wedge fixture, 66 free DOF per harmonic): the dense generalized
+    eigensolver against the oracle's restatement of solve_dense (hermitian_lanczos.cpp:68-110)."""
+    from turbomodal_gb300.meshgen import STEEL
+    from turbomodal_gb300.solver import CyclicSymmetrySolver
+
+    m = load_fixture("wedge_sector", 24)
+    res = CyclicSymmetrySolver(m, STEEL).solve_at_rpm(rpm, 5)
+    om = oracle.OracleModel(m, STEEL)
+    om.prepare(rpm)
+    ref = {r["harmonic_index"]: r for r in om.solve(rpm, 5)}
+    check_against_oracle(res, ref)
+
+
 def test_leissa_clamped_disk_gpu(oracle):
     from turbomodal_gb300.meshgen import Material
     from turbomodal_gb300.solver import CyclicSymmetrySolver

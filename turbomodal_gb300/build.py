@@ -29,6 +29,7 @@ UNITS = [
     ("mf.cu", []),
     ("lz.cu", []),
     ("engine.cu", []),
+    ("dense.cu", []),
     ("sym.cpp", []),
 ]
 

@@ -24,8 +24,12 @@ struct numeric_error : std::runtime_error {
     } while (0)
 
 // Every kernel launch of this library goes through TMG_LAUNCH so the host can report
-// how many of its kernels ran in a timed region.
-extern int64_t g_kernel_launches;
+// how many of its kernels ran in a timed region (counted per host thread: a context is
+// driven by one thread at a time).
+extern thread_local int64_t g_kernel_launches;
+// Stream of the context the calling thread is working for (set on entry to every C-ABI call
+// that touches the device); device buffers are allocated, copied and freed in its order.
+extern thread_local cudaStream_t g_stream;
 #define TMG_LAUNCH(kernel, grid, block, smem, stream, ...)                                    \
     do {                                                                                      \
         kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);                            \

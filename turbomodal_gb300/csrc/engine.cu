@@ -21,6 +21,7 @@
 
 #include "../../include/turbomodal_gb300.h"
 #include "engine.hpp"
+#include "dense.cuh"
 #include "fe.cuh"
 
 namespace tmg {
@@ -60,6 +61,18 @@ __global__ void k_gather(int64_t n, const int64_t* __restrict__ idx, const doubl
                          double* __restrict__ out) {
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e < n) out[e] = idx[e] >= 0 ? src[idx[e]] : 0.0;
+}
+
+__global__ void k_gather_masked(int64_t n, const int64_t* __restrict__ idx, const double* __restrict__ v,
+                                const uint8_t* __restrict__ keep, double* __restrict__ out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e < n) out[e] = keep[idx[e]] ? v[idx[e]] : 0.0;
+}
+
+__global__ void k_mask_values(int64_t n, const double* __restrict__ v, const uint8_t* __restrict__ keep,
+                              double* __restrict__ out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e < n) out[e] = keep[e] ? v[e] : 0.0;
 }
 
 template <typename T>
@@ -285,6 +298,34 @@ void extract_free(cudaStream_t st, const ProjChain& ch, const std::vector<int32_
     TMG_CHECK_LAUNCH();
 }
 
+// Structural free-space pattern of a projection chain (every product entry, before pruning).
+void struct_free(const ProjChain& ch, const std::vector<int32_t>& r2free, int32_t nfree, FreeMat& out) {
+    out.spat.nrows = out.spat.ncols = nfree;
+    out.spat.p.assign(nfree + 1, 0);
+    out.spat.i.clear();
+    std::vector<int64_t> idx;
+    for (int32_t j = 0; j < ch.C.ncols; j++) {
+        const int32_t fj = r2free[j];
+        if (fj < 0) continue;
+        for (int64_t q = ch.C.p[j]; q < ch.C.p[j + 1]; q++) {
+            const int32_t fi = r2free[ch.C.i[q]];
+            if (fi >= 0) { out.spat.i.push_back(fi); idx.push_back(q); }
+        }
+        out.spat.p[fj + 1] = (int64_t)out.spat.i.size();
+    }
+    for (int32_t j = 0; j < nfree; j++) out.spat.p[j + 1] = std::max(out.spat.p[j + 1], out.spat.p[j]);
+    out.sidx.upload(idx);
+    out.sv.alloc(idx.size());
+}
+
+// Values on the structural pattern: the pruned value where the entry survives, else 0.
+void struct_values(cudaStream_t st, const ProjChain& ch, FreeMat& out) {
+    if (out.sv.n)
+        TMG_LAUNCH(k_gather_masked, nblk(out.sv.n), 256, 0, st, (int64_t)out.sv.n, out.sidx.p, ch.Cv.p, ch.Cf.p,
+                   out.sv.p);
+    TMG_CHECK_LAUNCH();
+}
+
 // Union of patterns with per-constituent index maps, CSR view and lower triangle.
 void build_union(UnionMaps& um, const std::vector<const Pattern*>& parts) {
     um.U = pattern_union(parts);
@@ -365,13 +406,17 @@ struct tmg_context {
     OpSymbolic symC;
     std::string symC_key;
     UnionMaps W0, WM0;                   // real-sum domains (Kc + s Kp + s Kp^H)
+    Symbolic symRef[3];                  // analyses of the reference patterns (tmg_symbolic)
+    std::string symRef_key[3];
     struct RealOp {
-        FreeMat Kr, Mr;
-        UnionMaps op;
-        OpSymbolic sym;
-        std::string key;
+        FreeMat Kr, Mr;                   // filtered matrices (reference patterns)
+        DVec<double> Ks, Ms;              // the same values on the structural domains W, W_M
         bool valid = false;
     } real[2];                            // 0: k = 0, 1: k = N/2
+    // k = 0 and k = N/2 solved as one batch: operator on W, mass on W_M (structural domains)
+    UnionMaps pairOp, pairM;
+    OpSymbolic pairSym;
+    std::string pair_key;
     std::vector<ResultHost> results;
     double phase_ms[8] = {0};
     int64_t launches = 0;
@@ -389,6 +434,20 @@ struct tmg_context {
 
 namespace {
 
+// Free device memory plus what this process's stream-ordered pool holds unused.
+size_t device_free_bytes(int device) {
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t reserved = 0, used = 0;
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved);
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used);
+        if (reserved > used) fr += (size_t)(reserved - used);
+    }
+    return fr;
+}
+
 int set_err(tmg_context* c, int code, const std::string& m) {
     if (c) c->err = m;
     return code;
@@ -398,6 +457,7 @@ template <typename F>
 int guarded(tmg_context* c, F&& fn) {
     try {
         cudaSetDevice(c->device);
+        g_stream = c->st;
         return fn();
     } catch (const cuda_error& e) {
         return set_err(c, TMG_ERR_CUDA, e.what());
@@ -753,6 +813,12 @@ void project(tmg_context* c, const CandMat& A, ProjChain* ch, Flagged& fl, FreeM
     run_chain(c->st, ch[1], A.v.p, tol);
     extract_free(c->st, ch[0], S.r2free, S.n_free, cf);
     extract_free(c->st, ch[1], S.r2free, S.n_free, pf);
+    if (!same_pat || cf.spat.ncols != S.n_free) {
+        struct_free(ch[0], S.r2free, S.n_free, cf);
+        struct_free(ch[1], S.r2free, S.n_free, pf);
+    }
+    struct_values(c->st, ch[0], cf);
+    struct_values(c->st, ch[1], pf);
 }
 
 bool same_pattern(const Pattern& a, const Pattern& b) { return a.p == b.p && a.i == b.i && a.nrows == b.nrows; }
@@ -776,7 +842,8 @@ void prepare(tmg_context* c, double rpm, bool coriolis) {
             launch_elem_ksig(c->st, S.ne, S.dX.p, S.dconn.p, S.E, S.nu, c->u_static.p, S.Kel.p, bad.p);
             gather_into(c, S.Kel.p, c->Ks);
             int hb = 0;
-            TMG_CUDA(cudaMemcpy(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost));
+            TMG_CUDA(cudaMemcpyAsync(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+            TMG_CUDA(cudaStreamSynchronize(c->st));
             if (hb) throw numeric_error("TET10::B_matrix: singular Jacobian (degenerate element)");
             launch_cand_axpy3(c->st, nc, 1.0, c->K.v.p, c->K.f.p, -1.0, c->Kw.v.p, c->Kw.f.p, 1.0, c->Ks.v.p,
                               c->Ks.f.p, c->Keff.v.p, c->Keff.f.p);
@@ -792,15 +859,18 @@ void prepare(tmg_context* c, double rpm, bool coriolis) {
     project(c, c->M, c->chM, c->fM, c->Mcf, c->Mpf, 1e-27);
     c->coriolis = coriolis && std::fabs(omega) > 0.0;
     if (c->coriolis) project(c, c->G, c->chG, c->fG, c->Gcf, c->Gpf, 1e-27);
-    // complex harmonic operator: union of Kc, Kp, Kp^H, Mc, Mp, Mp^H
-    c->KpfH = transpose_map(c->Kpf.pat, c->kpT);
-    c->MpfH = transpose_map(c->Mpf.pat, c->mpT);
-    Pattern U = pattern_union({&c->Kcf.pat, &c->Kpf.pat, &c->KpfH, &c->Mcf.pat, &c->Mpf.pat, &c->MpfH});
-    const std::string key = pattern_key(U) + pattern_key(c->Kcf.pat) + pattern_key(c->Kpf.pat) +
-                            pattern_key(c->Mcf.pat) + pattern_key(c->Mpf.pat);
+    // Operators are built on the structural patterns of the projections (entries the reference
+    // prunes as roundoff are exact zeros there), which do not change with the speed: the
+    // unions, maps and symbolic analyses below are rebuilt only when the sector operator's own
+    // pattern changes (in practice once at rest and once at speed).
+    c->KpfH = transpose_map(c->Kpf.spat, c->kpT);
+    c->MpfH = transpose_map(c->Mpf.spat, c->mpT);
+    const std::string key = pattern_key(c->Kcf.spat) + pattern_key(c->Kpf.spat) + pattern_key(c->Mcf.spat) +
+                            pattern_key(c->Mpf.spat);
     if (key != c->symC_key) {
-        build_union(c->opC, {&c->Kcf.pat, &c->Kpf.pat, &c->KpfH, &c->Mcf.pat, &c->Mpf.pat, &c->MpfH});
-        build_union(c->opMC, {&c->Mcf.pat, &c->Mpf.pat, &c->MpfH});
+        // complex harmonic operator: union of Kc, Kp, Kp^H, Mc, Mp, Mp^H
+        build_union(c->opC, {&c->Kcf.spat, &c->Kpf.spat, &c->KpfH, &c->Mcf.spat, &c->Mpf.spat, &c->MpfH});
+        build_union(c->opMC, {&c->Mcf.spat, &c->Mpf.spat, &c->MpfH});
         // transposed-constituent maps must address the un-transposed value arrays
         for (int which : {2, 5}) {
             const std::vector<int64_t>& tm = which == 2 ? c->kpT : c->mpT;
@@ -816,34 +886,40 @@ void prepare(tmg_context* c, double rpm, bool coriolis) {
         c->symC.valid = false;
         c->symC_key = key;
         // real sums domain W = Kc u Kp u Kp^H (and the mass analogue)
-        build_union(c->W0, {&c->Kcf.pat, &c->Kpf.pat, &c->KpfH});
-        build_union(c->WM0, {&c->Mcf.pat, &c->Mpf.pat, &c->MpfH});
+        build_union(c->W0, {&c->Kcf.spat, &c->Kpf.spat, &c->KpfH});
+        build_union(c->WM0, {&c->Mcf.spat, &c->Mpf.spat, &c->MpfH});
         for (UnionMaps* w : {&c->W0, &c->WM0}) {
             const std::vector<int64_t>& tm = (w == &c->W0) ? c->kpT : c->mpT;
             std::vector<int64_t> m = w->maps[2].download();
             for (auto& v : m) if (v >= 0) v = tm[v];
             w->maps[2].upload(m);
         }
+        // real harmonics k = 0 and N/2: operator K on W, mass on W_M, both problems one batch
+        build_union(c->pairOp, {&c->W0.U, &c->WM0.U});
+        build_union(c->pairM, {&c->WM0.U});
+        c->pairSym.valid = false;
+        c->pair_key = key;
     }
-    // real k = 0 / N/2 matrices: filtered sums (cyclic_solver.cpp:673-723)
+    // real k = 0 / N/2 matrices: filtered sums (cyclic_solver.cpp:673-723); the filtered
+    // patterns are what tmg_projection reports, the masked values on W / W_M feed the solver
     for (int h = 0; h < 2; h++) {
         if (h == 1 && !(S.ns % 2 == 0 && S.ns / 2 > 0)) { c->real[h].valid = false; continue; }
         const double sgn = h == 0 ? 1.0 : -1.0;
         auto& R = c->real[h];
-        Pattern newK, newM;
-        DVec<double> kv, mv;
-        DVec<uint8_t> kf, mf;
         for (int which = 0; which < 2; which++) {
             UnionMaps& w = which == 0 ? c->W0 : c->WM0;
             const FreeMat& cc = which == 0 ? c->Kcf : c->Mcf;
             const FreeMat& pp = which == 0 ? c->Kpf : c->Mpf;
-            DVec<double>& vv = which == 0 ? kv : mv;
-            DVec<uint8_t>& ff = which == 0 ? kf : mf;
+            DVec<double> vv;
+            DVec<uint8_t> ff;
             vv.alloc(w.U.nnz());
             ff.alloc(w.U.nnz());
             if (w.U.nnz())
                 TMG_LAUNCH(k_form_real_sum, nblk(w.U.nnz()), 256, 0, c->st, w.U.nnz(), w.maps[0].p, w.maps[1].p,
-                           w.maps[2].p, cc.v.p, pp.v.p, sgn, vv.p, ff.p);
+                           w.maps[2].p, cc.sv.p, pp.sv.p, sgn, vv.p, ff.p);
+            DVec<double>& sv = which == 0 ? R.Ks : R.Ms;
+            sv.alloc(w.U.nnz());
+            if (w.U.nnz()) TMG_LAUNCH(k_mask_values, nblk(w.U.nnz()), 256, 0, c->st, w.U.nnz(), vv.p, ff.p, sv.p);
             Flagged fl = flagged(w.U, ff.download());
             FreeMat& dst = which == 0 ? R.Kr : R.Mr;
             dst.pat = fl.pat;
@@ -853,12 +929,6 @@ void prepare(tmg_context* c, double rpm, bool coriolis) {
                 TMG_LAUNCH(k_gather, nblk(fl.cand.size()), 256, 0, c->st, (int64_t)fl.cand.size(), dst.idx.p, vv.p,
                            dst.v.p);
             TMG_CUDA(cudaStreamSynchronize(c->st));
-        }
-        const std::string rkey = pattern_key(R.Kr.pat) + pattern_key(R.Mr.pat);
-        if (!R.valid || rkey != R.key) {
-            build_union(R.op, {&R.Kr.pat, &R.Mr.pat});
-            R.sym.valid = false;
-            R.key = rkey;
         }
         R.valid = true;
     }
@@ -1229,7 +1299,8 @@ std::vector<EigOut<Tv>> lanczos(tmg_context* c, ShiftInvertB<Tv, Tf>& op, const 
         std::vector<Tv> v0(n);
         for (int64_t i = 0; i < n; i++) v0[i] = rnd_entry<Tv>(gen, dist);
         for (int p = 0; p < B; p++)
-            TMG_CUDA(cudaMemcpy(V.p + p * vs, v0.data(), n * sizeof(Tv), cudaMemcpyHostToDevice));
+            TMG_CUDA(cudaMemcpyAsync(V.p + p * vs, v0.data(), n * sizeof(Tv), cudaMemcpyHostToDevice, st));
+        TMG_CUDA(cudaStreamSynchronize(st));
         lz_spmv<Tv>(st, B, M, V.p, vs, MV.p, vs, 1, n);
         lz_multidot<Tv>(st, B, n, V.p, vs, n, 1, MV.p, vs, part.p, dot.p);
         lz_scale_first<Tv>(st, B, n, dot.p, V.p, MV.p, vs);
@@ -1273,9 +1344,11 @@ std::vector<EigOut<Tv>> lanczos(tmg_context* c, ShiftInvertB<Tv, Tf>& op, const 
             ne = std::min(ne, nev);
             std::vector<double> Sh((size_t)m * m), lh(m);
             std::vector<int> oh(m);
-            TMG_CUDA(cudaMemcpy(Sh.data(), S.p + (int64_t)p * ncv * ncv, Sh.size() * sizeof(double), cudaMemcpyDeviceToHost));
-            TMG_CUDA(cudaMemcpy(lh.data(), lam.p + (int64_t)p * ncv, m * sizeof(double), cudaMemcpyDeviceToHost));
-            TMG_CUDA(cudaMemcpy(oh.data(), order.p + (int64_t)p * ncv, m * sizeof(int), cudaMemcpyDeviceToHost));
+            TMG_CUDA(cudaMemcpyAsync(Sh.data(), S.p + (int64_t)p * ncv * ncv, Sh.size() * sizeof(double),
+                                     cudaMemcpyDeviceToHost, st));
+            TMG_CUDA(cudaMemcpyAsync(lh.data(), lam.p + (int64_t)p * ncv, m * sizeof(double), cudaMemcpyDeviceToHost, st));
+            TMG_CUDA(cudaMemcpyAsync(oh.data(), order.p + (int64_t)p * ncv, m * sizeof(int), cudaMemcpyDeviceToHost, st));
+            TMG_CUDA(cudaStreamSynchronize(st));
             std::vector<double> Csel((size_t)m * ne);
             out[p].lam.resize(ne);
             for (int t = 0; t < ne; t++) {
@@ -1323,7 +1396,7 @@ struct Problem {
 // sector DOFs.
 template <typename Tv>
 void finish_result(tmg_context* c, const Problem& pr, EigOut<Tv>& eo, const DevCsr<Tv>& A, const DevCsr<Tv>& M,
-                   double shift, int num_modes, double min_frequency) {
+                   double shift, int num_modes, double min_frequency, const double* residuals = nullptr) {
     Sector& S = *c->sec;
     ResultHost& R = *pr.R;
     cudaStream_t st = c->st;
@@ -1346,7 +1419,9 @@ void finish_result(tmg_context* c, const Problem& pr, EigOut<Tv>& eo, const DevC
         lz_copy<Tv>(st, n, eo.X.p + (int64_t)keep[t] * n, Xk.p + (int64_t)t * n);
         R.freqs.push_back(lam[t] > 0.0 ? std::sqrt(lam[t]) / (2.0 * PI) : 0.0);
     }
-    if (nk > 0) {   // ||K x - lambda M x|| / ||K x|| (cyclic_solver.cpp:1099-1114)
+    if (nk > 0 && residuals) {   // computed with the dense matrices
+        for (int t = 0; t < nk; t++) R.max_residual = std::max(R.max_residual, residuals[keep[t]]);
+    } else if (nk > 0) {   // ||K x - lambda M x|| / ||K x|| (cyclic_solver.cpp:1099-1114)
         DVec<Tv> AX, MX, KX, RR;
         DVec<double> dl, np, nr;
         AX.alloc((size_t)n * nk); MX.alloc((size_t)n * nk); KX.alloc((size_t)n * nk); RR.alloc((size_t)n * nk);
@@ -1393,7 +1468,10 @@ void finish_result(tmg_context* c, const Problem& pr, EigOut<Tv>& eo, const DevC
                        c->d_isr.p, c->d_r2free.p, Xsrc, n, pr.P, full.p, (int64_t)ndof);
     TMG_CHECK_LAUNCH();
     R.shapes.resize((size_t)ndof * nm);
-    if (nm) TMG_CUDA(cudaMemcpy(R.shapes.data(), full.p, R.shapes.size() * sizeof(zd), cudaMemcpyDeviceToHost));
+    if (nm) {
+        TMG_CUDA(cudaMemcpyAsync(R.shapes.data(), full.p, R.shapes.size() * sizeof(zd), cudaMemcpyDeviceToHost, st));
+        TMG_CUDA(cudaStreamSynchronize(st));
+    }
 }
 
 // Factor and solve a batch of problems that share one symbolic analysis.
@@ -1458,9 +1536,7 @@ int batch_size(tmg_context* c, const OpSymbolic& os, const UnionMaps& um, int64_
     const double per = fb * (double)(D.l_entries + D.u_entries + D.t_entries + n) +
                        vb * (double)(3 * um.U.nnz() + 2 * um.lower2csc.n + 2 * nM) +
                        vb * n * (2.0 * (ncv + 1) + 12.0) + 8.0 * ncv * ncv * 4;
-    size_t fr = 0, tot = 0;
-    cudaMemGetInfo(&fr, &tot);
-    const double avail = std::min<double>((double)c->budget, 0.85 * (double)fr);
+    const double avail = std::min<double>((double)c->budget, 0.85 * (double)device_free_bytes(c->device));
     const int b = (int)std::floor(avail / per);
     if (b < 1) throw numeric_error("device memory budget too small for one problem");
     return std::max(1, std::min(nprob, b));
@@ -1475,7 +1551,7 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
     const bool mixed = precision == TMG_PREC_MIXED;
     const double shift = 1.0;
     results.assign(ks.size(), ResultHost{});
-    std::vector<Problem> cplx, real0, realh;
+    std::vector<Problem> cplx, real0, realh, dense;
     for (size_t q = 0; q < ks.size(); q++) {
         const int k = ks[q];
         ResultHost& R = results[q];
@@ -1489,48 +1565,128 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
         pr.degenerate = (k > 0) && !(N % 2 == 0 && k == max_k);
         if (c->coriolis && k > 0) { R.status = TMG_ERR_STATE; continue; }
         pr.nev_target = pr.degenerate ? (num_modes + 1) / 2 : num_modes;
-        if (S.n_free <= 200) { R.status = TMG_ERR_ARG; continue; }
         const bool is_real = (k == 0) || (N % 2 == 0 && k == max_k);
+        if (S.n_free <= 200) { dense.push_back(pr); continue; }
         if (!is_real) cplx.push_back(pr);
         else if (k == 0) real0.push_back(pr);
         else realh.push_back(pr);
     }
     const int n_extra = min_frequency > 0.0 ? 6 : 0;
-    // real harmonics k = 0, N/2 (B = 1 each: own operators)
-    for (auto* grp : {&real0, &realh}) {
-        if (grp->empty()) continue;
-        Problem& pr = (*grp)[0];
-        auto& RO = c->real[pr.k == 0 ? 0 : 1];
-        if (!RO.valid) { pr.R->status = TMG_ERR_STATE; continue; }
-        if (!RO.sym.valid) analyze_op(RO.sym, RO.op);
-        int nev = std::min(pr.nev_target + n_extra, S.n_free - 1);
-        const int ncv = std::min(std::max(4 * nev + 1, 40), S.n_free);
-        nev = std::min(nev, S.n_free - 1);
-        DVec<double> vals;
-        vals.alloc(RO.op.U.nnz());
-        if (vals.n)
-            TMG_LAUNCH(k_form_real_op, nblk(vals.n), 256, 0, st, (int64_t)vals.n, RO.op.maps[0].p, RO.op.maps[1].p,
-                       RO.Kr.v.p, RO.Mr.v.p, shift, 1.0, vals.p);
-        std::vector<int64_t> mp;
-        Pattern Mt = transpose_map(RO.Mr.pat, mp);
-        DVec<int64_t> mrp, mperm;
-        DVec<int32_t> mci;
-        mrp.upload(Mt.p); mci.upload(Mt.i); mperm.upload(mp);
-        DVec<double> mv;
-        mv.alloc(mp.size());
-        if (mv.n) TMG_LAUNCH(k_gather_t<double>, nblk(mv.n), 256, 0, st, (int64_t)mv.n, mperm.p, RO.Mr.v.p, mv.p);
-        DevCsr<double> M;
-        M.nrows = S.n_free; M.nnz = mv.n; M.rowptr = mrp.p; M.col = mci.p; M.val = mv.p; M.vstride = 0;
-        try {
-            if (mixed)
-                run_batch<double, float>(c, *grp, RO.sym, RO.op, vals.p, M, nev, ncv, shift, 1000, true, num_modes,
-                                         min_frequency);
-            else
-                run_batch<double, double>(c, *grp, RO.sym, RO.op, vals.p, M, nev, ncv, shift, 1000, false, num_modes,
-                                          min_frequency);
-        } catch (const numeric_error& e) {
-            pr.R->status = TMG_ERR_NUMERIC;
-            c->err = e.what();
+    // small sectors (n <= 200): dense generalized eigensolver, all harmonics in one launch
+    // (src/hermitian_lanczos.cpp:68-110, :283)
+    if (!dense.empty()) {
+        const int n = S.n_free;
+        const int B = (int)dense.size();
+        int nev = 1;                                           // computed for every problem
+        for (const Problem& pr : dense) nev = std::max(nev, std::min(pr.nev_target + n_extra, n - 1));
+        const int64_t nn = (int64_t)n * n;
+        DVec<zd> Kd, Md, work, X;
+        DVec<double> lam, res;
+        DVec<int> status;
+        Kd.alloc((size_t)B * nn); Md.alloc((size_t)B * nn); work.alloc((size_t)B * 5 * nn);
+        X.alloc((size_t)B * n * nev); lam.alloc((size_t)B * nev); res.alloc((size_t)B * nev); status.alloc(B);
+        status.zero(st);
+        for (int p = 0; p < B; p++) {
+            const Problem& pr = dense[p];
+            const bool is_real = (pr.k == 0) || (N % 2 == 0 && pr.k == max_k);
+            for (int which = 0; which < 2; which++) {      // 0: K_k, 1: M_k
+                DVec<int64_t> cp;
+                DVec<int32_t> ri;
+                DVec<zd> v;
+                if (is_real) {
+                    const auto& R = c->real[pr.k == 0 ? 0 : 1];
+                    if (!R.valid) throw numeric_error("real harmonic operator missing");
+                    const FreeMat& fm = which == 0 ? R.Kr : R.Mr;
+                    cp.upload(fm.pat.p); ri.upload(fm.pat.i);
+                    v.alloc(std::max<size_t>(1, fm.v.n));
+                    if (fm.v.n) TMG_LAUNCH(k_real_to_complex, nblk(fm.v.n), 256, 0, st, (int64_t)fm.v.n, fm.v.p, v.p);
+                } else {
+                    const UnionMaps& w = which == 0 ? c->W0 : c->WM0;
+                    const FreeMat& cc = which == 0 ? c->Kcf : c->Mcf;
+                    const FreeMat& pp = which == 0 ? c->Kpf : c->Mpf;
+                    cp.upload(w.U.p); ri.upload(w.U.i);
+                    DVec<double> ph;
+                    ph.upload(std::vector<double>{pr.P.x, pr.P.y});
+                    v.alloc(std::max<int64_t>(1, w.U.nnz()));
+                    if (w.U.nnz())
+                        TMG_LAUNCH(k_form_csum, dim3(nblk(w.U.nnz()), 1), 256, 0, st, w.U.nnz(), w.maps[0].p,
+                                   w.maps[1].p, w.maps[2].p, cc.sv.p, pp.sv.p, ph.p, v.p);
+                    TMG_CUDA(cudaStreamSynchronize(st));
+                }
+                dense_csc_to_dense(st, n, cp.p, ri.p, v.p, (which == 0 ? Kd.p : Md.p) + p * nn);
+                TMG_CUDA(cudaStreamSynchronize(st));
+            }
+        }
+        auto t1 = std::chrono::steady_clock::now();
+        dense_geig(st, B, n, nev, Kd.p, Md.p, work.p, lam.p, X.p, res.p, status.p);
+        const std::vector<double> hl = lam.download(), hr = res.download();
+        const std::vector<int> hs = status.download();
+        auto t2 = std::chrono::steady_clock::now();
+        c->phase_ms[2] += std::chrono::duration<double, std::milli>(t2 - t1).count();
+        DevCsr<zd> none;
+        for (int p = 0; p < B; p++) {
+            ResultHost& R = *dense[p].R;
+            if (hs[p]) { R.status = TMG_ERR_NUMERIC; c->err = "dense eigensolver: M is not positive definite"; continue; }
+            const int nev_p = std::max(1, std::min(dense[p].nev_target + n_extra, n - 1));
+            EigOut<zd> eo;
+            eo.ne = nev_p;
+            eo.converged = true;
+            eo.lam.assign(hl.begin() + (int64_t)p * nev, hl.begin() + (int64_t)p * nev + nev_p);
+            eo.X.alloc((size_t)n * nev_p);
+            lz_copy<zd>(st, (int64_t)n * nev_p, X.p + (int64_t)p * n * nev, eo.X.p);
+            R.converged = 1;
+            finish_result<zd>(c, dense[p], eo, none, none, shift, num_modes, min_frequency, hr.data() + (int64_t)p * nev);
+        }
+        c->phase_ms[3] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t2).count();
+    }
+    // real harmonics k = 0 and N/2: one batch (of one or two problems) on the structural
+    // domains W (operator) and W_M (mass), whose analysis is shared by both and by every speed
+    {
+        std::vector<Problem> grp;
+        for (auto* g : {&real0, &realh})
+            for (auto& pr : *g) {
+                if (!c->real[pr.k == 0 ? 0 : 1].valid) { pr.R->status = TMG_ERR_STATE; continue; }
+                grp.push_back(pr);
+            }
+        if (!grp.empty()) {
+            if (!c->pairSym.valid) analyze_op(c->pairSym, c->pairOp);
+            const int nev = std::min(grp[0].nev_target + n_extra, S.n_free - 1);
+            const int ncv = std::min(std::max(4 * nev + 1, 40), S.n_free);
+            UnionMaps& um = c->pairOp;
+            UnionMaps& mu = c->pairM;
+            const int B = (int)grp.size();
+            const int64_t nU = um.U.nnz(), nMU = mu.U.nnz();
+            DVec<double> vals, mcsc, mcsr;
+            vals.alloc((size_t)B * nU);
+            mcsc.alloc((size_t)B * nMU);
+            mcsr.alloc((size_t)B * nMU);
+            for (int q = 0; q < B; q++) {
+                const auto& R = c->real[grp[q].k == 0 ? 0 : 1];
+                if (nU)
+                    TMG_LAUNCH(k_form_real_op, nblk(nU), 256, 0, st, nU, um.maps[0].p, um.maps[1].p, R.Ks.p, R.Ms.p,
+                               shift, 1.0, vals.p + q * nU);
+                if (nMU)
+                    TMG_LAUNCH(k_form_real_op, nblk(nMU), 256, 0, st, nMU, mu.maps[0].p, mu.maps[0].p, R.Ms.p, R.Ms.p,
+                               0.0, 1.0, mcsc.p + q * nMU);
+            }
+            if (nMU)
+                TMG_LAUNCH(k_gather_b<double>, dim3(nblk(nMU), B), 256, 0, st, nMU, mu.csr2csc.p, mcsc.p, nMU, mcsr.p,
+                           nMU);
+            mcsc.release();
+            DevCsr<double> M;
+            M.nrows = S.n_free; M.nnz = nMU; M.rowptr = mu.csr_rowptr.p; M.col = mu.csr_col.p; M.val = mcsr.p;
+            M.vstride = nMU;
+            try {
+                if (mixed)
+                    run_batch<double, float>(c, grp, c->pairSym, um, vals.p, M, nev, ncv, shift, 1000, true, num_modes,
+                                             min_frequency);
+                else
+                    run_batch<double, double>(c, grp, c->pairSym, um, vals.p, M, nev, ncv, shift, 1000, false,
+                                              num_modes, min_frequency);
+            } catch (const numeric_error& e) {
+                for (auto& pr : grp) pr.R->status = TMG_ERR_NUMERIC;
+                c->err = e.what();
+            }
         }
     }
     // complex harmonics: one shared symbolic analysis, batched under the memory budget
@@ -1554,11 +1710,11 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
             mcsr.alloc((size_t)B * mu.U.nnz());
             if (um.U.nnz())
                 TMG_LAUNCH(k_form_complex, dim3(nblk(um.U.nnz()), B), 256, 0, st, um.U.nnz(), um.maps[0].p, um.maps[1].p,
-                           um.maps[2].p, um.maps[3].p, um.maps[4].p, um.maps[5].p, c->Kcf.v.p, c->Kpf.v.p, c->Mcf.v.p,
-                           c->Mpf.v.p, dph.p, shift, vals.p);
+                           um.maps[2].p, um.maps[3].p, um.maps[4].p, um.maps[5].p, c->Kcf.sv.p, c->Kpf.sv.p, c->Mcf.sv.p,
+                           c->Mpf.sv.p, dph.p, shift, vals.p);
             if (mu.U.nnz()) {
                 TMG_LAUNCH(k_form_csum, dim3(nblk(mu.U.nnz()), B), 256, 0, st, mu.U.nnz(), mu.maps[0].p, mu.maps[1].p,
-                           mu.maps[2].p, c->Mcf.v.p, c->Mpf.v.p, dph.p, mvals.p);
+                           mu.maps[2].p, c->Mcf.sv.p, c->Mpf.sv.p, dph.p, mvals.p);
                 TMG_LAUNCH(k_gather_b<zd>, dim3(nblk(mu.U.nnz()), B), 256, 0, st, mu.U.nnz(), mu.csr2csc.p, mvals.p,
                            mu.U.nnz(), mcsr.p, mu.U.nnz());
             }
@@ -1597,7 +1753,11 @@ int copy_csc(const Pattern& P, const double* dvals_or_null, const std::vector<do
         if (hvals) v = *hvals;
         else {
             v.resize(P.nnz());
-            if (P.nnz()) TMG_CUDA(cudaMemcpy(v.data(), dvals_or_null, v.size() * sizeof(double), cudaMemcpyDeviceToHost));
+            if (P.nnz()) {
+                TMG_CUDA(cudaMemcpyAsync(v.data(), dvals_or_null, v.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                         g_stream));
+                TMG_CUDA(cudaStreamSynchronize(g_stream));
+            }
         }
         if (complex_out)
             for (int64_t q = 0; q < P.nnz(); q++) { values[2 * q] = v[q]; values[2 * q + 1] = 0.0; }
@@ -1621,23 +1781,42 @@ int tmg_create(int device, size_t mem_budget_bytes, tmg_context** out) {
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return TMG_ERR_CUDA;
     auto* c = new tmg_context();
     c->device = device;
-    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreate(&c->st) != cudaSuccess) {
+    // non-blocking stream: contexts driven from different host threads overlap on the device
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
         delete c;
         return TMG_ERR_CUDA;
     }
-    size_t fr = 0, tot = 0;
-    cudaMemGetInfo(&fr, &tot);
-    c->budget = mem_budget_bytes ? mem_budget_bytes : (size_t)(0.9 * fr);
+    {   // keep freed stream-ordered allocations in this process's pool instead of returning them
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t thr = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    }
+    c->budget = mem_budget_bytes ? mem_budget_bytes : (size_t)(0.9 * (double)device_free_bytes(device));
     *out = c;
     return TMG_OK;
+}
+
+int tmg_set_memory_budget(tmg_context* c, size_t mem_budget_bytes) {
+    if (!c) return TMG_ERR_ARG;
+    return guarded(c, [&]() {
+        c->budget = mem_budget_bytes ? mem_budget_bytes : (size_t)(0.9 * (double)device_free_bytes(c->device));
+        return TMG_OK;
+    });
 }
 
 int tmg_destroy(tmg_context* c) {
     if (!c) return TMG_ERR_ARG;
     cudaSetDevice(c->device);
     cudaStream_t st = c->st;
+    g_stream = st;                     // the context's buffers are freed in its stream's order
     delete c;
-    if (st) cudaStreamDestroy(st);
+    g_stream = nullptr;
+    if (st) {
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+    }
     return TMG_OK;
 }
 
@@ -1717,13 +1896,16 @@ int tmg_projection(tmg_context* c, int which, int k, int64_t* nnz, int32_t* n, i
                 ph.upload(std::vector<double>{std::cos(k * alpha), std::sin(k * alpha)});
                 if (v.n)
                     TMG_LAUNCH(k_form_csum, dim3(nblk(v.n), 1), 256, 0, c->st, (int64_t)v.n, w.maps[0].p, w.maps[1].p,
-                               w.maps[2].p, cc.v.p, pp.v.p, ph.p, v.p);
+                               w.maps[2].p, cc.sv.p, pp.sv.p, ph.p, v.p);
                 TMG_CUDA(cudaStreamSynchronize(c->st));
                 *nnz = w.U.nnz();
                 if (!colptr) return TMG_OK;
                 for (int32_t j = 0; j <= w.U.ncols; j++) colptr[j] = (int32_t)w.U.p[j];
                 if (rowidx) std::copy(w.U.i.begin(), w.U.i.end(), rowidx);
-                if (values && v.n) TMG_CUDA(cudaMemcpy(values, v.p, v.n * sizeof(zd), cudaMemcpyDeviceToHost));
+                if (values && v.n) {
+                    TMG_CUDA(cudaMemcpyAsync(values, v.p, v.n * sizeof(zd), cudaMemcpyDeviceToHost, c->st));
+                    TMG_CUDA(cudaStreamSynchronize(c->st));
+                }
                 return TMG_OK;
             }
             default: return set_err(c, TMG_ERR_ARG, "unknown projection selector");
@@ -1737,22 +1919,35 @@ int tmg_symbolic(tmg_context* c, int kind, int32_t* n, int32_t* perm, int32_t* p
     if (!c || !n) return TMG_ERR_ARG;
     if (!c->prepared) return set_err(c, TMG_ERR_STATE, "call tmg_prepare first");
     return guarded(c, [&]() {
-        OpSymbolic* os = nullptr;
+        // the analysis of the reference's operator pattern (pruned / filtered matrices)
+        const Symbolic* sp = nullptr;
         if (kind == 0) {
-            if (!c->symC.valid) analyze_op(c->symC, c->opC);
-            os = &c->symC;
+            std::vector<int64_t> t1, t2;
+            const Pattern kh = transpose_map(c->Kpf.pat, t1), mh = transpose_map(c->Mpf.pat, t2);
+            const Pattern U = pattern_union({&c->Kcf.pat, &c->Kpf.pat, &kh, &c->Mcf.pat, &c->Mpf.pat, &mh});
+            const std::string key = pattern_key(U);
+            if (key != c->symRef_key[0]) {
+                c->symRef[0] = analyze(lower_triangle(U), 0.0, 0);
+                c->symRef_key[0] = key;
+            }
+            sp = &c->symRef[0];
         } else if (kind == 1 || kind == 2) {
             auto& RO = c->real[kind - 1];
             if (!RO.valid) return set_err(c, TMG_ERR_STATE, "no such real harmonic");
-            if (!RO.sym.valid) analyze_op(RO.sym, RO.op);
-            os = &RO.sym;
+            const Pattern U = pattern_union({&RO.Kr.pat, &RO.Mr.pat});
+            const std::string key = pattern_key(U);
+            if (key != c->symRef_key[kind]) {
+                c->symRef[kind] = analyze(lower_triangle(U), 0.0, 0);
+                c->symRef_key[kind] = key;
+            }
+            sp = &c->symRef[kind];
         } else {
             return set_err(c, TMG_ERR_ARG, "unknown symbolic kind");
         }
-        *n = os->S.n;
-        if (perm) std::copy(os->S.amd.begin(), os->S.amd.end(), perm);
-        if (parent) std::copy(os->S.etree.begin(), os->S.etree.end(), parent);
-        if (colcount) std::copy(os->S.colcount.begin(), os->S.colcount.end(), colcount);
+        *n = sp->n;
+        if (perm) std::copy(sp->amd.begin(), sp->amd.end(), perm);
+        if (parent) std::copy(sp->etree.begin(), sp->etree.end(), parent);
+        if (colcount) std::copy(sp->colcount.begin(), sp->colcount.end(), colcount);
         return TMG_OK;
     });
 }
@@ -1761,15 +1956,15 @@ int tmg_symbolic_stats(tmg_context* c, int kind, double* out) {
     if (!c || !out) return TMG_ERR_ARG;
     if (!c->prepared) return set_err(c, TMG_ERR_STATE, "call tmg_prepare first");
     return guarded(c, [&]() {
+        // the factorisation the solver runs (structural operator pattern)
         OpSymbolic* os = nullptr;
         if (kind == 0) {
             if (!c->symC.valid) analyze_op(c->symC, c->opC);
             os = &c->symC;
         } else if (kind == 1 || kind == 2) {
-            auto& RO = c->real[kind - 1];
-            if (!RO.valid) return set_err(c, TMG_ERR_STATE, "no such real harmonic");
-            if (!RO.sym.valid) analyze_op(RO.sym, RO.op);
-            os = &RO.sym;
+            if (!c->real[kind - 1].valid) return set_err(c, TMG_ERR_STATE, "no such real harmonic");
+            if (!c->pairSym.valid) analyze_op(c->pairSym, c->pairOp);
+            os = &c->pairSym;
         } else {
             return set_err(c, TMG_ERR_ARG, "unknown symbolic kind");
         }
@@ -1932,8 +2127,8 @@ extern "C" int tmg_projection_harmonic_static(tmg_context* c, int which, int k, 
         zd* out = static_scratch(c->device);
         const double alpha = 2.0 * PI / S.ns;
         if (ne)
-            TMG_LAUNCH(k_form_csum_static, nblk(ne), 256, 0, c->st, ne, w.maps[0].p, w.maps[1].p, w.maps[2].p, cc.v.p,
-                       pp.v.p, std::cos(k * alpha), std::sin(k * alpha), out);
+            TMG_LAUNCH(k_form_csum_static, nblk(ne), 256, 0, c->st, ne, w.maps[0].p, w.maps[1].p, w.maps[2].p, cc.sv.p,
+                       pp.sv.p, std::cos(k * alpha), std::sin(k * alpha), out);
         TMG_CHECK_LAUNCH();
         for (int32_t j = 0; j <= w.U.ncols; j++) colptr[j] = (int32_t)w.U.p[j];
         if (rowidx) std::copy(w.U.i.begin(), w.U.i.end(), rowidx);

@@ -22,29 +22,48 @@ template <typename T>
 struct DVec {
     T* p = nullptr;
     size_t n = 0;
+    cudaStream_t s_ = nullptr;       // stream the buffer was allocated on (freed in its order)
     DVec() = default;
     DVec(const DVec&) = delete;
     DVec& operator=(const DVec&) = delete;
-    DVec(DVec&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
-    DVec& operator=(DVec&& o) noexcept { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; return *this; }
+    DVec(DVec&& o) noexcept : p(o.p), n(o.n), s_(o.s_) { o.p = nullptr; o.n = 0; }
+    DVec& operator=(DVec&& o) noexcept {
+        release();
+        p = o.p; n = o.n; s_ = o.s_;
+        o.p = nullptr; o.n = 0;
+        return *this;
+    }
     ~DVec() { release(); }
+    // stream-ordered allocation on the calling context's stream
     void alloc(size_t count) {
         if (count == n && p) return;
         release();
         n = count;
-        if (count) TMG_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
+        s_ = g_stream;
+        if (count) TMG_CUDA(cudaMallocAsync((void**)&p, count * sizeof(T), s_));
     }
     void zero(cudaStream_t st) { if (n) TMG_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), st)); }
     void upload(const std::vector<T>& h) {
         alloc(h.size());
-        if (n) TMG_CUDA(cudaMemcpy(p, h.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+        if (n) {
+            TMG_CUDA(cudaMemcpyAsync(p, h.data(), n * sizeof(T), cudaMemcpyHostToDevice, s_));
+            TMG_CUDA(cudaStreamSynchronize(s_));
+        }
     }
     std::vector<T> download() const {
         std::vector<T> h(n);
-        if (n) TMG_CUDA(cudaMemcpy(h.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost));
+        if (n) {
+            cudaStream_t st = s_ ? s_ : g_stream;
+            TMG_CUDA(cudaMemcpyAsync(h.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost, st));
+            TMG_CUDA(cudaStreamSynchronize(st));
+        }
         return h;
     }
-    void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+    void release() {
+        if (p) cudaFreeAsync(p, s_);
+        p = nullptr;
+        n = 0;
+    }
     size_t bytes() const { return n * sizeof(T); }
 };
 
@@ -73,9 +92,14 @@ struct ProjChain {
 
 // A free-space matrix extracted from a projection: pattern + gather indices into C values.
 struct FreeMat {
-    Pattern pat;                         // n_free x n_free
+    Pattern pat;                         // n_free x n_free, after the reference's pruning
     DVec<int64_t> idx;                   // entry -> index in ProjChain::Cv
     DVec<double> v;                      // values (real-valued projections)
+    // structural pattern: every entry the projection can produce (does not depend on the
+    // values, so analyses built on it hold for every speed); pruned entries are exact zeros
+    Pattern spat;
+    DVec<int64_t> sidx;
+    DVec<double> sv;
 };
 
 // Index maps of a union pattern onto its constituent matrices (entry index or -1).

@@ -14,12 +14,14 @@
 // same L and D in exact arithmetic.
 #include <algorithm>
 #include <map>
+#include <mutex>
 
 #include "mf.cuh"
 
 namespace tmg {
 
-int64_t g_kernel_launches = 0;
+thread_local int64_t g_kernel_launches = 0;
+thread_local cudaStream_t g_stream = nullptr;
 
 template <typename T>
 __device__ __forceinline__ T dev_div(T a, typename real_of<T>::type d) { return a / d; }
@@ -295,6 +297,7 @@ __global__ void __launch_bounds__(128) k_inv_small(const int32_t* __restrict__ i
     const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
     const int b0 = b * NB;
     const int nbb = min(NB, w - b0);             // <= 32 by construction of the item list
+    if (nbb < 2 || nbb > 32) return;             // guard: this kernel's shared tiles hold 32 rows
     T* Fs = L + p * lstride + S.loff[s];
     for (int k = 0; k < nbb; k++)
         if (lane > k && lane < nbb) Lb[wi][lane][k] = Fs[(int64_t)(b0 + k) * m + b0 + lane];
@@ -322,6 +325,7 @@ __global__ void __launch_bounds__(256) k_inv_large(const int32_t* __restrict__ i
     const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
     const int b0 = b * NB;
     const int nbb = min(NB, w - b0);
+    if (nbb <= 0) return;
     T* Fs = L + p * lstride + S.loff[s];
     for (int q = threadIdx.x; q < NB * NB; q += blockDim.x) {
         const int i = q % NB, k = q / NB;
@@ -795,11 +799,14 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
         }
     }
     u_entries = std::max<int64_t>(ff.peak, 1);
+    alloc_stream = g_stream;
     auto put = [&](auto*& dptr, const auto& vec) {
         using E = typename std::decay<decltype(vec[0])>::type;
         const size_t b = std::max<size_t>(1, vec.size()) * sizeof(E);
-        TMG_CUDA(cudaMalloc((void**)&dptr, b));
-        if (!vec.empty()) TMG_CUDA(cudaMemcpy(dptr, vec.data(), vec.size() * sizeof(E), cudaMemcpyHostToDevice));
+        TMG_CUDA(cudaMallocAsync((void**)&dptr, b, alloc_stream));
+        if (!vec.empty())
+            TMG_CUDA(cudaMemcpyAsync(dptr, vec.data(), vec.size() * sizeof(E), cudaMemcpyHostToDevice, alloc_stream));
+        TMG_CUDA(cudaStreamSynchronize(alloc_stream));   // the host vectors are temporaries
         bytes += b;
     };
     put(sn_first, S.sn_first); put(sn_rows, S.sn_rows); put(rel, S.rel); put(child_ptr, S.child_ptr);
@@ -906,6 +913,7 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
     std::vector<int32_t> si;
     for (int pl = 0; pl < 2; pl++) {
         SolvePlan& P = plans[pl];
+        P = SolvePlan{};                     // a re-analysis starts from empty lists and counts
         const int nb = pl == 0 ? 64 : 128;
         P.nb = nb;
         P.levels.assign(nlev, SolveLevel{});
@@ -975,7 +983,7 @@ void DevSymbolic::release() {
     for (void* p : {(void*)sn_first, (void*)sn_rows, (void*)rel, (void*)child_ptr, (void*)child_list,
                     (void*)sn_row_ptr, (void*)loff, (void*)uoff, (void*)rel_ptr, (void*)perm, (void*)level_sn,
                     (void*)items, (void*)sitems, (void*)dest, (void*)conj})
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, alloc_stream);
     sn_first = sn_rows = rel = child_ptr = child_list = perm = level_sn = items = sitems = nullptr;
     sn_row_ptr = loff = uoff = rel_ptr = dest = nullptr;
     conj = nullptr;
@@ -995,12 +1003,11 @@ void mf_invert_diag(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt);
 
 template <typename T>
 void mf_factor(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, int* status) {
-    static bool attr_set = false;
     const size_t upd_smem = 2 * MF_NB * MF_TILE * sizeof(T);
-    if (!attr_set) {
+    static std::once_flag attr_once;
+    std::call_once(attr_once, [&]() {
         TMG_CUDA(cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem));
-        attr_set = true;
-    }
+    });
     const SnDev sn = S.sn();
     const unsigned B = bt.B;
     for (const auto& stp : S.steps) {
@@ -1047,11 +1054,10 @@ void mf_invert_diag(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt) {
                    S.sitems + P.inv_small_off, P.inv_small_cnt, sn, bt.L, bt.lstride);
     if (P.inv_large_cnt) {
         const size_t smem = (size_t)NB * (NB + 1) * sizeof(T);
-        static bool attr_set = false;
-        if (!attr_set) {
+        static std::once_flag attr_once;
+        std::call_once(attr_once, [&]() {
             TMG_CUDA(cudaFuncSetAttribute(k_inv_large<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            attr_set = true;
-        }
+        });
         TMG_LAUNCH((k_inv_large<T, NB>), dim3(P.inv_large_cnt, B), 256, smem, st, S.sitems + P.inv_large_off, sn, bt.L,
                    bt.lstride);
     }
@@ -1067,14 +1073,13 @@ void mf_solve(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, T* x, T
     const SolveArgs A{bt.lstride, (int64_t)S.n, S.t_entries, skip};
     const unsigned B = bt.B;
     const size_t xs = (size_t)64 * XS_LD * sizeof(T);
-    static bool attr_set = false;
-    if (!attr_set) {
+    static std::once_flag attr_once;
+    std::call_once(attr_once, [&]() {
         TMG_CUDA(cudaFuncSetAttribute(k_fwd_gather<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
         TMG_CUDA(cudaFuncSetAttribute(k_fwd_tri<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
         TMG_CUDA(cudaFuncSetAttribute(k_bwd_rect<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
         TMG_CUDA(cudaFuncSetAttribute(k_bwd_tri<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
-        attr_set = true;
-    }
+    });
     for (int l = 0; l < nlev; l++) {
         const int cnt = S.level_ptr[l + 1] - S.level_ptr[l];
         if (!cnt) continue;

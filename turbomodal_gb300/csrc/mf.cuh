@@ -57,6 +57,7 @@ struct DevSymbolic {
     int64_t nlower = 0;
     double flops = 0.0;        // real flops of one complex factorisation (4 sum c_j^2)
     size_t bytes = 0;
+    cudaStream_t alloc_stream = nullptr;   // stream the device arrays were allocated on
     struct Step {
         int32_t level = 0, kb = 0;
         int64_t uzero_off = 0;                 // (s) items whose update blocks are zeroed

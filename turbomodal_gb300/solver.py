@@ -175,6 +175,14 @@ class CyclicSymmetrySolver:
         A.has_sorted_indices = True
         return A
 
+    def set_memory_budget(self, nbytes: int) -> None:
+        """Device-memory budget of later solves (tmg_set_memory_budget)."""
+        self.ctx.check(self.ctx.L.tmg_set_memory_budget(self.ctx.h, int(nbytes)), "tmg_set_memory_budget")
+
+    def close(self) -> None:
+        """Release the device context and its memory now."""
+        self.ctx.close()
+
     def symbolic_stats(self, kind: int = 0) -> dict:
         out = np.zeros(10)
         self.ctx.check(self.ctx.L.tmg_symbolic_stats(self.ctx.h, kind, _lib.ptr(out, C.c_double)),
