@@ -1,0 +1,54 @@
+"""The multi-rank bench path on CPU: two gloo ranks shard the speeds without overlap and
+combine their timings (max) and eigenpair counts (sum) as bench.py does for N GPUs."""
+
+import os
+import socket
+
+import numpy as np
+import pytest
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _rank(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    import bench
+
+    ws, r, local, pg = bench.dist_setup()
+    mine = bench.shard_speeds(bench.RPMS, r, ws)
+    t = bench.max_over_ranks(pg, 1.5 + r)
+    n = bench.sum_over_ranks(pg, float(len(mine)))
+    bench.barrier(pg)
+    out.put((r, ws, [float(x) for x in mine], t, n))
+    pg.destroy_process_group()
+
+
+def test_two_ranks_shard_and_reduce():
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    ps = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in ps)
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    import bench
+
+    all_speeds = sorted(res[0][2] + res[1][2])
+    assert all_speeds == sorted(float(x) for x in bench.RPMS)
+    assert not set(res[0][2]) & set(res[1][2])
+    assert all(r[1] == 2 for r in res)
+    assert all(r[3] == 2.5 for r in res)                       # max over ranks
+    assert all(r[4] == float(len(bench.RPMS)) for r in res)   # sum over ranks
