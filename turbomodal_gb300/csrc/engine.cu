@@ -1062,9 +1062,6 @@ __global__ void k_ir_update(int64_t n, T* __restrict__ x, const T* __restrict__ 
     x[p * n + i] += d[p * n + i];
 }
 
-template <typename T>
-__global__ void k_count_nonpos_dummy() {}
-
 // ---- shift-invert operator of a batch ----------------------------------------------------
 template <typename Tv, typename Tf>
 struct ShiftInvertB {

@@ -563,10 +563,12 @@ __global__ void __launch_bounds__(256) k_fwd_rect(const int32_t* __restrict__ it
 // block then applies X^H
 template <typename T>
 __global__ void __launch_bounds__(256) k_bwd_rect(const int32_t* __restrict__ items, SnDev S, SolveArgs A,
-                                                  const T* __restrict__ L, T* __restrict__ x, T* __restrict__ tbuf) {
+                                                  const T* __restrict__ L, T* __restrict__ x, T* __restrict__ tbuf,
+                                                  int chunk) {
+    // dynamic shared memory: `chunk` gathered solution entries, then the staged inverse block
     extern __shared__ unsigned char sv_smem[];
-    T* Xs = reinterpret_cast<T*>(sv_smem);
-    __shared__ T xs[SV_CH];
+    T* xs = reinterpret_cast<T*>(sv_smem);
+    T* Xs = xs + chunk;
     __shared__ T zs[64], xo[64], red[256];
     pdl_trigger();
     const int64_t p = blockIdx.y;
@@ -591,8 +593,8 @@ __global__ void __launch_bounds__(256) k_bwd_rect(const int32_t* __restrict__ it
     T acc[8];
 #pragma unroll
     for (int c = 0; c < 8; c++) acc[c] = zero_of<T>();
-    for (int64_t q0 = w; q0 < m; q0 += SV_CH) {
-        const int len = (int)(m - q0 < SV_CH ? m - q0 : SV_CH);
+    for (int64_t q0 = w; q0 < m; q0 += chunk) {
+        const int len = (int)(m - q0 < chunk ? m - q0 : chunk);
         __syncthreads();
         for (int q = threadIdx.x; q < len; q += blockDim.x) xs[q] = x[rows[q0 + q]];
         __syncthreads();
@@ -911,10 +913,10 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
     put(items, it);
     // triangular-solve schedules (diagonal-block widths 64 and 128)
     std::vector<int32_t> si;
-    for (int pl = 0; pl < 2; pl++) {
-        SolvePlan& P = plans[pl];
+    {
+        SolvePlan& P = plan64;
         P = SolvePlan{};                     // a re-analysis starts from empty lists and counts
-        const int nb = pl == 0 ? 64 : 128;
+        const int nb = 64;
         P.nb = nb;
         P.levels.assign(nlev, SolveLevel{});
         for (int l = 0; l < nlev; l++) {
@@ -925,6 +927,12 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
                 maxw = std::max(maxw, S.sn_first[s + 1] - S.sn_first[s]);
             }
             const int nbk = (maxw + nb - 1) / nb;
+            L.maxw = maxw;
+            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                const int s = S.level_sn[q];
+                L.maxu = std::max<int64_t>(L.maxu, (S.sn_row_ptr[s + 1] - S.sn_row_ptr[s]) -
+                                                       (S.sn_first[s + 1] - S.sn_first[s]));
+            }
             L.ftri_off.assign(std::max(nbk, 1), 0);
             L.ftri_cnt.assign(std::max(nbk, 1), 0);
             L.btri_off.assign(std::max(nbk, 1), 0);
@@ -1045,7 +1053,7 @@ void mf_factor(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, int* s
 template <typename T>
 void mf_invert_diag(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt) {
     constexpr int NB = sv_nb<T>();
-    const auto& P = S.plan(NB);
+    const auto& P = S.plan64;
     const SnDev sn = S.sn();
     const unsigned B = bt.B;
     if (P.inv_small_cnt)
@@ -1067,7 +1075,7 @@ void mf_invert_diag(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt) {
 template <typename T>
 void mf_solve(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, T* x, T* tbuf, const int* skip) {
     static_assert(sv_nb<T>() == 64, "the solve kernels work on 64-wide diagonal blocks");
-    const auto& P = S.plan(64);
+    const auto& P = S.plan64;
     const int nlev = (int)S.level_ptr.size() - 1;
     const SnDev sn = S.sn();
     const SolveArgs A{bt.lstride, (int64_t)S.n, S.t_entries, skip};
@@ -1077,14 +1085,24 @@ void mf_solve(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, T* x, T
     std::call_once(attr_once, [&]() {
         TMG_CUDA(cudaFuncSetAttribute(k_fwd_gather<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
         TMG_CUDA(cudaFuncSetAttribute(k_fwd_tri<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
-        TMG_CUDA(cudaFuncSetAttribute(k_bwd_rect<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
+        TMG_CUDA(cudaFuncSetAttribute(k_bwd_rect<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(xs + SV_CH * sizeof(T))));
         TMG_CUDA(cudaFuncSetAttribute(k_bwd_tri<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
     });
+    // the levels near the leaves hold narrow fronts: their staged blocks are sized to the
+    // level's widest front (and the gathered rows to its largest rectangle), so more CTAs fit
+    auto xs_of = [&](const DevSymbolic::SolveLevel& L) {
+        return (size_t)std::min(64, std::max(1, L.maxw)) * XS_LD * sizeof(T);
+    };
+    auto chunk_of = [&](const DevSymbolic::SolveLevel& L) {
+        return (int)std::max<int64_t>(1, std::min<int64_t>(SV_CH, L.maxu));
+    };
     for (int l = 0; l < nlev; l++) {
         const int cnt = S.level_ptr[l + 1] - S.level_ptr[l];
         if (!cnt) continue;
         const auto& L = P.levels[l];
-        TMG_LAUNCH_PDL(k_fwd_gather<T>, dim3(cnt, B), 256, xs, st, S.level_sn + S.level_ptr[l], sn, A, bt.L, x, tbuf);
+        TMG_LAUNCH_PDL(k_fwd_gather<T>, dim3(cnt, B), 256, xs_of(L), st, S.level_sn + S.level_ptr[l], sn, A, bt.L, x,
+                       tbuf);
         for (size_t b = 0; b < L.ftri_cnt.size(); b++)
             if (L.ftri_cnt[b])
                 TMG_LAUNCH_PDL(k_fwd_tri<T>, dim3(L.ftri_cnt[b], B), 256, xs, st, S.sitems + L.ftri_off[b], (int)b, sn, A,
@@ -1095,7 +1113,8 @@ void mf_solve(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, T* x, T
     for (int l = nlev - 1; l >= 0; l--) {
         const auto& L = P.levels[l];
         if (L.brect_cnt)
-            TMG_LAUNCH_PDL(k_bwd_rect<T>, dim3(L.brect_cnt, B), 256, xs, st, S.sitems + L.brect_off, sn, A, bt.L, x, tbuf);
+            TMG_LAUNCH_PDL(k_bwd_rect<T>, dim3(L.brect_cnt, B), 256, xs_of(L) + chunk_of(L) * sizeof(T), st,
+                           S.sitems + L.brect_off, sn, A, bt.L, x, tbuf, chunk_of(L));
         for (int b = (int)L.btri_cnt.size() - 1; b >= 1; b--)
             if (L.btri_cnt[b])
                 TMG_LAUNCH_PDL(k_bwd_tri<T>, dim3(L.btri_cnt[b], B), 256, xs, st, S.sitems + L.btri_off[b], b, sn, A, bt.L,

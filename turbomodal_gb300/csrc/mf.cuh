@@ -80,6 +80,8 @@ struct DevSymbolic {
         std::vector<int32_t> ftri_cnt, btri_cnt;
         int64_t frect_off = 0, brect_off = 0;
         int32_t frect_cnt = 0, brect_cnt = 0;
+        int32_t maxw = 0;                          // widest front of the level
+        int64_t maxu = 0;                          // most rows below a triangle (m - w)
     };
     struct SolvePlan {
         int nb = 0;
@@ -87,8 +89,7 @@ struct DevSymbolic {
         int64_t inv_small_off = 0, inv_large_off = 0;   // items (s, b): diagonal blocks to invert
         int32_t inv_small_cnt = 0, inv_large_cnt = 0;   // small: width <= 32
     };
-    SolvePlan plans[2];        // nb = 64, nb = 128
-    const SolvePlan& plan(int nb) const { return plans[nb == 64 ? 0 : 1]; }
+    SolvePlan plan64;          // the solve schedule for 64-wide diagonal blocks
     std::vector<int32_t> level_ptr;
     SnDev sn() const {
         return SnDev{sn_first, sn_row_ptr, sn_rows, loff, uoff, child_ptr, child_list, rel_ptr, rel};
