@@ -1,0 +1,225 @@
+// Host check of the triangular-solve schedule (tests/test_solve_schedule.py): builds the
+// supernodal analysis and the solve plan with the library's own host code (sym.cpp), replays
+// every launch item with the index arithmetic of the device kernels (mf.cu: k_inv_*,
+// k_fwd_gather, k_fwd_tri, k_fwd_rect, k_bwd_rect, k_bwd_tri) with bounds checks, and compares
+// the result with a plain column-by-column supernodal solve on the same random unit-lower L and
+// positive D.  Prints "max_rel_err=<e> bounds_errors=<k> launches=<n>".
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+#include <vector>
+
+#include "sym.hpp"
+
+using namespace tmg;
+
+static long nerr = 0;
+
+int main(int argc, char** argv) {
+    if (argc < 2) return 2;
+    FILE* f = std::fopen(argv[1], "rb");
+    if (!f) return 2;
+    int64_t hdr[2];
+    if (std::fread(hdr, 8, 2, f) != 2) return 2;
+    Pattern P;
+    P.nrows = P.ncols = (int32_t)hdr[0];
+    P.p.resize(hdr[0] + 1);
+    P.i.resize(hdr[1]);
+    if (std::fread(P.p.data(), 8, hdr[0] + 1, f) != (size_t)hdr[0] + 1) return 2;
+    if (std::fread(P.i.data(), 4, hdr[1], f) != (size_t)hdr[1]) return 2;
+    std::fclose(f);
+    const int NB = 64, RR = 64, CH = 2048;
+    const Symbolic S = analyze(P, 0.0, 0);
+    std::vector<int32_t> items;
+    const SolvePlan plan = build_solve_plan(S, NB, RR, items);
+    const int ns = S.ns, n = S.n;
+    auto W = [&](int s) { return S.sn_first[s + 1] - S.sn_first[s]; };
+    auto H = [&](int s) { return (int64_t)(S.sn_row_ptr[s + 1] - S.sn_row_ptr[s]); };
+    std::vector<int64_t> lo(ns + 1, 0);
+    for (int s = 0; s < ns; s++) lo[s + 1] = lo[s] + H(s) * W(s);
+    std::vector<double> L(lo[ns]), L0;
+    std::mt19937 g(7);
+    std::uniform_real_distribution<double> U(-0.3, 0.3);
+    for (int s = 0; s < ns; s++)
+        for (int j = 0; j < W(s); j++)
+            for (int64_t r = 0; r < H(s); r++)
+                L[lo[s] + j * H(s) + r] = r == j ? 1.0 + std::fabs(U(g)) : (r > j ? U(g) / std::sqrt((double)H(s)) : 1e300);
+    L0 = L;
+    std::vector<double> b(n);
+    for (auto& v : b) v = U(g);
+    // reference: L y = b, x = D^-1 y, L^T x = x (supernode order = etree postorder)
+    std::vector<double> xr(b);
+    for (int s = 0; s < ns; s++) {
+        const int32_t* rows = &S.sn_rows[S.sn_row_ptr[s]];
+        for (int j = 0; j < W(s); j++)
+            for (int64_t r = j + 1; r < H(s); r++) xr[rows[r]] -= L0[lo[s] + j * H(s) + r] * xr[S.sn_first[s] + j];
+    }
+    for (int s = 0; s < ns; s++)
+        for (int j = 0; j < W(s); j++) xr[S.sn_first[s] + j] /= L0[lo[s] + j * H(s) + j];
+    for (int s = ns - 1; s >= 0; s--) {
+        const int32_t* rows = &S.sn_rows[S.sn_row_ptr[s]];
+        for (int j = W(s) - 1; j >= 0; j--) {
+            double a = xr[S.sn_first[s] + j];
+            for (int64_t r = j + 1; r < H(s); r++) a -= L0[lo[s] + j * H(s) + r] * xr[rows[r]];
+            xr[S.sn_first[s] + j] = a;
+        }
+    }
+    // bounds-checked accessors of the kernels' address arithmetic
+    auto Lat = [&](int s, int64_t idx) -> double& {
+        if (!(idx >= 0 && idx < H(s) * W(s))) nerr++;
+        return L[lo[s] + std::max<int64_t>(0, std::min<int64_t>(idx, H(s) * W(s) - 1))];
+    };
+    std::vector<double> t(S.sn_row_ptr[ns], 0.0), x(b);
+    auto Tat = [&](int s, int64_t r) -> double& {
+        if (!(r >= 0 && r < H(s))) nerr++;
+        return t[S.sn_row_ptr[s] + std::max<int64_t>(0, std::min<int64_t>(r, H(s) - 1))];
+    };
+    auto Xat = [&](int64_t i) -> double& {
+        if (!(i >= 0 && i < n)) nerr++;
+        return x[std::max<int64_t>(0, std::min<int64_t>(i, n - 1))];
+    };
+    auto item = [&](int64_t off, int k, int c) { return items[off + 2 * k + c]; };
+    long launches = 0;
+    // k_inv_small / k_inv_large: unit-lower inverse of every listed diagonal block
+    for (int pass = 0; pass < 2; pass++) {
+        const int64_t off = pass == 0 ? plan.inv_small_off : plan.inv_large_off;
+        const int cnt = pass == 0 ? plan.inv_small_cnt : plan.inv_large_cnt;
+        launches++;
+        for (int it = 0; it < cnt; it++) {
+            const int s = item(off, it, 0), bb = item(off, it, 1);
+            const int b0 = bb * NB, nbb = std::min(NB, W(s) - b0);
+            if (pass == 0 && (nbb < 2 || nbb > 32)) nerr++;
+            std::vector<double> Lb(64 * 64, 0.0);
+            for (int k = 0; k < nbb; k++)
+                for (int i = k + 1; i < nbb; i++) Lb[i * 64 + k] = Lat(s, (int64_t)(b0 + k) * H(s) + b0 + i);
+            for (int j = 0; j < nbb - 1; j++) {
+                std::vector<double> v(nbb, 0.0);
+                v[j] = 1.0;
+                for (int k = j; k < nbb - 1; k++)
+                    for (int i = k + 1; i < nbb; i++) v[i] -= Lb[i * 64 + k] * v[k];
+                for (int i = j + 1; i < nbb; i++) Lat(s, (int64_t)(b0 + j) * H(s) + b0 + i) = v[i];
+            }
+        }
+    }
+    const int nlev = (int)plan.levels.size();
+    auto applyX = [&](int s, int c0, int nbk, const std::vector<double>& u, std::vector<double>& v) {
+        for (int i = 0; i < nbk; i++) {
+            double a = u[i];
+            for (int k = 0; k < i; k++) a += Lat(s, (int64_t)(c0 + k) * H(s) + c0 + i) * u[k];
+            v[i] = a;
+        }
+    };
+    auto applyXt = [&](int s, int c0, int nbk, const std::vector<double>& u, std::vector<double>& v) {
+        for (int i = 0; i < nbk; i++) {
+            double a = u[i];
+            for (int k = i + 1; k < nbk; k++) a += Lat(s, (int64_t)(c0 + i) * H(s) + c0 + k) * u[k];
+            v[i] = a;
+        }
+    };
+    // forward sweep
+    for (int l = 0; l < nlev; l++) {
+        const SolveLevel& Lv = plan.levels[l];
+        launches++;
+        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {      // k_fwd_gather
+            const int s = S.level_sn[q], fs = S.sn_first[s];
+            for (int64_t r = 0; r < H(s); r++) Tat(s, r) = r < W(s) ? Xat(fs + r) : 0.0;
+            for (int c = S.child_ptr[s]; c < S.child_ptr[s + 1]; c++) {
+                const int ch = S.child_list[c];
+                for (int64_t a = 0; a < H(ch) - W(ch); a++) Tat(s, S.rel[S.rel_ptr[ch] + a]) += Tat(ch, W(ch) + a);
+            }
+            const int nb0 = std::min(NB, W(s));
+            std::vector<double> u(nb0), v(nb0);
+            for (int i = 0; i < nb0; i++) u[i] = Tat(s, i);
+            applyX(s, 0, nb0, u, v);
+            for (int i = 0; i < nb0; i++) { Tat(s, i) = v[i]; Xat(fs + i) = v[i] / Lat(s, (int64_t)i * H(s) + i); }
+        }
+        for (size_t bb = 0; bb < Lv.ftri_cnt.size(); bb++) {             // k_fwd_tri
+            if (!Lv.ftri_cnt[bb]) continue;
+            launches++;
+            for (int it = 0; it < Lv.ftri_cnt[bb]; it++) {
+                const int s = item(Lv.ftri_off[bb], it, 0), r0 = item(Lv.ftri_off[bb], it, 1);
+                const int fs = S.sn_first[s], b0 = (int)bb * NB, rend = std::min(r0 + NB, W(s));
+                std::vector<double> ys(NB), tn(NB, 0.0), yn(NB, 0.0);
+                for (int j = 0; j < NB; j++) ys[j] = Tat(s, b0 + j);
+                for (int r = r0; r < rend; r++) {
+                    double a = 0.0;
+                    for (int j = 0; j < NB; j++) a += Lat(s, (int64_t)(b0 + j) * H(s) + r) * ys[j];
+                    Tat(s, r) -= a;
+                    tn[r - r0] = Tat(s, r);
+                }
+                if (r0 == b0 + NB) {
+                    applyX(s, r0, rend - r0, tn, yn);
+                    for (int i = 0; i < rend - r0; i++) {
+                        Tat(s, r0 + i) = yn[i];
+                        Xat(fs + r0 + i) = yn[i] / Lat(s, (int64_t)(r0 + i) * H(s) + r0 + i);
+                    }
+                }
+            }
+        }
+        if (Lv.frect_cnt) launches++;
+        for (int it = 0; it < Lv.frect_cnt; it++) {                        // k_fwd_rect
+            const int s = item(Lv.frect_off, it, 0), r0 = item(Lv.frect_off, it, 1);
+            for (int64_t r = r0; r < std::min<int64_t>(r0 + RR, H(s)); r++) {
+                double a = 0.0;
+                for (int j = 0; j < W(s); j++) a += Lat(s, (int64_t)j * H(s) + r) * Tat(s, j);
+                Tat(s, r) -= a;
+            }
+        }
+    }
+    // backward sweep
+    for (int l = nlev - 1; l >= 0; l--) {
+        const SolveLevel& Lv = plan.levels[l];
+        if (Lv.brect_cnt) launches++;
+        for (int it = 0; it < Lv.brect_cnt; it++) {                        // k_bwd_rect
+            const int s = item(Lv.brect_off, it, 0), c0 = item(Lv.brect_off, it, 1);
+            const int fs = S.sn_first[s], nc = std::min(NB, W(s) - c0);
+            const int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(CH, Lv.maxu));
+            const int32_t* rows = &S.sn_rows[S.sn_row_ptr[s]];
+            std::vector<double> zs(NB, 0.0), xo(NB, 0.0);
+            for (int64_t q0 = W(s); q0 < H(s); q0 += chunk) {
+                const int len = (int)std::min<int64_t>(chunk, H(s) - q0);
+                if (len > chunk) nerr++;
+                for (int jj = 0; jj < nc; jj++) {
+                    double a = 0.0;
+                    for (int q = 0; q < len; q++) a += Lat(s, (int64_t)(c0 + jj) * H(s) + q0 + q) * Xat(rows[q0 + q]);
+                    zs[jj] += a;
+                }
+            }
+            for (int jj = 0; jj < nc; jj++) { const double z = Xat(fs + c0 + jj) - zs[jj]; Tat(s, c0 + jj) = z; zs[jj] = z; }
+            if (c0 + nc == W(s)) {
+                if (nc > std::min(64, std::max(1, Lv.maxw))) nerr++;     // staged block fits the level's size
+                applyXt(s, c0, nc, zs, xo);
+                for (int i = 0; i < nc; i++) Xat(fs + c0 + i) = xo[i];
+            }
+        }
+        for (int bb = (int)Lv.btri_cnt.size() - 1; bb >= 1; bb--) {      // k_bwd_tri
+            if (!Lv.btri_cnt[bb]) continue;
+            launches++;
+            for (int it = 0; it < Lv.btri_cnt[bb]; it++) {
+                const int s = item(Lv.btri_off[bb], it, 0), c0 = item(Lv.btri_off[bb], it, 1);
+                const int fs = S.sn_first[s], b0 = bb * NB, nbb = std::min(NB, W(s) - b0);
+                std::vector<double> xb(nbb), zs(NB), xo(NB);
+                for (int r = 0; r < nbb; r++) xb[r] = Xat(fs + b0 + r);
+                for (int jj = 0; jj < NB; jj++) {
+                    double a = 0.0;
+                    for (int r = 0; r < nbb; r++) a += Lat(s, (int64_t)(c0 + jj) * H(s) + b0 + r) * xb[r];
+                    const double z = Tat(s, c0 + jj) - a;
+                    Tat(s, c0 + jj) = z;
+                    zs[jj] = z;
+                }
+                if (c0 + NB == b0) {
+                    applyXt(s, c0, NB, zs, xo);
+                    for (int i = 0; i < NB; i++) Xat(fs + c0 + i) = xo[i];
+                }
+            }
+        }
+    }
+    double err = 0.0, sc = 0.0;
+    for (int i = 0; i < n; i++) {
+        err = std::max(err, std::fabs(x[i] - xr[i]));
+        sc = std::max(sc, std::fabs(xr[i]));
+    }
+    std::printf("max_rel_err=%.3e bounds_errors=%ld launches=%ld supernodes=%d\n", err / sc, nerr, launches, ns);
+    return 0;
+}

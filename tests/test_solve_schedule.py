@@ -1,0 +1,55 @@
+"""The triangular-solve schedule on the host: the library's supernodal analysis and solve plan
+(turbomodal_gb300/csrc/sym.cpp) replayed with the device kernels' index arithmetic
+(tests/native/solve_schedule_check.cpp) must stay inside every panel, front vector and solution
+vector and reproduce a plain supernodal solve to roundoff (1e-12 relative)."""
+
+import os
+import subprocess
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from conftest import ROOT
+
+CSRC = os.path.join(ROOT, "turbomodal_gb300", "csrc")
+
+
+@pytest.fixture(scope="module")
+def checker(tmp_path_factory):
+    d = tmp_path_factory.mktemp("sched")
+    exe = str(d / "solve_schedule_check")
+    cmd = ["g++", "-O2", "-std=c++17", "-I", CSRC, os.path.join(ROOT, "tests", "native", "solve_schedule_check.cpp"),
+           os.path.join(CSRC, "sym.cpp"), "-o", exe]
+    subprocess.run(cmd, check=True)
+    return exe, d
+
+
+def operator_pattern(oracle, mesh, rpm, path):
+    from turbomodal_gb300.meshgen import TITANIUM
+
+    om = oracle.OracleModel(mesh, TITANIUM)
+    om.prepare(rpm)
+    K, M = om.matrix("Kk", k=1), om.matrix("Mk", k=1)
+    P = sp.tril(sp.csc_matrix((abs(K) + abs(M)) > 0, dtype=float)).tocsc()
+    P.sort_indices()
+    with open(path, "wb") as f:
+        np.array([P.shape[0], P.nnz], np.int64).tofile(f)
+        P.indptr.astype(np.int64).tofile(f)
+        P.indices.astype(np.int32).tofile(f)
+
+
+@pytest.mark.parametrize("case", ["config0", "bladed"])
+def test_solve_schedule_matches_plain_solve(checker, oracle, case):
+    from turbomodal_gb300.meshgen import config_mesh, sector_mesh
+
+    exe, d = checker
+    mesh = config_mesh(0) if case == "config0" else sector_mesh(
+        12, 8, 3, seed=4, blade=dict(ns=10, nc=4, nb=2, span=0.12, chord=0.05, thick=0.004, twist_deg=30.0))
+    pat = str(d / f"{case}.pat")
+    operator_pattern(oracle, mesh, 3000.0, pat)
+    out = subprocess.run([exe, pat], check=True, capture_output=True, text=True).stdout
+    vals = dict(kv.split("=") for kv in out.split())
+    assert int(vals["bounds_errors"]) == 0
+    assert float(vals["max_rel_err"]) <= 1e-12
+    assert int(vals["launches"]) > 0

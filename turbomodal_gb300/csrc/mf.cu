@@ -911,79 +911,9 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
         }
     }
     put(items, it);
-    // triangular-solve schedules (diagonal-block widths 64 and 128)
+    // triangular-solve schedule (64-wide diagonal blocks)
     std::vector<int32_t> si;
-    {
-        SolvePlan& P = plan64;
-        P = SolvePlan{};                     // a re-analysis starts from empty lists and counts
-        const int nb = 64;
-        P.nb = nb;
-        P.levels.assign(nlev, SolveLevel{});
-        for (int l = 0; l < nlev; l++) {
-            SolveLevel& L = P.levels[l];
-            int maxw = 0;
-            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-                const int s = S.level_sn[q];
-                maxw = std::max(maxw, S.sn_first[s + 1] - S.sn_first[s]);
-            }
-            const int nbk = (maxw + nb - 1) / nb;
-            L.maxw = maxw;
-            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-                const int s = S.level_sn[q];
-                L.maxu = std::max<int64_t>(L.maxu, (S.sn_row_ptr[s + 1] - S.sn_row_ptr[s]) -
-                                                       (S.sn_first[s + 1] - S.sn_first[s]));
-            }
-            L.ftri_off.assign(std::max(nbk, 1), 0);
-            L.ftri_cnt.assign(std::max(nbk, 1), 0);
-            L.btri_off.assign(std::max(nbk, 1), 0);
-            L.btri_cnt.assign(std::max(nbk, 1), 0);
-            for (int b = 0; b + 1 < nbk; b++) {          // forward triangle launches
-                L.ftri_off[b] = (int64_t)si.size();
-                for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-                    const int s = S.level_sn[q];
-                    const int w = S.sn_first[s + 1] - S.sn_first[s];
-                    for (int r0 = (b + 1) * nb; r0 < w; r0 += nb) { si.push_back(s); si.push_back(r0); L.ftri_cnt[b]++; }
-                }
-            }
-            L.frect_off = (int64_t)si.size();
-            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-                const int s = S.level_sn[q];
-                const int w = S.sn_first[s + 1] - S.sn_first[s];
-                const int64_t m = S.sn_row_ptr[s + 1] - S.sn_row_ptr[s];
-                for (int64_t r0 = w; r0 < m; r0 += SV_RR) { si.push_back(s); si.push_back((int32_t)r0); L.frect_cnt++; }
-            }
-            L.brect_off = (int64_t)si.size();
-            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-                const int s = S.level_sn[q];
-                const int w = S.sn_first[s + 1] - S.sn_first[s];
-                for (int c0 = 0; c0 < w; c0 += nb) { si.push_back(s); si.push_back(c0); L.brect_cnt++; }
-            }
-            for (int b = 1; b < nbk; b++) {              // backward triangle launches
-                L.btri_off[b] = (int64_t)si.size();
-                for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-                    const int s = S.level_sn[q];
-                    const int w = S.sn_first[s + 1] - S.sn_first[s];
-                    if (w <= b * nb) continue;
-                    for (int c0 = 0; c0 < b * nb; c0 += nb) { si.push_back(s); si.push_back(c0); L.btri_cnt[b]++; }
-                }
-            }
-        }
-        // diagonal blocks to invert after the factorisation
-        P.inv_small_off = (int64_t)si.size();
-        for (int s = 0; s < ns; s++) {
-            const int w = S.sn_first[s + 1] - S.sn_first[s];
-            for (int b = 0; b * nb < w; b++)
-                if (std::min(nb, w - b * nb) <= 32 && std::min(nb, w - b * nb) > 1) {
-                    si.push_back(s); si.push_back(b); P.inv_small_cnt++;
-                }
-        }
-        P.inv_large_off = (int64_t)si.size();
-        for (int s = 0; s < ns; s++) {
-            const int w = S.sn_first[s + 1] - S.sn_first[s];
-            for (int b = 0; b * nb < w; b++)
-                if (std::min(nb, w - b * nb) > 32) { si.push_back(s); si.push_back(b); P.inv_large_cnt++; }
-        }
-    }
+    plan64 = build_solve_plan(S, 64, SV_RR, si);
     put(sitems, si);
 }
 

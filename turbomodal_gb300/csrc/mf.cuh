@@ -69,26 +69,8 @@ struct DevSymbolic {
         int32_t diag_cnt = 0, panel_cnt = 0, upd_cnt = 0, trail_cnt = 0;
     };
     std::vector<Step> steps;
-    // Triangular-solve schedule for one diagonal-block width nb, per tree level:
-    //   forward:  gather (level supernodes), triangle launches b = 0 .. (items (s, r0): rows
-    //             [r0, r0 + nb) of the triangle below block b), one rectangle launch
-    //             (items (s, r0): rows [r0, r0 + SV_RR) below the triangle);
-    //   backward: one rectangle launch (items (s, c0): columns [c0, c0 + nb)), triangle
-    //             launches b = last .. 1 (items (s, c0): columns [c0, c0 + nb) left of block b).
-    struct SolveLevel {
-        std::vector<int64_t> ftri_off, btri_off;   // index b
-        std::vector<int32_t> ftri_cnt, btri_cnt;
-        int64_t frect_off = 0, brect_off = 0;
-        int32_t frect_cnt = 0, brect_cnt = 0;
-        int32_t maxw = 0;                          // widest front of the level
-        int64_t maxu = 0;                          // most rows below a triangle (m - w)
-    };
-    struct SolvePlan {
-        int nb = 0;
-        std::vector<SolveLevel> levels;
-        int64_t inv_small_off = 0, inv_large_off = 0;   // items (s, b): diagonal blocks to invert
-        int32_t inv_small_cnt = 0, inv_large_cnt = 0;   // small: width <= 32
-    };
+    using SolveLevel = tmg::SolveLevel;
+    using SolvePlan = tmg::SolvePlan;
     SolvePlan plan64;          // the solve schedule for 64-wide diagonal blocks
     std::vector<int32_t> level_ptr;
     SnDev sn() const {

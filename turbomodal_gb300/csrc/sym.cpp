@@ -660,4 +660,65 @@ void scatter_map(const Symbolic& S, const Pattern& lower, std::vector<int64_t>& 
         }
 }
 
+SolvePlan build_solve_plan(const Symbolic& S, int nb, int rows_per_rect, std::vector<int32_t>& si) {
+    SolvePlan P;
+    P.nb = nb;
+    const int nlev = (int)S.level_ptr.size() - 1;
+    P.levels.assign(std::max(nlev, 0), SolveLevel{});
+    auto width = [&](int s) { return S.sn_first[s + 1] - S.sn_first[s]; };
+    auto height = [&](int s) { return S.sn_row_ptr[s + 1] - S.sn_row_ptr[s]; };
+    for (int l = 0; l < nlev; l++) {
+        SolveLevel& L = P.levels[l];
+        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+            const int s = S.level_sn[q];
+            L.maxw = std::max(L.maxw, width(s));
+            L.maxu = std::max<int64_t>(L.maxu, height(s) - width(s));
+        }
+        const int nbk = (L.maxw + nb - 1) / nb;
+        L.ftri_off.assign(std::max(nbk, 1), 0);
+        L.ftri_cnt.assign(std::max(nbk, 1), 0);
+        L.btri_off.assign(std::max(nbk, 1), 0);
+        L.btri_cnt.assign(std::max(nbk, 1), 0);
+        for (int b = 0; b + 1 < nbk; b++) {              // forward triangle launches
+            L.ftri_off[b] = (int64_t)si.size();
+            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                const int s = S.level_sn[q];
+                for (int r0 = (b + 1) * nb; r0 < width(s); r0 += nb) { si.push_back(s); si.push_back(r0); L.ftri_cnt[b]++; }
+            }
+        }
+        L.frect_off = (int64_t)si.size();
+        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+            const int s = S.level_sn[q];
+            for (int64_t r0 = width(s); r0 < height(s); r0 += rows_per_rect) {
+                si.push_back(s); si.push_back((int32_t)r0); L.frect_cnt++;
+            }
+        }
+        L.brect_off = (int64_t)si.size();
+        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+            const int s = S.level_sn[q];
+            for (int c0 = 0; c0 < width(s); c0 += nb) { si.push_back(s); si.push_back(c0); L.brect_cnt++; }
+        }
+        for (int b = 1; b < nbk; b++) {                  // backward triangle launches
+            L.btri_off[b] = (int64_t)si.size();
+            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                const int s = S.level_sn[q];
+                if (width(s) <= b * nb) continue;
+                for (int c0 = 0; c0 < b * nb; c0 += nb) { si.push_back(s); si.push_back(c0); L.btri_cnt[b]++; }
+            }
+        }
+    }
+    // diagonal blocks to invert after the factorisation
+    P.inv_small_off = (int64_t)si.size();
+    for (int s = 0; s < S.ns; s++)
+        for (int b = 0; b * nb < width(s); b++) {
+            const int nbb = std::min(nb, width(s) - b * nb);
+            if (nbb <= 32 && nbb > 1) { si.push_back(s); si.push_back(b); P.inv_small_cnt++; }
+        }
+    P.inv_large_off = (int64_t)si.size();
+    for (int s = 0; s < S.ns; s++)
+        for (int b = 0; b * nb < width(s); b++)
+            if (std::min(nb, width(s) - b * nb) > 32) { si.push_back(s); si.push_back(b); P.inv_large_cnt++; }
+    return P;
+}
+
 }  // namespace tmg

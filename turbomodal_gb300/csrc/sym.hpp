@@ -59,6 +59,30 @@ struct Symbolic {
 // explicit zeros (0 = fundamental supernodes only).
 Symbolic analyze(const Pattern& lower, double relax = 0.0, int32_t relax_max_width = 0);
 
+// Triangular-solve schedule for diagonal blocks of width nb, per tree level (host side; the
+// device kernels read the item lists).  Forward: gather (the level's supernodes), triangle
+// launches b = 0.. (items (s, r0): rows [r0, r0 + nb) of the triangle below block b), one
+// rectangle launch (items (s, r0): rows [r0, r0 + rows_per_rect) below the triangle).
+// Backward: one rectangle launch (items (s, c0): columns [c0, c0 + nb)), triangle launches
+// b = last .. 1 (items (s, c0): columns [c0, c0 + nb) left of block b).  Inverse lists: items
+// (s, b) of the diagonal blocks to invert after a factorisation (small: width <= 32).
+struct SolveLevel {
+    std::vector<int64_t> ftri_off, btri_off;   // index b
+    std::vector<int32_t> ftri_cnt, btri_cnt;
+    int64_t frect_off = 0, brect_off = 0;
+    int32_t frect_cnt = 0, brect_cnt = 0;
+    int32_t maxw = 0;                          // widest front of the level
+    int64_t maxu = 0;                          // most rows below a triangle (m - w)
+};
+struct SolvePlan {
+    int nb = 0;
+    std::vector<SolveLevel> levels;
+    int64_t inv_small_off = 0, inv_large_off = 0;
+    int32_t inv_small_cnt = 0, inv_large_cnt = 0;
+};
+// Builds the schedule of S; its items are appended to `items` (offsets index that array).
+SolvePlan build_solve_plan(const Symbolic& S, int nb, int rows_per_rect, std::vector<int32_t>& items);
+
 // Destination of every lower-triangle entry of `lower` (in its CSC order) inside the
 // front storage of `S`; conj flag set when the entry lands transposed.
 void scatter_map(const Symbolic& S, const Pattern& lower, std::vector<int64_t>& dest, std::vector<uint8_t>& conj);
