@@ -1,0 +1,61 @@
+"""Consumers of a result set (host side): stationary-frame conversion with the reference's own
+test cases (tests/test_cyclic.cpp:451-535), Campbell arrays and the CSV exports."""
+
+import numpy as np
+
+from turbomodal_gb300.solver import (ModalResult, campbell_data, compute_stationary_frame, export_campbell_csv,
+                                     export_zzenf_csv)
+
+
+def result(k, rpm, freqs, whirl=None):
+    f = np.asarray(freqs, dtype=float)
+    w = np.zeros(len(f), np.int32) if whirl is None else np.asarray(whirl, np.int32)
+    return ModalResult(k, rpm, f, np.zeros((6, len(f)), np.complex128), w)
+
+
+def test_fw_bw_split():
+    sf = compute_stationary_frame(result(3, 6000.0, [500.0, 1000.0]), 24)
+    np.testing.assert_allclose(sf.frequencies, [200.0, 700.0, 800.0, 1300.0], atol=0.1)
+    assert sf.whirl_direction.tolist() == [-1, -1, 1, 1]
+
+
+def test_no_split_at_k0_kN2_and_rest():
+    for k, rpm in ((0, 6000.0), (12, 6000.0), (5, 0.0)):
+        f = [100.0, 200.0, 300.0] if k == 0 else [500.0, 1000.0]
+        sf = compute_stationary_frame(result(k, rpm, f), 24)
+        np.testing.assert_allclose(sf.frequencies, f, atol=1e-10)
+        assert not sf.whirl_direction.any()
+
+
+def test_whirl_carrying_modes_move_per_mode():
+    # degenerate pairs carry +1/-1: each mode moves by whirl * k * Omega / 2 pi (300 Hz here)
+    sf = compute_stationary_frame(result(3, 6000.0, [500.0, 500.0], [1, -1]), 24)
+    np.testing.assert_allclose(sf.frequencies, [200.0, 800.0])
+    assert sf.whirl_direction.tolist() == [-1, 1]
+
+
+def test_campbell_arrays():
+    sweep = [[result(0, 0.0, [100.0, 200.0]), result(3, 0.0, [500.0])],
+             [result(0, 6000.0, [110.0, 210.0]), result(3, 6000.0, [500.0])]]
+    d = campbell_data(sweep, num_sectors=24)
+    assert d["frequencies"].shape == (2, 2, 4)
+    assert d["harmonic_index"].tolist() == [0, 3]
+    np.testing.assert_allclose(d["rpm"], [0.0, 6000.0])
+    np.testing.assert_allclose(d["frequencies"][1, 1, :2], [200.0, 800.0])
+    assert d["whirl_direction"][1, 1, :2].tolist() == [-1, 1]
+    np.testing.assert_allclose(d["frequencies"][1, 0, :2], [110.0, 210.0])
+    assert np.isnan(d["frequencies"][0, 0, 2:]).all()
+
+
+def test_csv_exports(tmp_path):
+    rows = [[result(3, 6000.0, [500.0, 1000.0])]]
+    p = tmp_path / "campbell.csv"
+    export_campbell_csv(str(p), rows, 24)
+    lines = p.read_text().splitlines()
+    assert lines[0] == "rpm,harmonic_index,mode_family,frequency_hz,whirl_direction"
+    assert lines[1] == "6000.000000,3,1,200.000000,-1"
+    assert len(lines) == 5
+    q = tmp_path / "zzenf.csv"
+    export_zzenf_csv(str(q), rows[0])
+    assert q.read_text().splitlines() == ["nodal_diameter,mode_family,frequency_hz,rpm", "3,1,500.000000,6000.000000",
+                                          "3,2,1000.000000,6000.000000"]

@@ -175,6 +175,16 @@ class CyclicSymmetrySolver:
         A.has_sorted_indices = True
         return A
 
+    def compute_stationary_frame(self, rotating_result, num_sectors: int | None = None) -> "StationaryFrameResult":
+        """Stationary-frame frequencies of one result (python_bindings.cpp:402)."""
+        return compute_stationary_frame(rotating_result, num_sectors or self.mesh.num_sectors)
+
+    def export_campbell_csv(self, filename: str, results) -> None:
+        export_campbell_csv(filename, results, self.mesh.num_sectors)
+
+    def export_zzenf_csv(self, filename: str, results_at_rpm) -> None:
+        export_zzenf_csv(filename, results_at_rpm)
+
     def set_memory_budget(self, nbytes: int) -> None:
         """Device-memory budget of later solves (tmg_set_memory_budget)."""
         self.ctx.check(self.ctx.L.tmg_set_memory_budget(self.ctx.h, int(nbytes)), "tmg_set_memory_budget")
@@ -268,3 +278,108 @@ def rpm_sweep(mesh: Mesh, material: Material, rpm_values, num_modes: int = 10, h
         masses = _modal_mass_from_M(M, res, mesh.num_sectors)
         out.append([EnrichedModalResult(_result=r, modal_mass_kg=m) for r, m in zip(res, masses)])
     return out
+
+
+# --- consumers of a result set (host side) ----------------------------------------------------
+@dataclass
+class StationaryFrameResult:
+    """Stationary-frame frequencies of one rotating-frame result (cyclic_solver.hpp)."""
+
+    frequencies: np.ndarray
+    whirl_direction: np.ndarray
+
+
+def compute_stationary_frame(result, num_sectors: int) -> StationaryFrameResult:
+    """Rotating-frame result -> stationary frame (src/cyclic_solver.cpp:374-454): modes that
+    carry a whirl direction at speed (k > 0) move by whirl * k * Omega / 2 pi; otherwise, for
+    0 < k < N/2 at speed, every mode splits into a forward (f + k Omega / 2 pi) and a backward
+    (|f - k Omega / 2 pi|) wave; k = 0, k = N/2 and rest stay standing (whirl 0)."""
+    k = int(result.harmonic_index)
+    omega = float(result.rpm) * 2.0 * np.pi / 60.0
+    f = np.asarray(result.frequencies, dtype=np.float64)
+    w = np.asarray(result.whirl_direction, dtype=np.int32)
+    kw = k * abs(omega) / (2.0 * np.pi)
+    if np.any(w != 0) and abs(omega) > 0.0 and k > 0:
+        sf = np.abs(f + w * kw)
+        order = np.argsort(sf, kind="stable")
+        return StationaryFrameResult(sf[order], w[order])
+    if abs(omega) > 0.0 and 0 < k < num_sectors // 2:
+        allf = np.empty(2 * len(f))
+        allw = np.empty(2 * len(f), dtype=np.int32)
+        allf[0::2], allf[1::2] = f + kw, np.abs(f - kw)
+        allw[0::2], allw[1::2] = 1, -1
+        order = np.argsort(allf, kind="stable")
+        return StationaryFrameResult(allf[order], allw[order])
+    return StationaryFrameResult(f.copy(), np.zeros(len(f), dtype=np.int32))
+
+
+def campbell_data(results, num_sectors: int = 0) -> dict:
+    """Campbell-diagram arrays from an rpm sweep (python/turbomodal/solver.py:631-744): 'rpm' (N,),
+    'frequencies' (N, H, M) stationary-frame Hz (NaN-padded), 'harmonic_index' (H,),
+    'whirl_direction' (N, H, M) with +1 forward, -1 backward, 0 standing; M = 2 x the most
+    modes of any result.  num_sectors = 0 infers N = 2 x the largest harmonic index."""
+    if not results:
+        return {"rpm": np.array([]), "frequencies": np.array([]), "harmonic_index": np.array([]),
+                "whirl_direction": np.array([])}
+    hs = np.array(sorted({r.harmonic_index for row in results for r in row}))
+    col = {h: i for i, h in enumerate(hs)}
+    if num_sectors <= 0:
+        num_sectors = 2 * (int(hs[-1]) if len(hs) else 0)
+    max_k = num_sectors // 2
+    n_modes = 2 * max((len(r.frequencies) for row in results for r in row), default=0)
+    rpm = np.zeros(len(results))
+    freqs = np.full((len(results), len(hs), n_modes), np.nan)
+    whirl = np.zeros((len(results), len(hs), n_modes), dtype=np.int32)
+    for i, row in enumerate(results):
+        if row:
+            rpm[i] = row[0].rpm
+        omega = rpm[i] * 2.0 * np.pi / 60.0
+        for r in row:
+            j = col.get(r.harmonic_index)
+            if j is None:
+                continue
+            k = r.harmonic_index
+            f = np.asarray(r.frequencies, dtype=np.float64)
+            w = np.asarray(r.whirl_direction, dtype=np.int32)
+            kw = k * abs(omega) / (2.0 * np.pi)
+            if np.any(w != 0) and abs(omega) > 0 and k > 0:
+                sf = np.abs(f + w * kw)
+                order = np.argsort(sf)
+                m = min(n_modes, len(f))
+                freqs[i, j, :m] = sf[order][:m]
+                whirl[i, j, :m] = w[order][:m]
+            elif abs(omega) > 0 and 0 < k < max_k:
+                allf = np.empty(2 * len(f))
+                allw = np.empty(2 * len(f), dtype=np.int32)
+                allf[0::2], allf[1::2] = f + kw, np.abs(f - kw)
+                allw[0::2], allw[1::2] = 1, -1
+                order = np.argsort(allf)
+                m = min(n_modes, 2 * len(f))
+                freqs[i, j, :m] = allf[order][:m]
+                whirl[i, j, :m] = allw[order][:m]
+            else:
+                m = min(n_modes, len(f))
+                freqs[i, j, :m] = f[:m]
+    return {"rpm": rpm, "frequencies": freqs, "harmonic_index": hs, "whirl_direction": whirl}
+
+
+def export_campbell_csv(filename: str, results, num_sectors: int) -> None:
+    """rpm,harmonic_index,mode_family,frequency_hz,whirl_direction with stationary-frame
+    frequencies, six decimals (src/cyclic_solver.cpp:1487-1506)."""
+    with open(filename, "w") as fh:
+        fh.write("rpm,harmonic_index,mode_family,frequency_hz,whirl_direction\n")
+        for row in results:
+            for r in row:
+                sf = compute_stationary_frame(r, num_sectors)
+                for m, (f, w) in enumerate(zip(sf.frequencies, sf.whirl_direction)):
+                    fh.write(f"{r.rpm:.6f},{r.harmonic_index},{m + 1},{f:.6f},{int(w)}\n")
+
+
+def export_zzenf_csv(filename: str, results_at_rpm) -> None:
+    """nodal_diameter,mode_family,frequency_hz,rpm for the results of one speed, six decimals
+    (src/cyclic_solver.cpp:1508-1523)."""
+    with open(filename, "w") as fh:
+        fh.write("nodal_diameter,mode_family,frequency_hz,rpm\n")
+        for r in results_at_rpm:
+            for m, f in enumerate(r.frequencies):
+                fh.write(f"{r.harmonic_index},{m + 1},{f:.6f},{r.rpm:.6f}\n")
