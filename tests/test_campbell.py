@@ -59,3 +59,21 @@ def test_csv_exports(tmp_path):
     export_zzenf_csv(str(q), rows[0])
     assert q.read_text().splitlines() == ["nodal_diameter,mode_family,frequency_hz,rpm", "3,1,500.000000,6000.000000",
                                           "3,2,1000.000000,6000.000000"]
+
+
+def test_modal_mass_enrichment():
+    """modal_mass_kg = N * Re(phi^H M_sector phi) per mode (python/turbomodal/solver.py:91-103)."""
+    import scipy.sparse as sp
+
+    from turbomodal_gb300.solver import EnrichedModalResult, _modal_mass_from_M
+
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((6, 6))
+    M = sp.csc_matrix(A @ A.T + 6 * np.eye(6))
+    phi = rng.standard_normal((6, 2)) + 1j * rng.standard_normal((6, 2))
+    r = ModalResult(1, 0.0, np.array([1.0, 2.0]), phi, np.zeros(2, np.int32))
+    (mm,) = _modal_mass_from_M(M, [r], 24)
+    expect = [24 * np.real(np.vdot(phi[:, q], M @ phi[:, q])) for q in range(2)]
+    np.testing.assert_allclose(mm, expect, rtol=1e-13)
+    e = EnrichedModalResult(_result=r, modal_mass_kg=mm)
+    assert e.harmonic_index == 1 and e.modal_mass_kg is mm
