@@ -22,7 +22,6 @@ from __future__ import annotations
 
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys
@@ -206,9 +205,6 @@ def run_reference(args, ws, rank, pg):
     needs Eigen and Spectra, which are not available) on the same workload family."""
     if rank != 0:
         return
-    from turbomodal_gb300.meshgen import config_mesh
-    from turbomodal_gb300.solver import CyclicSymmetrySolver  # noqa: F401  (F_target needs no GPU below)
-
     cores = os.cpu_count() or 1
     # factorisation flops of the config-1 harmonic operator (host symbolic analysis only)
     F_target = 3.79696e12

@@ -10,7 +10,7 @@ for the modal solve; it carries no device state.
 from __future__ import annotations
 
 import math
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 
