@@ -46,6 +46,8 @@ extern "C" {
 #define TMG_MAT_MHR 23
 #define TMG_MAT_KK 30      /* per-harmonic K_k, M_k       cyclic_solver.cpp:942-947 */
 #define TMG_MAT_MK 31
+#define TMG_MAT_L1 32      /* Lancaster L1 = [[i 2 omega G_k, K_k], [K_k, 0]]  modal_solver.cpp:151-177 */
+#define TMG_MAT_L2 33      /* Lancaster L2 = [[M_k, 0], [0, K_k]]             modal_solver.cpp:179-198 */
 
 /* Arithmetic of the shift-invert factorisation and triangular solves. */
 #define TMG_PREC_FP64 0    /* plain FP64 supernodal LDL^H */
@@ -116,8 +118,10 @@ int tmg_prepare(tmg_context* ctx, double rpm, int coriolis);
 /* Copy a projected matrix (complex interleaved values) after tmg_prepare.
  * k selects the harmonic for TMG_MAT_KK / TMG_MAT_MK, which are returned on the union of the
  * projections' structural patterns (the operator the solver factorises): entries that the
- * reference's pruning removes as roundoff are present as exact zeros.  Pass NULL arrays to
- * query. */
+ * reference's pruning removes as roundoff are present as exact zeros.  TMG_MAT_L1 / TMG_MAT_L2
+ * (after tmg_prepare with coriolis at a nonzero speed, 0 < k <= N/2) are the 2n x 2n matrices of
+ * the Coriolis QEP, both on the pattern of the shifted operator L1 - sigma L2 (*n = 2n).  Pass
+ * NULL arrays to query. */
 int tmg_projection(tmg_context* ctx, int which, int k, int64_t* nnz, int32_t* n,
                    int32_t* colptr, int32_t* rowidx, double* values);
 
@@ -128,7 +132,8 @@ int tmg_projection(tmg_context* ctx, int which, int k, int64_t* nnz, int32_t* n,
 int tmg_symbolic(tmg_context* ctx, int kind, int32_t* n, int32_t* perm, int32_t* parent,
                  int32_t* colcount);
 
-/* Size of the symbolic factorisation of kind (see tmg_symbolic), 10 doubles: out[0] n, [1] nnz(L)
+/* Size of the symbolic factorisation of kind (see tmg_symbolic; 3: the Coriolis QEP operator
+ * L1 - sigma L2 after tmg_prepare with coriolis), 10 doubles: out[0] n, [1] nnz(L)
  * of the simplicial factor, [2] supernodes, [3] tree levels, [4] largest front, [5] L-panel
  * storage entries per problem, [6] factorisation flops (real; complex arithmetic counted x4),
  * [7] operator lower-triangle entries, [8] update-block workspace entries per problem,

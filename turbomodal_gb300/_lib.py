@@ -20,7 +20,7 @@ ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "state error", 4: "numerica
 
 MAT = {"K": 0, "M": 1, "Komega": 2, "G": 3, "Ksigma": 4, "Keff": 5,
        "Kcf": 10, "Kpf": 11, "Mcf": 12, "Mpf": 13, "Gcf": 14, "Gpf": 15,
-       "K0r": 20, "M0r": 21, "Khr": 22, "Mhr": 23, "Kk": 30, "Mk": 31}
+       "K0r": 20, "M0r": 21, "Khr": 22, "Mhr": 23, "Kk": 30, "Mk": 31, "L1": 32, "L2": 33}
 PREC = {"fp64": 0, "mixed": 1}
 STATIC_SCRATCH_ENTRIES = 524288   # TMG_STATIC_SCRATCH_ENTRIES
 

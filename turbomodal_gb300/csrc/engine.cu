@@ -417,6 +417,18 @@ struct tmg_context {
     UnionMaps pairOp, pairM;
     OpSymbolic pairSym;
     std::string pair_key;
+    // Coriolis QEP: gyroscopic sum domain W_G = Gc u Gp u Gp^H and the Lancaster block maps
+    // of the shifted operator L1 - sigma L2 and of L2 over (W, W_M, W_G)
+    std::vector<int64_t> gpT;
+    Pattern GpfH;
+    UnionMaps WG0;
+    struct Qep {
+        DVec<int64_t> sk, sm, sg, sk2, sm2, sg2;
+        DVec<int8_t> blk, blk2;
+        UnionMaps op, l2;
+        OpSymbolic sym;
+        std::string key;
+    } qep;
     std::vector<ResultHost> results;
     double phase_ms[8] = {0};
     int64_t launches = 0;
@@ -938,6 +950,29 @@ void prepare(tmg_context* c, double rpm, bool coriolis) {
     c->phase_ms[0] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
+// Gyroscopic sum domain and Lancaster block maps of the prepared speed (built when the
+// structural patterns of K, M or G change; the symbolic analysis follows lazily).
+void ensure_qep(tmg_context* c) {
+    const std::string key = c->symC_key + pattern_key(c->Gcf.spat) + pattern_key(c->Gpf.spat);
+    if (key == c->qep.key) return;
+    c->GpfH = transpose_map(c->Gpf.spat, c->gpT);
+    build_union(c->WG0, {&c->Gcf.spat, &c->Gpf.spat, &c->GpfH});
+    {
+        std::vector<int64_t> m = c->WG0.maps[2].download();
+        for (auto& v : m) if (v >= 0) v = c->gpT[v];
+        c->WG0.maps[2].upload(m);
+    }
+    auto& Q = c->qep;
+    const LancasterBlocks A = lancaster_blocks(c->W0.U, c->WM0.U, c->WG0.U, 0);
+    const LancasterBlocks L2 = lancaster_blocks(c->W0.U, c->WM0.U, c->WG0.U, 1);
+    build_union(Q.op, {&A.P});
+    build_union(Q.l2, {&L2.P});
+    Q.sk.upload(A.srcK); Q.sm.upload(A.srcM); Q.sg.upload(A.srcG); Q.blk.upload(A.blk);
+    Q.sk2.upload(L2.srcK); Q.sm2.upload(L2.srcM); Q.sg2.upload(L2.srcG); Q.blk2.upload(L2.blk);
+    Q.sym.valid = false;
+    Q.key = key;
+}
+
 }  // namespace
 
 namespace {
@@ -980,6 +1015,34 @@ __global__ void k_form_complex(int64_t n, const int64_t* __restrict__ ikc, const
     const zd kk = (zd{a, 0.0} + P * zd{b, 0.0}) + Pc * zd{c, 0.0};
     const zd mm = (zd{am, 0.0} + P * zd{bm, 0.0}) + Pc * zd{cm, 0.0};
     out[p * n + e] = kk - sigma * mm;
+}
+
+// Lancaster matrices of the Coriolis QEP per problem (src/modal_solver.cpp:151-198 and the
+// shifted operator of src/hermitian_lanczos.cpp:15): L1 = [[D, K], [K, 0]] with
+// D = (i 2 omega) G, L2 = [[M, 0], [0, K]].  mode 0: L1 - sigma_p L2, 1: L1, 2: L2.  K, M, G
+// hold each problem's harmonic values on their domains (nK, nM, nG entries per problem);
+// an absent block entry reads as an exact zero.
+__global__ void k_form_lancaster(int64_t ne, const int64_t* __restrict__ sk, const int64_t* __restrict__ sm,
+                                 const int64_t* __restrict__ sg, const int8_t* __restrict__ blk,
+                                 const zd* __restrict__ K, int64_t nK, const zd* __restrict__ M, int64_t nM,
+                                 const zd* __restrict__ G, int64_t nG, double two_omega,
+                                 const double* __restrict__ sigma, int mode, zd* __restrict__ out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t p = blockIdx.y;
+    if (e >= ne) return;
+    const int b = blk[e];
+    const zd z{0.0, 0.0};
+    const zd kv = sk[e] >= 0 ? K[p * nK + sk[e]] : z;
+    zd l1 = z, l2 = z;
+    if (b == 0) {
+        if (sg[e] >= 0) l1 = zd{0.0, two_omega} * G[p * nG + sg[e]];
+        if (sm[e] >= 0) l2 = M[p * nM + sm[e]];
+    } else if (b == 3) {
+        l2 = kv;
+    } else {
+        l1 = kv;
+    }
+    out[p * ne + e] = mode == 1 ? l1 : (mode == 2 ? l2 : l1 - sigma[p] * l2);
 }
 
 // free-space degenerate duplication: column m <- src m/2, conjugated when m is odd
@@ -1271,7 +1334,7 @@ template <> zd rnd_entry<zd>(std::mt19937& g, std::normal_distribution<double>& 
 // restart cycle and extracts every problem as soon as it has converged.
 template <typename Tv, typename Tf>
 std::vector<EigOut<Tv>> lanczos(tmg_context* c, ShiftInvertB<Tv, Tf>& op, const DevCsr<Tv>& M, int nev, int ncv,
-                                double shift, double tol, int max_restarts) {
+                                double shift, double tol, int max_restarts, const double* dshifts = nullptr) {
     const int64_t n = op.n;
     const int B = op.B;
     cudaStream_t st = c->st;
@@ -1330,7 +1393,8 @@ std::vector<EigOut<Tv>> lanczos(tmg_context* c, ShiftInvertB<Tv, Tf>& op, const 
                 remaining--;
             }
         if (remaining == 0) break;
-        lz_tridiag(st, B, m, ncv, nev, shift, tol, alpha.p, beta.p, theta.p, S.p, lam.p, order.p, nconv.p, Z.p);
+        lz_tridiag(st, B, m, ncv, nev, shift, tol, alpha.p, beta.p, theta.p, S.p, lam.p, order.p, nconv.p, Z.p,
+                   dshifts);
         TMG_CUDA(cudaMemcpyAsync(hn.data(), nconv.p, B * sizeof(int), cudaMemcpyDeviceToHost, st));
         TMG_CUDA(cudaStreamSynchronize(st));
         for (int p = 0; p < B; p++) {
@@ -1387,6 +1451,24 @@ struct Problem {
     int nev_target = 0;
     ResultHost* R = nullptr;
 };
+
+// Mode-shape expansion u_full = T(0) u_reduced with the right-boundary rows times e^{ik alpha}
+// (src/cyclic_solver.cpp:1185-1211); X holds nm free-space columns of n_free entries.
+void expand_to_sector(tmg_context* c, const Problem& pr, const zd* X, int nm, ResultHost& R) {
+    Sector& S = *c->sec;
+    cudaStream_t st = c->st;
+    const int32_t ndof = 3 * S.nn;
+    DVec<zd> full;
+    full.alloc((size_t)ndof * std::max(nm, 1));
+    if (nm) TMG_LAUNCH(k_expand, dim3(nblk(ndof), nm), 256, 0, st, ndof, c->dT0_rp.p, c->dT0_ci.p, c->dT0_v.p,
+                       c->d_isr.p, c->d_r2free.p, X, (int64_t)S.n_free, pr.P, full.p, (int64_t)ndof);
+    TMG_CHECK_LAUNCH();
+    R.shapes.resize((size_t)ndof * nm);
+    if (nm) {
+        TMG_CUDA(cudaMemcpyAsync(R.shapes.data(), full.p, R.shapes.size() * sizeof(zd), cudaMemcpyDeviceToHost, st));
+        TMG_CUDA(cudaStreamSynchronize(st));
+    }
+}
 
 // Post-processing of one problem (cyclic_solver.cpp:1058-1211): frequencies, min-frequency
 // filter, truncation, residual diagnostic, degenerate duplication, expansion to the full
@@ -1458,24 +1540,60 @@ void finish_result(tmg_context* c, const Problem& pr, EigOut<Tv>& eo, const DevC
         R.freqs = f2;
         Xsrc = Xd.p;
     }
-    const int32_t ndof = 3 * S.nn;
-    DVec<zd> full;
-    full.alloc((size_t)ndof * std::max(nm, 1));
-    if (nm) TMG_LAUNCH(k_expand, dim3(nblk(ndof), nm), 256, 0, st, ndof, c->dT0_rp.p, c->dT0_ci.p, c->dT0_v.p,
-                       c->d_isr.p, c->d_r2free.p, Xsrc, n, pr.P, full.p, (int64_t)ndof);
-    TMG_CHECK_LAUNCH();
-    R.shapes.resize((size_t)ndof * nm);
-    if (nm) {
-        TMG_CUDA(cudaMemcpyAsync(R.shapes.data(), full.p, R.shapes.size() * sizeof(zd), cudaMemcpyDeviceToHost, st));
-        TMG_CUDA(cudaStreamSynchronize(st));
+    expand_to_sector(c, pr, Xsrc, nm, R);
+}
+
+// Coriolis QEP post-processing (src/modal_solver.cpp:249-309, then src/cyclic_solver.cpp:
+// 1058-1094 and :1185-1211): Ritz values |omega| < 1e-6 dropped, the lowest num_modes forward
+// (omega > 0) and backward (omega < 0) values by |omega| kept and re-sorted by |omega|,
+// frequencies |omega| / 2 pi, whirl +1 / -1, shapes = the first n rows of the 2n Lancaster
+// vectors; then the min-frequency filter, the truncation to num_modes and the expansion to
+// the sector DOFs.  The QEP has no residual check and no degenerate duplication.
+void finish_qep(tmg_context* c, const Problem& pr, const EigOut<zd>& eo, int num_modes, double min_frequency) {
+    Sector& S = *c->sec;
+    ResultHost& R = *pr.R;
+    const int64_t n = S.n_free, n2 = 2 * n;
+    struct Entry { double om; int idx; int wh; };
+    std::vector<Entry> ent;
+    for (int i = 0; i < eo.ne; i++) {
+        const double om = eo.lam[i];
+        if (std::fabs(om) < 1e-6) continue;
+        ent.push_back({om, i, om > 0 ? 1 : -1});
     }
+    auto byabs = [](const Entry& a, const Entry& b) { return std::fabs(a.om) < std::fabs(b.om); };
+    std::sort(ent.begin(), ent.end(), byabs);
+    int nfw = 0, nbw = 0;
+    std::vector<Entry> sel;
+    for (const Entry& e : ent) {
+        if (e.wh == 1 && nfw < num_modes) { sel.push_back(e); nfw++; }
+        else if (e.wh == -1 && nbw < num_modes) { sel.push_back(e); nbw++; }
+        if (nfw >= num_modes && nbw >= num_modes) break;
+    }
+    std::sort(sel.begin(), sel.end(), byabs);
+    if (!eo.converged && sel.empty()) { R.status = TMG_ERR_NUMERIC; return; }
+    std::vector<Entry> keep;
+    for (const Entry& e : sel)
+        if (!(min_frequency > 0.0) || std::fabs(e.om) / (2.0 * PI) > min_frequency) keep.push_back(e);
+    if (keep.size() < sel.size() && keep.empty()) { R.status = TMG_ERR_NUMERIC; return; }
+    if ((int)keep.size() > pr.nev_target) keep.resize(pr.nev_target);
+    const int nm = (int)keep.size();
+    DVec<zd> Xq;
+    Xq.alloc((size_t)n * std::max(nm, 1));
+    R.freqs.clear();
+    R.whirl.clear();
+    for (int t = 0; t < nm; t++) {
+        R.freqs.push_back(std::fabs(keep[t].om) / (2.0 * PI));
+        R.whirl.push_back(keep[t].wh);
+        lz_copy<zd>(c->st, n, eo.X.p + (int64_t)keep[t].idx * n2, Xq.p + (int64_t)t * n);
+    }
+    expand_to_sector(c, pr, Xq.p, nm, R);
 }
 
 // Factor and solve a batch of problems that share one symbolic analysis.
 template <typename Tv, typename Tf>
 void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os, const UnionMaps& um,
                const Tv* vals_csc, const DevCsr<Tv>& M, int nev, int ncv, double shift, int max_restarts, bool mixed,
-               int num_modes, double min_frequency) {
+               int num_modes, double min_frequency, const std::vector<double>* shifts = nullptr, bool qep = false) {
     cudaStream_t st = c->st;
     const int B = (int)probs.size();
     const int64_t nl = (int64_t)um.lower2csc.n, nU = um.U.nnz();
@@ -1492,7 +1610,9 @@ void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os
     op.factor(lower.p);
     lower.release();
     auto t1 = std::chrono::steady_clock::now();
-    std::vector<EigOut<Tv>> eo = lanczos<Tv, Tf>(c, op, M, nev, ncv, shift, 1e-8, max_restarts);
+    DVec<double> dsh;
+    if (shifts) dsh.upload(*shifts);
+    std::vector<EigOut<Tv>> eo = lanczos<Tv, Tf>(c, op, M, nev, ncv, shift, 1e-8, max_restarts, shifts ? dsh.p : nullptr);
     auto t2 = std::chrono::steady_clock::now();
     c->phase_ms[1] += std::chrono::duration<double, std::milli>(t1 - t0).count();
     c->phase_ms[2] += std::chrono::duration<double, std::milli>(t2 - t1).count();
@@ -1514,6 +1634,9 @@ void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os
         R.applies = op.applies;
         if (!eo[p].failed.empty()) { R.status = TMG_ERR_NUMERIC; c->err = eo[p].failed; continue; }
         if (!eo[p].converged && eo[p].ne == 0) { R.status = TMG_ERR_NUMERIC; continue; }
+        if constexpr (std::is_same<Tv, zd>::value) {
+            if (qep) { finish_qep(c, probs[p], eo[p], num_modes, min_frequency); continue; }
+        }
         DevCsr<Tv> Ap = A, Mp = M;
         Ap.val = A.val + p * A.vstride;
         Mp.val = M.val + p * M.vstride;
@@ -1539,6 +1662,136 @@ int batch_size(tmg_context* c, const OpSymbolic& os, const UnionMaps& um, int64_
     return std::max(1, std::min(nprob, b));
 }
 
+// Coriolis harmonics k > 0: the Lancaster QEP (src/modal_solver.cpp:200-312) on the 2n block
+// operator.  Shift per harmonic sqrt(|K_k|_F / |M_k|_F) (src/cyclic_solver.cpp:985-1006, the
+// square root taken at src/modal_solver.cpp:243); nev = 2n - 1 on
+// the dense path (2n <= 200), else min(6 num_modes, 2n - 1) with ncv = min(max(4 nev + 1, 40),
+// 2n) and 20 restarts, batched like the standard harmonics under the memory budget.  The shifted
+// operator [[D - sigma M, K], [K, -sigma K]] is indefinite and factorised without pivoting, as
+// in the reference, where refinement of an FP32 factor has no convergence guarantee: the QEP
+// runs in FP64 at either precision setting.
+void solve_qep(tmg_context* c, std::vector<Problem>& probs, int num_modes, double min_frequency) {
+    Sector& S = *c->sec;
+    cudaStream_t st = c->st;
+    ensure_qep(c);
+    auto& Q = c->qep;
+    const int64_t n2 = 2 * (int64_t)S.n_free;
+    const double two_omega = 2.0 * (c->rpm * 2.0 * PI / 60.0);
+    const bool dense = n2 <= 200;
+    const int nev = dense ? (int)n2 - 1 : (int)std::min<int64_t>(6 * (int64_t)num_modes, n2 - 1);
+    const int ncv = (int)std::min<int64_t>(std::max(4 * nev + 1, 40), n2);
+    if (nev <= 0 || (!dense && ncv > 256)) {
+        for (auto& pr : probs) pr.R->status = TMG_ERR_NUMERIC;
+        c->err = nev <= 0 ? "Coriolis QEP: system too small for the requested modes"
+                          : "Coriolis QEP: a Lanczos subspace of " + std::to_string(ncv) +
+                                " vectors (num_modes > 10) is not supported";
+        return;
+    }
+    const UnionMaps &WK = c->W0, &WM = c->WM0, &WG = c->WG0;
+    const int64_t nK = WK.U.nnz(), nM = WM.U.nnz(), nG = WG.U.nnz();
+    const int64_t nA = Q.op.U.nnz(), nL = Q.l2.U.nnz();
+    int bmax = (int)probs.size();
+    if (!dense) {
+        if (!Q.sym.valid) analyze_op(Q.sym, Q.op);
+        bmax = batch_size(c, Q.sym, Q.op, nL, ncv, true, false, (int)probs.size());
+    }
+    for (size_t b0 = 0; b0 < probs.size(); b0 += bmax) {
+        std::vector<Problem> grp(probs.begin() + b0, probs.begin() + std::min(probs.size(), b0 + bmax));
+        const int B = (int)grp.size();
+        std::vector<double> ph(2 * B);
+        for (int p = 0; p < B; p++) { ph[2 * p] = grp[p].P.x; ph[2 * p + 1] = grp[p].P.y; }
+        DVec<double> dph;
+        dph.upload(ph);
+        // K_k, M_k, G_k on their structural domains
+        DVec<zd> Kv, Mv, Gv;
+        Kv.alloc((size_t)B * std::max<int64_t>(1, nK));
+        Mv.alloc((size_t)B * std::max<int64_t>(1, nM));
+        Gv.alloc((size_t)B * std::max<int64_t>(1, nG));
+        if (nK) TMG_LAUNCH(k_form_csum, dim3(nblk(nK), B), 256, 0, st, nK, WK.maps[0].p, WK.maps[1].p, WK.maps[2].p,
+                           c->Kcf.sv.p, c->Kpf.sv.p, dph.p, Kv.p);
+        if (nM) TMG_LAUNCH(k_form_csum, dim3(nblk(nM), B), 256, 0, st, nM, WM.maps[0].p, WM.maps[1].p, WM.maps[2].p,
+                           c->Mcf.sv.p, c->Mpf.sv.p, dph.p, Mv.p);
+        if (nG) TMG_LAUNCH(k_form_csum, dim3(nblk(nG), B), 256, 0, st, nG, WG.maps[0].p, WG.maps[1].p, WG.maps[2].p,
+                           c->Gcf.sv.p, c->Gpf.sv.p, dph.p, Gv.p);
+        std::vector<double> sig(B);
+        {
+            DVec<double> part, nk2, nm2;
+            part.alloc((size_t)B * LZ_DOT_BLOCKS);
+            nk2.alloc(B);
+            nm2.alloc(B);
+            lz_norm2<zd>(st, B, nK, Kv.p, nK, part.p, nk2.p);
+            lz_norm2<zd>(st, B, nM, Mv.p, nM, part.p, nm2.p);
+            const std::vector<double> hk = nk2.download(), hm = nm2.download();
+            for (int p = 0; p < B; p++) {
+                const double mn = std::sqrt(hm[p]);
+                const double sh = mn > 0.0 ? std::sqrt(hk[p]) / mn : 1.0;
+                sig[p] = sh > 0.0 ? std::sqrt(sh) : 0.1;
+            }
+        }
+        DVec<double> dsig;
+        dsig.upload(sig);
+        if (dense) {   // all eigenpairs of (L1, L2) by the dense solver (src/hermitian_lanczos.cpp:68-110)
+            const int64_t nn = n2 * n2;
+            DVec<zd> L1v, L2v, L1d, L2d, work, X;
+            DVec<double> lam, res;
+            DVec<int> status;
+            L1v.alloc((size_t)B * nA); L2v.alloc((size_t)B * nA);
+            for (int mode : {1, 2})
+                TMG_LAUNCH(k_form_lancaster, dim3(nblk(nA), B), 256, 0, st, nA, Q.sk.p, Q.sm.p, Q.sg.p, Q.blk.p, Kv.p,
+                           nK, Mv.p, nM, Gv.p, nG, two_omega, dsig.p, mode, mode == 1 ? L1v.p : L2v.p);
+            L1d.alloc((size_t)B * nn); L2d.alloc((size_t)B * nn); work.alloc((size_t)B * 5 * nn);
+            X.alloc((size_t)B * n2 * nev); lam.alloc((size_t)B * nev); res.alloc((size_t)B * nev); status.alloc(B);
+            status.zero(st);
+            DVec<int64_t> cp;
+            DVec<int32_t> ri;
+            cp.upload(Q.op.U.p);
+            ri.upload(Q.op.U.i);
+            for (int p = 0; p < B; p++) {
+                dense_csc_to_dense(st, (int)n2, cp.p, ri.p, L1v.p + p * nA, L1d.p + p * nn);
+                dense_csc_to_dense(st, (int)n2, cp.p, ri.p, L2v.p + p * nA, L2d.p + p * nn);
+            }
+            auto t1 = std::chrono::steady_clock::now();
+            dense_geig(st, B, (int)n2, nev, L1d.p, L2d.p, work.p, lam.p, X.p, res.p, status.p);
+            const std::vector<double> hl = lam.download();
+            const std::vector<int> hs = status.download();
+            c->phase_ms[2] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
+            for (int p = 0; p < B; p++) {
+                ResultHost& R = *grp[p].R;
+                if (hs[p]) { R.status = TMG_ERR_NUMERIC; c->err = "dense eigensolver: L2 is not positive definite"; continue; }
+                EigOut<zd> eo;
+                eo.ne = nev;
+                eo.converged = true;
+                eo.lam.assign(hl.begin() + (int64_t)p * nev, hl.begin() + (int64_t)(p + 1) * nev);
+                eo.X.alloc((size_t)n2 * nev);
+                lz_copy<zd>(st, n2 * nev, X.p + (int64_t)p * n2 * nev, eo.X.p);
+                R.converged = 1;
+                finish_qep(c, grp[p], eo, num_modes, min_frequency);
+            }
+            continue;
+        }
+        DVec<zd> vals, l2c, l2r;
+        vals.alloc((size_t)B * nA);
+        l2c.alloc((size_t)B * nL);
+        l2r.alloc((size_t)B * nL);
+        TMG_LAUNCH(k_form_lancaster, dim3(nblk(nA), B), 256, 0, st, nA, Q.sk.p, Q.sm.p, Q.sg.p, Q.blk.p, Kv.p, nK, Mv.p,
+                   nM, Gv.p, nG, two_omega, dsig.p, 0, vals.p);
+        TMG_LAUNCH(k_form_lancaster, dim3(nblk(nL), B), 256, 0, st, nL, Q.sk2.p, Q.sm2.p, Q.sg2.p, Q.blk2.p, Kv.p, nK,
+                   Mv.p, nM, Gv.p, nG, two_omega, dsig.p, 2, l2c.p);
+        TMG_LAUNCH(k_gather_b<zd>, dim3(nblk(nL), B), 256, 0, st, nL, Q.l2.csr2csc.p, l2c.p, nL, l2r.p, nL);
+        l2c.release(); Kv.release(); Mv.release(); Gv.release();
+        DevCsr<zd> L2;
+        L2.nrows = n2; L2.nnz = nL; L2.rowptr = Q.l2.csr_rowptr.p; L2.col = Q.l2.csr_col.p; L2.val = l2r.p;
+        L2.vstride = nL;
+        try {
+            run_batch<zd, zd>(c, grp, Q.sym, Q.op, vals.p, L2, nev, ncv, 0.0, 20, false, num_modes, min_frequency,
+                              &sig, true);
+        } catch (const numeric_error& e) {
+            for (auto& pr : grp) pr.R->status = TMG_ERR_NUMERIC;
+            c->err = e.what();
+        }
+    }
+}
+
 void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double min_frequency, int precision,
                std::vector<ResultHost>& results) {
     Sector& S = *c->sec;
@@ -1548,7 +1801,7 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
     const bool mixed = precision == TMG_PREC_MIXED;
     const double shift = 1.0;
     results.assign(ks.size(), ResultHost{});
-    std::vector<Problem> cplx, real0, realh, dense;
+    std::vector<Problem> cplx, real0, realh, dense, qep;
     for (size_t q = 0; q < ks.size(); q++) {
         const int k = ks[q];
         ResultHost& R = results[q];
@@ -1560,7 +1813,11 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
         pr.R = &R;
         if (S.n_free <= 1) { R.status = TMG_ERR_ARG; continue; }
         pr.degenerate = (k > 0) && !(N % 2 == 0 && k == max_k);
-        if (c->coriolis && k > 0) { R.status = TMG_ERR_STATE; continue; }
+        if (c->coriolis && k > 0) {   // QEP: the full mode count, no degenerate duplication
+            pr.nev_target = num_modes;
+            qep.push_back(pr);
+            continue;
+        }
         pr.nev_target = pr.degenerate ? (num_modes + 1) / 2 : num_modes;
         const bool is_real = (k == 0) || (N % 2 == 0 && k == max_k);
         if (S.n_free <= 200) { dense.push_back(pr); continue; }
@@ -1732,6 +1989,7 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
             }
         }
     }
+    if (!qep.empty()) solve_qep(c, qep, num_modes, min_frequency);
     TMG_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -1905,6 +2163,42 @@ int tmg_projection(tmg_context* c, int which, int k, int64_t* nnz, int32_t* n, i
                 }
                 return TMG_OK;
             }
+            case TMG_MAT_L1:
+            case TMG_MAT_L2: {
+                if (!c->coriolis) return set_err(c, TMG_ERR_STATE, "prepare with coriolis at a nonzero speed first");
+                if (k <= 0 || k > S.ns / 2) return set_err(c, TMG_ERR_ARG, "the Coriolis QEP is solved for 0 < k <= N/2");
+                ensure_qep(c);
+                const auto& Q = c->qep;
+                const UnionMaps *WK = &c->W0, *WM = &c->WM0, *WG = &c->WG0;
+                const int64_t nK = WK->U.nnz(), nM = WM->U.nnz(), nG = WG->U.nnz(), nA = Q.op.U.nnz();
+                const double alpha = 2.0 * PI / S.ns;
+                DVec<double> ph, sig;
+                ph.upload(std::vector<double>{std::cos(k * alpha), std::sin(k * alpha)});
+                sig.upload(std::vector<double>{0.0});
+                DVec<zd> Kv, Mv, Gv, v;
+                Kv.alloc(std::max<int64_t>(1, nK)); Mv.alloc(std::max<int64_t>(1, nM)); Gv.alloc(std::max<int64_t>(1, nG));
+                v.alloc(std::max<int64_t>(1, nA));
+                if (nK) TMG_LAUNCH(k_form_csum, dim3(nblk(nK), 1), 256, 0, c->st, nK, WK->maps[0].p, WK->maps[1].p,
+                                   WK->maps[2].p, c->Kcf.sv.p, c->Kpf.sv.p, ph.p, Kv.p);
+                if (nM) TMG_LAUNCH(k_form_csum, dim3(nblk(nM), 1), 256, 0, c->st, nM, WM->maps[0].p, WM->maps[1].p,
+                                   WM->maps[2].p, c->Mcf.sv.p, c->Mpf.sv.p, ph.p, Mv.p);
+                if (nG) TMG_LAUNCH(k_form_csum, dim3(nblk(nG), 1), 256, 0, c->st, nG, WG->maps[0].p, WG->maps[1].p,
+                                   WG->maps[2].p, c->Gcf.sv.p, c->Gpf.sv.p, ph.p, Gv.p);
+                if (nA) TMG_LAUNCH(k_form_lancaster, dim3(nblk(nA), 1), 256, 0, c->st, nA, Q.sk.p, Q.sm.p, Q.sg.p,
+                                   Q.blk.p, Kv.p, nK, Mv.p, nM, Gv.p, nG, 2.0 * (c->rpm * 2.0 * PI / 60.0), sig.p,
+                                   which == TMG_MAT_L1 ? 1 : 2, v.p);
+                TMG_CUDA(cudaStreamSynchronize(c->st));
+                if (n) *n = Q.op.U.ncols;
+                *nnz = nA;
+                if (!colptr) return TMG_OK;
+                for (int32_t j = 0; j <= Q.op.U.ncols; j++) colptr[j] = (int32_t)Q.op.U.p[j];
+                if (rowidx) std::copy(Q.op.U.i.begin(), Q.op.U.i.end(), rowidx);
+                if (values && nA) {
+                    TMG_CUDA(cudaMemcpyAsync(values, v.p, nA * sizeof(zd), cudaMemcpyDeviceToHost, c->st));
+                    TMG_CUDA(cudaStreamSynchronize(c->st));
+                }
+                return TMG_OK;
+            }
             default: return set_err(c, TMG_ERR_ARG, "unknown projection selector");
         }
         TMG_CUDA(cudaStreamSynchronize(c->st));
@@ -1962,6 +2256,11 @@ int tmg_symbolic_stats(tmg_context* c, int kind, double* out) {
             if (!c->real[kind - 1].valid) return set_err(c, TMG_ERR_STATE, "no such real harmonic");
             if (!c->pairSym.valid) analyze_op(c->pairSym, c->pairOp);
             os = &c->pairSym;
+        } else if (kind == 3) {
+            if (!c->coriolis) return set_err(c, TMG_ERR_STATE, "prepare with coriolis at a nonzero speed first");
+            ensure_qep(c);
+            if (!c->qep.sym.valid) analyze_op(c->qep.sym, c->qep.op);
+            os = &c->qep.sym;
         } else {
             return set_err(c, TMG_ERR_ARG, "unknown symbolic kind");
         }

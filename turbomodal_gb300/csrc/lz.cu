@@ -189,7 +189,8 @@ void lz_scale_first(cudaStream_t st, int B, int64_t n, const T* dot, T* V, T* MV
 // Tridiagonal eigenproblem (implicit QL with eigenvectors, EISPACK tql2 formulation), one
 // CTA per problem.  Thread 0 runs the scalar recurrences and records each sweep's
 // rotations; every thread then applies the sweep to its own row of Z.
-__global__ void __launch_bounds__(256) k_tridiag(int m, int ldab, int nev, double shift, double tol,
+__global__ void __launch_bounds__(256) k_tridiag(int m, int ldab, int nev, double shift0,
+                                                 const double* __restrict__ shifts, double tol,
                                                  const double* __restrict__ alpha_b, const double* __restrict__ beta_b,
                                                  double* __restrict__ theta_b, double* __restrict__ S_b,
                                                  double* __restrict__ lam_b, int* __restrict__ order_b,
@@ -198,6 +199,7 @@ __global__ void __launch_bounds__(256) k_tridiag(int m, int ldab, int nev, doubl
     __shared__ int perm[256], ord[256];
     __shared__ int s_m, s_go, s_lo, s_hi;
     const int p = blockIdx.x;
+    const double shift = shifts ? shifts[p] : shift0;
     const double* alpha = alpha_b + (int64_t)p * ldab;
     const double* beta = beta_b + (int64_t)p * ldab;
     double* theta = theta_b + (int64_t)p * ldab;
@@ -320,9 +322,10 @@ __global__ void __launch_bounds__(256) k_tridiag(int m, int ldab, int nev, doubl
 }
 
 void lz_tridiag(cudaStream_t st, int B, int m, int ldab, int nev, double shift, double tol, const double* alpha,
-                const double* beta, double* theta, double* S, double* lam, int* order, int* nconv, double* Z) {
+                const double* beta, double* theta, double* S, double* lam, int* order, int* nconv, double* Z,
+                const double* shifts) {
     if (m > 256) throw std::runtime_error("Lanczos subspace above 256 vectors is not supported");
-    TMG_LAUNCH(k_tridiag, B, 256, 0, st, m, ldab, nev, shift, tol, alpha, beta, theta, S, lam, order, nconv, Z);
+    TMG_LAUNCH(k_tridiag, B, 256, 0, st, m, ldab, nev, shift, shifts, tol, alpha, beta, theta, S, lam, order, nconv, Z);
     TMG_CHECK_LAUNCH();
 }
 

@@ -51,9 +51,11 @@ template <typename T>
 void lz_scale_first(cudaStream_t st, int B, int64_t n, const T* dot, T* V, T* MV, int64_t vs);
 
 // Tridiagonal eigenproblem of each problem (one CTA per problem): theta ascending,
-// S (m x m column-major), lambda = shift + 1/theta, order (by lambda), nconv.
+// S (m x m column-major), lambda = shift + 1/theta, order (by lambda), nconv.  `shifts`
+// (device, one per problem) replaces `shift` when given.
 void lz_tridiag(cudaStream_t st, int B, int m, int ldab, int nev, double shift, double tol, const double* alpha,
-                const double* beta, double* theta, double* S, double* lam, int* order, int* nconv, double* Z);
+                const double* beta, double* theta, double* S, double* lam, int* order, int* nconv, double* Z,
+                const double* shifts = nullptr);
 
 // Implicit restart QR sweeps of each problem; Q: m x m per problem; rot: scratch per problem
 void lz_restart_qr(cudaStream_t st, int B, int m, int ldab, int nev, const double* theta, double* alpha, double* beta,

@@ -2,6 +2,7 @@
 #include "sym.hpp"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <numeric>
 #include <stdexcept>
@@ -342,6 +343,39 @@ Pattern lower_triangle(const Pattern& A) {
         for (int64_t q = A.p[j]; q < A.p[j + 1]; q++)
             if (A.i[q] >= j) L.i.push_back(A.i[q]);
         L.p[j + 1] = (int64_t)L.i.size();
+    }
+    return L;
+}
+
+LancasterBlocks lancaster_blocks(const Pattern& K, const Pattern& M, const Pattern& G, int which) {
+    const int32_t n = K.ncols;
+    LancasterBlocks L;
+    L.P.nrows = L.P.ncols = 2 * n;
+    L.P.p.assign(2 * (size_t)n + 1, 0);
+    auto put = [&](int32_t r, int64_t k, int64_t m, int64_t g, int8_t b) {
+        L.P.i.push_back(r);
+        L.srcK.push_back(k); L.srcM.push_back(m); L.srcG.push_back(g); L.blk.push_back(b);
+    };
+    for (int32_t j = 0; j < n; j++) {              // block column 0: [D - sigma M; K] or [M; 0]
+        int64_t qm = M.p[j], qg = which == 0 ? G.p[j] : 0;
+        const int64_t em = M.p[j + 1], eg = which == 0 ? G.p[j + 1] : 0;
+        while (qm < em || qg < eg) {               // sorted merge of the M and G columns
+            const int32_t rm = qm < em ? M.i[qm] : INT32_MAX;
+            const int32_t rg = qg < eg ? G.i[qg] : INT32_MAX;
+            const int32_t r = std::min(rm, rg);
+            put(r, -1, rm == r ? qm : -1, rg == r ? qg : -1, 0);
+            if (rm == r) qm++;
+            if (rg == r) qg++;
+        }
+        if (which == 0)
+            for (int64_t q = K.p[j]; q < K.p[j + 1]; q++) put(n + K.i[q], q, -1, -1, 2);
+        L.P.p[j + 1] = (int64_t)L.P.i.size();
+    }
+    for (int32_t j = 0; j < n; j++) {              // block column 1: [K; -sigma K] or [0; K]
+        if (which == 0)
+            for (int64_t q = K.p[j]; q < K.p[j + 1]; q++) put(K.i[q], q, -1, -1, 1);
+        for (int64_t q = K.p[j]; q < K.p[j + 1]; q++) put(n + K.i[q], q, -1, -1, 3);
+        L.P.p[n + j + 1] = (int64_t)L.P.i.size();
     }
     return L;
 }

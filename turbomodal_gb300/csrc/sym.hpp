@@ -96,6 +96,20 @@ struct Product {
 };
 Product product(const Pattern& A, const Pattern& B);
 
+// Block layout of the Lancaster linearisation of the Coriolis QEP (src/modal_solver.cpp:151-198):
+// L1 = [[D, K], [K, 0]], L2 = [[M, 0], [0, K]] with D = i 2 omega G.  `which` = 0 gives the
+// pattern of the shifted operator L1 - sigma L2 = [[D - sigma M, K], [K, -sigma K]] (also the
+// union of L1 and L2); `which` = 1 the pattern of L2 alone.  K, M, G are the n x n patterns
+// of the harmonic's stiffness, mass and gyroscopic matrices; every 2n x 2n entry records its
+// source entry in each of them (-1 when absent) and its block (0: top-left, 1: top-right,
+// 2: bottom-left, 3: bottom-right).
+struct LancasterBlocks {
+    Pattern P;
+    std::vector<int64_t> srcK, srcM, srcG;
+    std::vector<int8_t> blk;
+};
+LancasterBlocks lancaster_blocks(const Pattern& K, const Pattern& M, const Pattern& G, int which);
+
 Pattern transpose(const Pattern& A);
 // Union of patterns (same shape).
 Pattern pattern_union(const std::vector<const Pattern*>& parts);

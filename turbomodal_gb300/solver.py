@@ -83,6 +83,8 @@ class CyclicSymmetrySolver:
                      include_coriolis: bool = False, min_frequency: float = 0.0, progress_cb=None,
                      allow_condensation: bool = False, memory_reserve_fraction: float = 0.2,
                      precision: str | None = None) -> list[ModalResult]:
+        """Modal solve at one speed (src/python_bindings.cpp:332-361).  With include_coriolis,
+        harmonics k > 0 solve the Lancaster QEP and carry whirl directions +1 / -1."""
         prec = _lib.PREC[precision or self.precision]
         hi = np.asarray(list(harmonic_indices or []), dtype=np.int32)
         nres = C.c_int32()
