@@ -316,7 +316,9 @@ def main():
 
         reqs = request_stream(args.serve_requests, seed=2024, rate_hz=20.0, min_nodes=2000,
                               max_nodes=args.serve_max_nodes)
-        done = ModalServer(device=local, budget_bytes=150 << 30, max_inflight=4).serve(reqs)
+        srv = ModalServer(device=local, budget_bytes=150 << 30, max_inflight=4)
+        done = srv.serve(reqs)
+        srv.close()
         serving = latency_summary(done)
         serving["sample"] = (f"{len(reqs)} requests, Poisson 20 req/s, config-0/1-style sectors of 2000-"
                              f"{args.serve_max_nodes} nodes (log-uniform), 24/36/48 sectors, rpm U(0,15000), "

@@ -77,3 +77,19 @@ def test_modal_mass_enrichment():
     np.testing.assert_allclose(mm, expect, rtol=1e-13)
     e = EnrichedModalResult(_result=r, modal_mass_kg=mm)
     assert e.harmonic_index == 1 and e.modal_mass_kg is mm
+
+
+def test_solve_parametric_is_solve_at_rpm_per_condition():
+    """src/cyclic_solver.cpp:1375-1485: the reference's per-condition K_eff is overwritten by the
+    solve_at_rpm it calls (:737-820), so each condition returns solve_at_rpm(condition.rpm) with
+    the call's other arguments; progress is reported once per condition."""
+    from turbomodal_gb300.solver import CyclicSymmetrySolver, ParametricCondition
+
+    calls, prog = [], []
+    s = CyclicSymmetrySolver.__new__(CyclicSymmetrySolver)
+    s.solve_at_rpm = lambda *a: calls.append(a) or [a[0]]
+    conds = [ParametricCondition(3000.0, 400.0), ParametricCondition(0.0), ParametricCondition(9000.0, 900.0, [0.01])]
+    out = s.solve_parametric(conds, 7, [1, 2], 3, True, 5.0, progress_cb=prog.append)
+    assert out == [[3000.0], [0.0], [9000.0]]
+    assert [c[:6] for c in calls] == [(r, 7, [1, 2], 3, True, 5.0) for r in (3000.0, 0.0, 9000.0)]
+    assert [p["completed"] for p in prog] == [1, 2, 3] and all(p["harmonic_k"] == -1 for p in prog)

@@ -65,3 +65,87 @@ def test_each_result_same_alone_and_in_the_mix():
         assert sorted(alone) == sorted(mixed)
         for k, a in alone.items():
             np.testing.assert_allclose(mixed[k].frequencies, a.frequencies, rtol=1e-9)
+
+
+def test_sector_key_tracks_sector_content():
+    import copy
+    import dataclasses
+
+    from turbomodal_gb300.meshgen import TITANIUM, sector_mesh
+    from turbomodal_gb300.serve import sector_key
+
+    a = sector_mesh(4, 3, 1, num_sectors=24, seed=1)
+    b = copy.deepcopy(a)
+    assert sector_key(a, TITANIUM) == sector_key(b, TITANIUM)
+    assert sector_key(a, TITANIUM) != sector_key(a, dataclasses.replace(TITANIUM, E=TITANIUM.E * 1.01))
+    b.nodes = b.nodes.copy()
+    b.nodes[5, 0] += 1e-9
+    assert sector_key(a, TITANIUM) != sector_key(b, TITANIUM)
+    c = sector_mesh(4, 3, 1, num_sectors=36, seed=1)
+    assert sector_key(a, TITANIUM) != sector_key(c, TITANIUM)
+
+
+def test_context_pool_reuse_and_eviction():
+    """Idle contexts are handed to later requests on the same sector; beyond max_cached the least
+    recently used are closed."""
+    from turbomodal_gb300.serve import ModalServer
+
+    made, closed = [], []
+
+    class Fake:
+        def __init__(self, tag):
+            self.tag = tag
+
+        def close(self):
+            closed.append(self.tag)
+
+    def factory(mesh, material, precision):
+        made.append(mesh)
+        return Fake(f"{mesh}-{len(made)}")
+
+    srv = ModalServer(budget_bytes=1, max_cached=2, solver_factory=factory)
+    s1, r1 = srv._checkout("A", "A", None, "mixed")
+    assert not r1 and made == ["A"]
+    srv._checkin("A", s1)
+    s2, r2 = srv._checkout("A", "A", None, "mixed")
+    assert r2 and s2 is s1 and made == ["A"]
+    s3, r3 = srv._checkout("A", "A", None, "mixed")          # the only idle one is in use
+    assert not r3 and made == ["A", "A"]
+    srv._checkin("A", s2)
+    srv._checkin("A", s3)
+    b1, _ = srv._checkout("B", "B", None, "mixed")
+    srv._checkin("B", b1)                                     # 3 idle > 2: the oldest A goes
+    assert closed == [s2.tag] and srv.cached_contexts() == 2
+    srv.close()
+    assert sorted(closed) == sorted([s2.tag, s3.tag, b1.tag]) and srv.cached_contexts() == 0
+
+
+def test_request_stream_with_repeated_designs():
+    from turbomodal_gb300.meshgen import TITANIUM
+    from turbomodal_gb300.serve import request_stream, sector_key
+
+    reqs = request_stream(8, seed=11, max_nodes=6000, distinct_sectors=2)
+    assert len({sector_key(r.mesh, TITANIUM) for r in reqs}) <= 2
+
+
+@pytest.mark.gpu
+def test_reused_contexts_give_fresh_results():
+    """Requests on repeated designs reuse a kept context (its sector matrices, operator patterns
+    and symbolic analyses); each result equals the request solved alone on a fresh solver."""
+    from turbomodal_gb300.serve import ModalServer, request_stream
+    from turbomodal_gb300.solver import CyclicSymmetrySolver
+
+    reqs = request_stream(6, seed=7, rate_hz=50.0, min_nodes=2000, max_nodes=9000, distinct_sectors=2)
+    srv = ModalServer(budget_bytes=24 << 30, max_inflight=2)
+    done = srv.serve(reqs)
+    srv.close()
+    assert all(not c.error for c in done), [c.error for c in done]
+    assert sum(c.reused for c in done) >= 1
+    for r, c in zip(sorted(reqs, key=lambda r: r.rid), done):
+        s = CyclicSymmetrySolver(r.mesh, r.material, precision=r.precision)
+        alone = {x.harmonic_index: x for x in s.solve_at_rpm(r.rpm, r.num_modes, r.harmonics, precision=r.precision)}
+        s.close()
+        got = {x.harmonic_index: x for x in c.results}
+        assert sorted(alone) == sorted(got)
+        for k, a in alone.items():
+            np.testing.assert_allclose(got[k].frequencies, a.frequencies, rtol=1e-9)

@@ -7,16 +7,24 @@ for the life of the request.  Worker threads take requests in arrival order; a r
 builds its operators (assembly, prestress, projections, symbolic analysis), then asks the
 server for the device memory its factorisation batch needs and waits until that much of the
 budget is free, so requests that arrive while others are on the GPU are admitted as memory
-frees up and their kernels overlap on the device.  The reference solves one request at a
-time on the CPU (python/turbomodal/solver.py:237-375); this layer has no counterpart there.
+frees up and their kernels overlap on the device.
+
+Contexts outlive their requests: an idle context is kept per sector (mesh, boundary data and
+material, by content), and a later request on the same sector takes it over with its
+assembled sector matrices, structural operator patterns and symbolic analyses, so only the
+speed-dependent work runs again.  At most `max_cached` idle contexts are kept (least recently
+used evicted).  The reference solves one request at a time on the CPU
+(python/turbomodal/solver.py:237-375); this layer has no counterpart there.
 """
 
 from __future__ import annotations
 
+import hashlib
 import math
 import queue
 import threading
 import time
+from collections import OrderedDict
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -47,6 +55,7 @@ class Completed:
     done: float = 0.0
     grant_bytes: int = 0
     error: str = ""
+    reused: bool = False           # ran on a context kept from an earlier request
 
     @property
     def latency(self) -> float:
@@ -70,15 +79,75 @@ def batch_bytes(stats: dict, num_modes: int, nproblems: int, precision: str) -> 
     return int(per * max(1, nproblems) * 1.15 + (256 << 20))
 
 
-class ModalServer:
-    """Concurrent request loop with admission by device-memory budget."""
+def sector_key(mesh, material, apply_hub_constraint: bool = True) -> str:
+    """Content fingerprint of everything a context's sector state depends on: geometry,
+    connectivity, cyclic boundary data, hub nodes and material."""
+    h = hashlib.sha1()
+    hub = mesh.find_node_set("hub_constraint") if apply_hub_constraint else None
+    for a in (mesh.nodes, mesh.elements, mesh.left_boundary, mesh.right_boundary, mesh.matched_pairs,
+              hub.node_ids if hub is not None else []):
+        arr = np.ascontiguousarray(np.asarray(a))
+        h.update(str(arr.dtype).encode() + str(arr.shape).encode())
+        h.update(arr.tobytes())
+    h.update(repr((int(mesh.num_sectors), int(mesh.rotation_axis), float(material.E), float(material.nu),
+                   float(material.rho))).encode())
+    return h.hexdigest()
 
-    def __init__(self, device: int = 0, budget_bytes: int = 150 << 30, max_inflight: int = 4):
+
+class ModalServer:
+    """Concurrent request loop with admission by device-memory budget and reuse of a sector's
+    context across requests."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 150 << 30, max_inflight: int = 4,
+                 max_cached: int = 8, solver_factory=None):
         self.device = device
         self.budget = int(budget_bytes)
         self.max_inflight = max_inflight
+        self.max_cached = max_cached
+        self._factory = solver_factory or (lambda mesh, material, precision: CyclicSymmetrySolver(
+            mesh, material, device=device, precision=precision, mem_budget_bytes=self.budget))
         self._used = 0
         self._cv = threading.Condition()
+        self._idle: OrderedDict = OrderedDict()   # sector key -> idle contexts, least recently used first
+        self._pool_lock = threading.Lock()
+
+    # -- context reuse ------------------------------------------------------------------
+    def _checkout(self, key: str, mesh, material, precision: str):
+        """An idle context of this sector (reused = True) or a new one."""
+        with self._pool_lock:
+            lst = self._idle.get(key)
+            if lst:
+                solver = lst.pop()
+                if not lst:
+                    del self._idle[key]
+                return solver, True
+        return self._factory(mesh, material, precision), False
+
+    def _checkin(self, key: str, solver) -> None:
+        """Keep an idle context; the least recently used ones beyond max_cached are closed."""
+        evicted = []
+        with self._pool_lock:
+            self._idle.setdefault(key, []).append(solver)
+            self._idle.move_to_end(key)
+            while sum(len(v) for v in self._idle.values()) > self.max_cached:
+                k0, lst = next(iter(self._idle.items()))
+                evicted.append(lst.pop(0))
+                if not lst:
+                    del self._idle[k0]
+        for s in evicted:
+            s.close()
+
+    def cached_contexts(self) -> int:
+        with self._pool_lock:
+            return sum(len(v) for v in self._idle.values())
+
+    def close(self) -> None:
+        """Release every idle context."""
+        with self._pool_lock:
+            items = [s for lst in self._idle.values() for s in lst]
+            self._idle.clear()
+        for s in items:
+            s.close()
 
     # -- memory admission ------------------------------------------------------------
     def _acquire(self, need: int) -> int:
@@ -99,9 +168,11 @@ class ModalServer:
         out = Completed(req.rid, arrival=req.arrival, start=time.perf_counter() - t0)
         solver = None
         grant = 0
+        key = sector_key(req.mesh, req.material)
+        ok = False
         try:
-            solver = CyclicSymmetrySolver(req.mesh, req.material, device=self.device, precision=req.precision,
-                                          mem_budget_bytes=self.budget)
+            solver, out.reused = self._checkout(key, req.mesh, req.material, req.precision)
+            solver.set_memory_budget(self.budget)
             solver.prepare(req.rpm)
             ks = list(req.harmonics) or list(range(req.mesh.num_sectors // 2 + 1))
             n_cplx = sum(1 for k in ks if 0 < k and 2 * k != req.mesh.num_sectors)
@@ -111,13 +182,17 @@ class ModalServer:
             out.grant_bytes = grant
             solver.set_memory_budget(grant)
             out.results = solver.solve_at_rpm(req.rpm, req.num_modes, ks, precision=req.precision)
+            ok = True
         except Exception as e:  # a failed request is reported, the stream goes on
             out.error = f"{type(e).__name__}: {e}"
         finally:
-            if solver is not None:
-                solver.close()
             if grant:
                 self._release(grant)
+            if solver is not None:
+                if ok:
+                    self._checkin(key, solver)
+                else:   # a context that failed mid-request is not kept
+                    solver.close()
             out.done = time.perf_counter() - t0
         return out
 
@@ -155,20 +230,32 @@ class ModalServer:
 
 
 def request_stream(n: int, seed: int, rate_hz: float = 20.0, min_nodes: int = 2000, max_nodes: int = 200000,
-                   precision: str = "mixed") -> list:
+                   precision: str = "mixed", distinct_sectors: int | None = None) -> list:
     """Seeded request stream: Poisson arrivals at `rate_hz`, config-0/1-style sectors of
     log-uniform size in [min_nodes, max_nodes], 24/36/48 sectors, rpm U(0, 15000), 5..20
-    modes, a random subset of 1..19 harmonic indices, titanium."""
+    modes, a random subset of 1..19 harmonic indices, titanium.  With `distinct_sectors`,
+    every request draws its sector from that many seeded designs (a fleet of repeated
+    designs) instead of a new sector per request."""
     from .meshgen import TITANIUM, scaled_mesh
 
     rng = np.random.default_rng(seed)
+    designs = []
+    if distinct_sectors:
+        for _ in range(distinct_sectors):
+            nodes = int(math.exp(rng.uniform(math.log(min_nodes), math.log(max_nodes))))
+            ns = int(rng.choice([24, 36, 48]))
+            designs.append(scaled_mesh(nodes, ns, seed=int(rng.integers(1 << 30)), with_blade=nodes > 6000))
     t = 0.0
     out = []
     for i in range(n):
         t += rng.exponential(1.0 / rate_hz)
-        nodes = int(math.exp(rng.uniform(math.log(min_nodes), math.log(max_nodes))))
-        ns = int(rng.choice([24, 36, 48]))
-        mesh = scaled_mesh(nodes, ns, seed=int(rng.integers(1 << 30)), with_blade=nodes > 6000)
+        if designs:
+            mesh = designs[int(rng.integers(len(designs)))]
+            ns = mesh.num_sectors
+        else:
+            nodes = int(math.exp(rng.uniform(math.log(min_nodes), math.log(max_nodes))))
+            ns = int(rng.choice([24, 36, 48]))
+            mesh = scaled_mesh(nodes, ns, seed=int(rng.integers(1 << 30)), with_blade=nodes > 6000)
         kmax = ns // 2
         nk = int(rng.integers(1, min(19, kmax + 1) + 1))
         ks = sorted(int(k) for k in rng.choice(kmax + 1, size=nk, replace=False))
@@ -184,4 +271,5 @@ def latency_summary(done: list) -> dict:
     pairs = sum(c.eigenpairs for c in ok)
     return {"requests": len(done), "failed": len(done) - len(ok), "p50_s": float(np.percentile(lat, 50)),
             "p99_s": float(np.percentile(lat, 99)), "eigenpairs": pairs,
-            "eigenpairs_per_s": pairs / span if span > 0 else 0.0, "makespan_s": span}
+            "eigenpairs_per_s": pairs / span if span > 0 else 0.0, "makespan_s": span,
+            "reused_contexts": sum(1 for c in done if c.reused)}

@@ -50,6 +50,19 @@ class ModalResult:
                 f"freqs={np.round(self.frequencies, 3).tolist()}, converged={self.converged})")
 
 
+@dataclass
+class ParametricCondition:
+    """Operating condition of solve_parametric (include/turbomodal/cyclic_solver.hpp:58-62,
+    src/python_bindings.cpp:300-318)."""
+
+    rpm: float = 0.0
+    temperature: float = 293.15
+    mistuning: list = field(default_factory=list)
+
+    def __repr__(self):
+        return f"<ParametricCondition rpm={self.rpm:f} T={self.temperature:f}K mistuning={len(self.mistuning)} blades>"
+
+
 class CyclicSymmetrySolver:
     """GPU cyclic-symmetry modal solver for one sector mesh and material."""
 
@@ -119,6 +132,24 @@ class CyclicSymmetrySolver:
             if progress_cb is not None:
                 progress_cb(dict(completed=len(out), total=nres.value, harmonic_k=r.harmonic_index,
                                  converged=r.converged, num_modes=m))
+        return out
+
+    def solve_parametric(self, conditions, num_modes_per_harmonic: int, harmonic_indices=(), max_threads: int = 0,
+                         include_coriolis: bool = False, min_frequency: float = 0.0, allow_condensation: bool = False,
+                         memory_reserve_fraction: float = 0.2, progress_cb=None) -> list[list[ModalResult]]:
+        """One result list per condition, in order (src/cyclic_solver.cpp:1375-1485).  The
+        reference scales K_base by E(T) / E_ref and projects it, but the solve_at_rpm it then
+        calls rebuilds K_eff from the unscaled K_base and projects again (:737-820).  So each
+        condition's result is solve_at_rpm(condition.rpm), and temperature and mistuning have no
+        effect; this mirror returns the same.  progress_cb gets one call per condition
+        (harmonic_k = -1)."""
+        out = []
+        for i, cond in enumerate(conditions):
+            out.append(self.solve_at_rpm(float(cond.rpm), num_modes_per_harmonic, harmonic_indices, max_threads,
+                                         include_coriolis, min_frequency, None, allow_condensation,
+                                         memory_reserve_fraction))
+            if progress_cb is not None:
+                progress_cb(dict(completed=i + 1, total=len(conditions), harmonic_k=-1, converged=True, num_modes=0))
         return out
 
     def solve_rpm_sweep(self, rpm_values, num_modes_per_harmonic: int, harmonic_indices=(), max_threads: int = 0,
