@@ -1,0 +1,114 @@
+"""The reference's own rotating-frame and Coriolis test cases replayed on the oracle (CPU), with the
+product's host-side result consumers (turbomodal_gb300.solver.compute_stationary_frame) where the
+reference test uses them.
+
+Sources: tests/test_cyclic.cpp:539-720 (Coriolis cases) and tests/test_rotating.cpp (whirl
+labels, rotating-frame frequencies, stationary-frame ordering), all on the reference's wedge
+fixture with E = 200 GPa, nu = 0.3, rho = 7850 kg/m^3 and 24 sectors.
+"""
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from conftest import load_fixture
+
+MAT = dict(E=200e9, nu=0.3, rho=7850.0)
+
+
+@pytest.fixture(scope="module")
+def wedge():
+    return load_fixture("wedge_sector", 24)
+
+
+@pytest.fixture(scope="module")
+def model(oracle, wedge):
+    from turbomodal_gb300.meshgen import Material
+
+    return oracle.OracleModel(wedge, Material(**MAT))
+
+
+def by_k(results):
+    return {r["harmonic_index"]: r for r in results}
+
+
+def test_whirl_labels_without_coriolis(model, wedge):
+    """test_cyclic.cpp:539-563 (CoriolisOffMatchesBaseline), test_rotating.cpp FWBWSplittingAtNonzeroRPM
+    and StandingWavesAtK0: standing harmonics (k = 0, N/2) carry whirl 0; the degenerate ones
+    carry +1 / -1 pairs."""
+    res = model.solve(5000.0, 5, max_threads=4)
+    assert len(res) == wedge.num_sectors // 2 + 1
+    for r in res:
+        k = r["harmonic_index"]
+        w = r["whirl_direction"]
+        if k == 0 or 2 * k == wedge.num_sectors:
+            assert np.all(w == 0)
+        else:
+            assert np.all(w != 0) and (w == 1).any() and (w == -1).any()
+
+
+def test_coriolis_k0_uses_standard_path(model):
+    """test_cyclic.cpp:565-577: k = 0 with Coriolis is solved by the standard path (whirl 0)."""
+    r = model.solve(5000.0, 5, harmonic_indices=[0], max_threads=4, include_coriolis=True)
+    assert len(r) == 1 and r[0]["harmonic_index"] == 0 and np.all(r[0]["whirl_direction"] == 0)
+
+
+def test_coriolis_at_rest_is_no_coriolis(model):
+    """test_cyclic.cpp:579-597: at 0 rpm the Coriolis flag changes nothing (1e-6 Hz)."""
+    a = model.solve(0.0, 5, harmonic_indices=[3], max_threads=4)
+    b = model.solve(0.0, 5, harmonic_indices=[3], max_threads=4, include_coriolis=True)
+    n = min(len(a[0]["frequencies"]), len(b[0]["frequencies"]))
+    assert n > 0
+    assert np.max(np.abs(a[0]["frequencies"][:n] - b[0]["frequencies"][:n])) <= 1e-6
+
+
+def test_coriolis_splits_forward_and_backward(model):
+    """test_cyclic.cpp:599-642: at 10000 rpm with Coriolis, k = 3 has forward and backward modes and
+    the first forward rotating-frame frequency exceeds the first backward one."""
+    r = model.solve(10000.0, 10, harmonic_indices=[3], max_threads=4, include_coriolis=True)
+    assert len(r) == 1 and r[0]["harmonic_index"] == 3
+    w, f = r[0]["whirl_direction"], r[0]["frequencies"]
+    assert (w == 1).any() and (w == -1).any()
+    assert f[w == 1][0] > f[w == -1][0]
+
+
+def test_gyroscopic_projection(oracle, wedge, model):
+    """test_cyclic.cpp:678-720: G is skew-symmetric and its direct projection T(3)^H G T(3) is
+    skew-Hermitian (1e-10 of its norm).  The solver's own G_k = Gc + P Gp + conj(P) Gp^H
+    (src/cyclic_solver.cpp:987), which the reference's QEP uses, is not: the split sum takes the
+    (right, non-right) block as the transpose of the (non-right, right) block, which holds for the
+    symmetric K and M but flips sign for the skew G."""
+    G = model.matrix("G")
+    assert abs(G + G.T).max() <= 1e-10 * sp.linalg.norm(G)
+    T = model.matrix("T", k=3)
+    Gd = (T.conj().T @ G.astype(complex) @ T).tocsc()
+    assert abs(Gd + Gd.conj().T).max() <= 1e-10 * sp.linalg.norm(Gd)
+    model.prepare(10000.0, True)
+    Gk = model.matrix("Gk", k=3)
+    assert sp.linalg.norm(Gk + Gk.conj().T) > 0.1 * sp.linalg.norm(Gk)
+
+
+def test_stationary_frame_forward_above_backward(model, wedge):
+    """test_rotating.cpp FWGreaterThanBWInStationaryFrame: for every degenerate harmonic at 5000 rpm,
+    the highest forward stationary-frame frequency exceeds the lowest backward one."""
+    from turbomodal_gb300.solver import ModalResult, compute_stationary_frame
+
+    for r in model.solve(5000.0, 3, max_threads=4):
+        k = r["harmonic_index"]
+        if not (0 < k < wedge.num_sectors // 2):
+            continue
+        mr = ModalResult(k, r["rpm"], r["frequencies"], r["mode_shapes"], r["whirl_direction"], r["converged"])
+        sf = compute_stationary_frame(mr, wedge.num_sectors)
+        fw = sf.frequencies[sf.whirl_direction == 1]
+        bw = sf.frequencies[sf.whirl_direction == -1]
+        if len(fw) and len(bw):
+            assert fw.max() > bw.min()
+
+
+def test_frequencies_change_with_speed(model):
+    """test_rotating.cpp FrequenciesChangeWithRPM: k = 0 frequencies at 10000 rpm differ from 0 rpm."""
+    a = by_k(model.solve(0.0, 3, harmonic_indices=[0], max_threads=4))[0]["frequencies"]
+    b = by_k(model.solve(10000.0, 3, harmonic_indices=[0], max_threads=4))[0]["frequencies"]
+    n = min(len(a), len(b))
+    assert n >= 1
+    assert np.max(np.abs(a[:n] - b[:n]) / a[:n]) > 1e-6
