@@ -1,0 +1,105 @@
+"""The reference's mesh test cases (tests/test_mesh.cpp) on the product's host-side sector mesh
+(turbomodal_gb300.mesh.Mesh: gmsh v2 reader, cyclic boundary identification, node matching).
+
+The wedge fixture is the reference's tests/test_data/wedge_sector.msh converted by
+tests/golden/make_fixtures.py: an annular sector R = 0.05..0.15 m, 15 degrees, 0.01 m thick."""
+
+import math
+
+import numpy as np
+import pytest
+
+from conftest import load_fixture
+
+
+@pytest.fixture(scope="module")
+def wedge():
+    return load_fixture("wedge_sector", 24)
+
+
+def test_boundary_nodes_on_their_planes(wedge):
+    """LeftBoundaryNodesAtThetaZero, RightBoundaryNodesAtThetaAlpha."""
+    left = wedge.find_node_set("left_boundary").node_ids
+    right = wedge.find_node_set("right_boundary").node_ids
+    assert np.abs(wedge.nodes[left, 1]).max() <= 1e-10
+    theta = np.arctan2(wedge.nodes[right, 1], wedge.nodes[right, 0])
+    assert np.abs(theta - math.pi / 12).max() <= 1e-6
+
+
+def test_matched_pairs_same_radius_same_z_unique(wedge):
+    """MatchBoundaryNodes, MatchBoundaryNodesSameRadii, MatchBoundaryNodesSameZ,
+    MatchBoundaryNodesUniquePairs."""
+    pairs = np.asarray(wedge.matched_pairs)
+    assert len(pairs) > 0
+    X = wedge.nodes
+    rl = np.hypot(X[pairs[:, 0], 0], X[pairs[:, 0], 1])
+    rr = np.hypot(X[pairs[:, 1], 0], X[pairs[:, 1], 1])
+    assert np.abs(rl - rr).max() <= 1e-8
+    assert np.abs(X[pairs[:, 0], 2] - X[pairs[:, 1], 2]).max() <= 1e-10
+    assert len(set(pairs[:, 0])) == len(pairs) and len(set(pairs[:, 1])) == len(pairs)
+
+
+def test_boundary_errors(wedge):
+    """IdentifyCyclicBoundariesThrowsWithoutGroups, MatchBoundaryNodesThrowsWithoutSectors,
+    MatchBoundaryNodesThrowsWithoutIdentify."""
+    from turbomodal_gb300.mesh import Mesh, NodeSet
+
+    with pytest.raises(RuntimeError):
+        Mesh().identify_cyclic_boundaries()
+    m = Mesh()
+    m.nodes, m.elements = wedge.nodes, wedge.elements
+    m.node_sets = [NodeSet(s.name, list(s.node_ids)) for s in wedge.node_sets]
+    m.identify_cyclic_boundaries()
+    with pytest.raises(RuntimeError):
+        m.match_boundary_nodes()          # num_sectors not set
+    m2 = Mesh()
+    m2.nodes, m2.elements, m2.node_sets, m2.num_sectors = wedge.nodes, wedge.elements, m.node_sets, 24
+    with pytest.raises(RuntimeError):
+        m2.match_boundary_nodes()         # boundaries not identified
+
+
+def test_find_node_set(wedge):
+    """FindNodeSetReturnsNullForMissing, FindNodeSetReturnsCorrectSet."""
+    assert wedge.find_node_set("nonexistent") is None
+    s = wedge.find_node_set("left_boundary")
+    assert s is not None and s.name == "left_boundary" and len(s.node_ids) > 0
+
+
+@pytest.mark.parametrize("header", [None, "4.1 0 8", "2.2 1 8"])
+def test_loader_errors(tmp_path, header):
+    """LoadThrowsForMissingFile, LoadThrowsForInvalidFormat, LoadThrowsForBinaryFormat."""
+    from turbomodal_gb300.mesh import Mesh
+
+    p = tmp_path / "m.msh"
+    if header is not None:
+        p.write_text("$MeshFormat\n" + header + "\n$EndMeshFormat\n")
+    with pytest.raises(RuntimeError):
+        Mesh().load_from_gmsh(str(p))
+
+
+def test_loader_rejects_unknown_node(tmp_path):
+    """An element naming a node the file does not define (src/mesh.cpp:131-134)."""
+    from turbomodal_gb300.mesh import Mesh
+
+    p = tmp_path / "m.msh"
+    p.write_text("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n1\n1 0 0 0\n$EndNodes\n"
+                 "$Elements\n1\n1 15 2 1 1 7\n$EndElements\n")
+    with pytest.raises(RuntimeError):
+        Mesh().load_from_gmsh(str(p))
+
+
+def test_element_volumes_and_total_volume(oracle, wedge):
+    """ElementVolumesPositive, TotalVolumeApproxCorrect: every corner tetrahedron has positive volume
+    and the sector volume, from the consistent mass matrix (sum of its x-x block = rho V), is the
+    annular-sector volume within 5 %."""
+    from turbomodal_gb300.meshgen import Material
+
+    X = wedge.nodes[wedge.elements[:, :4]]
+    vol = np.einsum("ij,ij->i", np.cross(X[:, 1] - X[:, 0], X[:, 2] - X[:, 0]), X[:, 3] - X[:, 0]) / 6
+    assert np.all(vol > 0)
+    rho = 7850.0
+    M = oracle.OracleModel(wedge, Material(200e9, 0.3, rho)).matrix("M").tocoo()
+    sel = (M.row % 3 == 0) & (M.col % 3 == 0)
+    V = M.data[sel].sum() / rho
+    V_ref = 0.5 * (0.15 ** 2 - 0.05 ** 2) * (math.pi / 12) * 0.01
+    assert abs(V - V_ref) <= 0.05 * V_ref

@@ -84,8 +84,11 @@ class Mesh:
         gmsh_to_local = {}
         tets = []
         node_set_map: dict[str, set] = {}
-        with open(filename, "r") as fh:
-            lines = [ln.rstrip("\r\n") for ln in fh]
+        try:
+            with open(filename, "r") as fh:
+                lines = [ln.rstrip("\r\n") for ln in fh]
+        except OSError:
+            raise RuntimeError(f"Cannot open mesh file: {filename}") from None
         i = 0
         while i < len(lines):
             line = lines[i]
@@ -123,7 +126,11 @@ class Mesh:
                     nn = _GMSH_NODE_COUNT.get(etype, -1)
                     if nn < 0:
                         raise RuntimeError(f"Unknown Gmsh element type: {etype}")
-                    enodes = [gmsh_to_local[g] for g in parts[3 + ntags:3 + ntags + nn]]
+                    enodes = []
+                    for g in parts[3 + ntags:3 + ntags + nn]:
+                        if g not in gmsh_to_local:
+                            raise RuntimeError(f"Element references unknown node ID: {g}")
+                        enodes.append(gmsh_to_local[g])
                     if etype == 11:
                         p = np.asarray(node_list, dtype=np.float64)
                         mid13 = 0.5 * (p[enodes[1]] + p[enodes[3]])
