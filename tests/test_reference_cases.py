@@ -2,9 +2,10 @@
 product's host-side result consumers (turbomodal_gb300.solver.compute_stationary_frame) where the
 reference test uses them.
 
-Sources: tests/test_cyclic.cpp:539-720 (Coriolis cases) and tests/test_rotating.cpp (whirl
-labels, rotating-frame frequencies, stationary-frame ordering), all on the reference's wedge
-fixture with E = 200 GPa, nu = 0.3, rho = 7850 kg/m^3 and 24 sectors.
+Sources: tests/test_cyclic.cpp:539-720 (Coriolis cases), tests/test_rotating.cpp (whirl labels,
+rotating-frame frequencies, stationary-frame ordering) and tests/test_solver.cpp (M-orthogonality,
+determinism), all on the reference's wedge fixture with E = 200 GPa, nu = 0.3, rho = 7850 kg/m^3
+and 24 sectors.
 """
 
 import numpy as np
@@ -112,3 +113,30 @@ def test_frequencies_change_with_speed(model):
     n = min(len(a), len(b))
     assert n >= 1
     assert np.max(np.abs(a[:n] - b[:n]) / a[:n]) > 1e-6
+
+
+def hub_clamped(model, wedge):
+    """The wedge's K and M with the hub nodes' DOFs removed (ModalSolver::eliminate_dofs,
+    src/modal_solver.cpp:314-360), no cyclic constraint."""
+    hub = wedge.find_node_set("hub_constraint").node_ids
+    fixed = set(3 * n + c for n in hub for c in range(3))
+    keep = np.array([d for d in range(wedge.num_dof()) if d not in fixed])
+    K = model.matrix("K").tocsc()[keep][:, keep]
+    M = model.matrix("M").tocsc()[keep][:, keep]
+    return sp.csc_matrix(K), sp.csc_matrix(M)
+
+
+def test_wedge_modes_m_orthogonal_and_deterministic(oracle, model, wedge):
+    """tests/test_solver.cpp WedgeSectorMOrthogonality and SolverDeterministic: ten modes of the
+    hub-clamped wedge are M-orthogonal (1e-6 of the geometric mean of their M-norms) and two solves
+    give bit-identical eigenvalues (the reference allows 1e-15)."""
+    K, M = hub_clamped(model, wedge)
+    ev1, V, info = oracle.lanczos(K, M, 10, shift=1.0, maxit=1000)
+    ev2, _, _ = oracle.lanczos(K, M, 10, shift=1.0, maxit=1000)
+    assert info[1] == 1 and len(ev1) >= 5
+    assert np.array_equal(ev1, ev2)
+    G = V.conj().T @ (M @ V)
+    d = np.real(np.diag(G))
+    assert np.all(d > 0)
+    off = np.abs(G - np.diag(np.diag(G)))
+    assert np.all(off <= 1e-6 * np.sqrt(np.outer(d, d)))
