@@ -3,7 +3,10 @@
 // every launch item with the index arithmetic of the device kernels (mf.cu: k_inv_*,
 // k_fwd_gather, k_fwd_tri, k_fwd_rect, k_bwd_rect, k_bwd_tri) with bounds checks, and compares
 // the result with a plain column-by-column supernodal solve on the same random unit-lower L and
-// positive D.  Prints "max_rel_err=<e> bounds_errors=<k> launches=<n>".
+// positive D, and checks every column's fill against the rows its front stores.  Optional
+// arguments: supernode relaxation and its width limit (analyze()).  Prints
+// "max_rel_err=<e> bounds_errors=<k> launches=<n> supernodes=<s> struct_errors=<f>".
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -30,7 +33,9 @@ int main(int argc, char** argv) {
     if (std::fread(P.i.data(), 4, hdr[1], f) != (size_t)hdr[1]) return 2;
     std::fclose(f);
     const int NB = 64, RR = 64, CH = 2048;
-    const Symbolic S = analyze(P, 0.0, 0);
+    const double relax = argc > 2 ? std::atof(argv[2]) : 0.0;
+    const int relax_w = argc > 3 ? std::atoi(argv[3]) : 0;
+    const Symbolic S = analyze(P, relax, relax_w);
     std::vector<int32_t> items;
     const SolvePlan plan = build_solve_plan(S, NB, RR, items);
     const int ns = S.ns, n = S.n;
@@ -220,6 +225,44 @@ int main(int argc, char** argv) {
         err = std::max(err, std::fabs(x[i] - xr[i]));
         sc = std::max(sc, std::fabs(xr[i]));
     }
-    std::printf("max_rel_err=%.3e bounds_errors=%ld launches=%ld supernodes=%d\n", err / sc, nerr, launches, ns);
+    // independent structure check: the fill of every factor column (its lower pattern in factor
+    // numbering united with its children's structures, children taken from that fill) must be
+    // inside the rows its supernode's front stores
+    long struct_errors = 0;
+    int64_t fill = 0;
+    {
+        std::vector<std::vector<int32_t>> col(n);
+        for (int32_t c = 0; c < P.ncols; c++)
+            for (int64_t q = P.p[c]; q < P.p[c + 1]; q++) {
+                const int32_t i = S.iperm[P.i[q]], j = S.iperm[c];
+                if (i != j) col[std::min(i, j)].push_back(std::max(i, j));
+            }
+        std::vector<std::vector<int32_t>> kids(n);
+        std::vector<int32_t> col2sn(n);
+        for (int s2 = 0; s2 < ns; s2++)
+            for (int j = S.sn_first[s2]; j < S.sn_first[s2 + 1]; j++) col2sn[j] = s2;
+        std::vector<char> in_front(n, 0);
+        for (int j = 0; j < n; j++) {
+            std::vector<int32_t> st = col[j];
+            for (int32_t c : kids[j])   // children precede j in factor numbering: col[c] is complete
+                for (int32_t r : col[c])
+                    if (r > j) st.push_back(r);
+            std::sort(st.begin(), st.end());
+            st.erase(std::unique(st.begin(), st.end()), st.end());
+            col[j] = st;
+            fill += (int64_t)st.size();
+            if (!st.empty()) kids[st[0]].push_back(j);
+            const int s2 = col2sn[j];
+            const int32_t* rows = &S.sn_rows[S.sn_row_ptr[s2]];
+            const int64_t h = S.sn_row_ptr[s2 + 1] - S.sn_row_ptr[s2];
+            for (int64_t r = 0; r < h; r++) in_front[rows[r]] = 1;
+            for (int32_t r : st)
+                if (!in_front[r]) struct_errors++;
+            for (int64_t r = 0; r < h; r++) in_front[rows[r]] = 0;
+        }
+    }
+    if (fill != S.nnz_l) struct_errors++;   // the recomputed fill must be the analysis's nnz(L)
+    std::printf("max_rel_err=%.3e bounds_errors=%ld launches=%ld supernodes=%d struct_errors=%ld\n", err / sc, nerr,
+                launches, ns, struct_errors);
     return 0;
 }
