@@ -103,3 +103,53 @@ def test_element_volumes_and_total_volume(oracle, wedge):
     V = M.data[sel].sum() / rho
     V_ref = 0.5 * (0.15 ** 2 - 0.05 ** 2) * (math.pi / 12) * 0.01
     assert abs(V - V_ref) <= 0.05 * V_ref
+
+
+def _match(mesh_factory, brute, monkeypatch):
+    import turbomodal_gb300.mesh as tm
+
+    monkeypatch.setattr(tm, "KDTREE_MIN_RIGHT", 10 ** 9 if brute else 0)
+    m = mesh_factory()
+    return m.matched_pairs, m.free_boundary, m.left_boundary, m.right_boundary
+
+
+@pytest.mark.parametrize("case", ["wedge", "blade", "config1", "perturbed"])
+def test_kdtree_matching_equals_full_scan(case, monkeypatch):
+    """The k-d tree candidate search gives the pairs, the free boundary and the boundary lists of
+    the reference's full scan (src/mesh.cpp:260-351), also with near-ties and with nodes moved
+    beyond the tolerance."""
+    from turbomodal_gb300.mesh import Mesh, NodeSet
+    from turbomodal_gb300.meshgen import config_mesh
+
+    def factory():
+        if case == "wedge":
+            return load_fixture("wedge_sector", 24)
+        if case == "blade":
+            return load_fixture("blade_sector", 24)
+        base = config_mesh(1) if case == "config1" else load_fixture("leissa_disk_sector", 24)
+        if case == "config1":
+            return base
+        # perturbed copy: right-boundary nodes moved by 0.3x / 3x the tolerance, some duplicated
+        # positions (ties) added as extra right nodes
+        rng = np.random.default_rng(5)
+        m = Mesh()
+        X = base.nodes.copy()
+        right = list(base.find_node_set("right_boundary").node_ids)
+        left = list(base.find_node_set("left_boundary").node_ids)
+        for i, nid in enumerate(right):
+            r = math.hypot(X[nid, 0], X[nid, 1])
+            tol = max(1e-6, 1e-4 * r)
+            X[nid] += rng.standard_normal(3) * (0.3 if i % 3 else 3.0) * tol / math.sqrt(3)
+        dup = right[::7]
+        X = np.vstack([X, X[dup]])
+        extra = list(range(len(base.nodes), len(base.nodes) + len(dup)))
+        sets = [NodeSet(s.name, list(s.node_ids)) for s in base.node_sets if s.name not in ("left_boundary",
+                                                                                           "right_boundary")]
+        sets += [NodeSet("left_boundary", left), NodeSet("right_boundary", right + extra)]
+        m.load_from_arrays(X, base.elements, sets, 24)
+        return m
+
+    full, tree = _match(factory, True, monkeypatch), _match(factory, False, monkeypatch)
+    assert full == tree and len(full[0]) > 0
+    if case == "perturbed":
+        assert len(full[1]) > 0          # some nodes moved beyond the tolerance stay free

@@ -24,6 +24,7 @@ class NodeSet:
 
 
 _GMSH_NODE_COUNT = {1: 2, 2: 3, 3: 4, 4: 4, 5: 8, 8: 3, 9: 6, 11: 10, 15: 1}
+KDTREE_MIN_RIGHT = 64   # right-boundary size above which matching queries a k-d tree
 
 
 class Mesh:
@@ -167,6 +168,8 @@ class Mesh:
         Left nodes are visited in order; each takes the closest unused right node
         (first index wins ties, as the reference's strict ``<``).  Pairs farther
         apart than max(1e-6, 1e-4 * r_left) leave both nodes on the free boundary.
+        The reference scans every right node per left node, O(L R); above 64 right
+        nodes the candidates come from a k-d tree ball query with the same result.
         """
         if self.num_sectors <= 0:
             raise RuntimeError("num_sectors must be set before matching boundary nodes.")
@@ -182,20 +185,35 @@ class Mesh:
         r1_rot = cos_a * r1 - sin_a * r2
         r2_rot = sin_a * r1 + cos_a * r2
         used = np.zeros(len(right), dtype=bool)
+        # Only right nodes within the tolerance can be accepted, so the closest unused node is
+        # taken from a ball query (k-d tree) instead of a scan of every right node: the pair,
+        # or the rejection, is the one the full scan gives (same distance formula, first index
+        # on ties).
+        tree = None
+        if len(right) > KDTREE_MIN_RIGHT:
+            from scipy.spatial import cKDTree
+            tree = cKDTree(np.column_stack([r1_rot, r2_rot, rax]))
         new_left, new_right, free_left, pairs = [], [], [], []
         for left_id in self.left_boundary:
             l1 = self.nodes[left_id, c1]
             l2 = self.nodes[left_id, c2]
             lax = self.nodes[left_id, cax]
-            d1 = l1 - r1_rot
-            d2 = l2 - r2_rot
-            dax = lax - rax
-            dist = np.sqrt(d1 * d1 + d2 * d2 + dax * dax)
-            dist = np.where(used, np.inf, dist)
-            best = int(np.argmin(dist)) if len(dist) else -1
             r_ref = math.sqrt(l1 * l1 + l2 * l2)
             tol = max(1e-6, 1e-4 * r_ref)
-            if best < 0 or not np.isfinite(dist[best]) or dist[best] > tol:
+            cand = (np.arange(len(right)) if tree is None else
+                    np.sort(np.asarray(tree.query_ball_point([l1, l2, lax], tol * (1.0 + 1e-9) + 1e-300),
+                                       dtype=np.int64)))
+            cand = cand[~used[cand]]
+            best = -1
+            if len(cand):
+                d1 = l1 - r1_rot[cand]
+                d2 = l2 - r2_rot[cand]
+                dax = lax - rax[cand]
+                dist = np.sqrt(d1 * d1 + d2 * d2 + dax * dax)
+                q = int(np.argmin(dist))
+                if dist[q] <= tol:
+                    best = int(cand[q])
+            if best < 0:
                 free_left.append(int(left_id))
                 continue
             used[best] = True
