@@ -148,6 +148,24 @@ def harmonics_arg(a):
     return [] if a == "all" else [int(x) for x in a.split(",")]
 
 
+def count_distinct_verified(mixed, fp64, tol=1e-6):
+    """Verified eigenpairs counting each degenerate (x, conj x) pair once.  On the standard path a
+    harmonic 0 < k < N/2 returns every eigenpair twice, at positions 2q and 2q+1 with the same
+    frequency (src/cyclic_solver.cpp:1162-1183); standing harmonics (whirl 0) return distinct
+    ones."""
+    ref = {r.harmonic_index: np.asarray(r.frequencies) for r in fp64}
+    n = 0
+    for r in mixed:
+        f = np.asarray(r.frequencies)
+        g = ref.get(r.harmonic_index)
+        if g is None or len(g) != len(f) or not r.converged:
+            continue
+        ok = np.abs(f - g) <= tol * np.maximum(np.abs(g), 1e-300)
+        paired = len(f) > 0 and bool(np.all(np.asarray(r.whirl_direction) != 0))
+        n += int(np.sum(ok[0::2])) if paired else int(np.sum(ok))
+    return n
+
+
 def count_verified(mixed, fp64, tol=1e-6):
     ref = {r.harmonic_index: np.asarray(r.frequencies) for r in fp64}
     n_ok = n_all = 0
@@ -268,10 +286,12 @@ def main():
     barrier(pg)
     # verification against the plain FP64 GPU path (untimed) and its own throughput
     n_ok = n_all = 0
+    n_distinct = None
     worst = 0.0
     fp64_ms = 0.0
     fp64_pairs = 0
     if not args.no_verify:
+        n_distinct = 0
         for rpm, res in zip(timed, results):
             ref = solver.solve_at_rpm(rpm, args.num_modes, hi, precision="fp64")
             fp64_ms += solver.last_timing()["device_ms"]
@@ -279,6 +299,7 @@ def main():
             a, b, w = count_verified(res, ref)
             n_ok += a
             n_all += b
+            n_distinct += count_distinct_verified(res, ref)
             worst = max(worst, w)
     else:
         n_ok = n_all = sum(len(r.frequencies) for res in results for r in res)
@@ -309,6 +330,8 @@ def main():
     t_dev = max_over_ranks(pg, sum(dev_ms) / 1e3)
     t_wall = max_over_ranks(pg, sum(wall_s))
     tot_ok = sum_over_ranks(pg, n_ok)
+    tot_all = sum_over_ranks(pg, n_all)
+    tot_distinct = sum_over_ranks(pg, n_distinct or 0)
     serving = None
     if rank == 0 and not args.no_serve:
         # served request stream (Poisson arrivals, mixed sizes, admission by memory budget)
@@ -336,7 +359,8 @@ def main():
             "config": {"workload": WORKLOAD, "harmonics": args.harmonics, "num_modes": args.num_modes,
                        "speeds": [float(r) for r in timed], "parallelism": f"replicas x{ws} (speeds sharded)",
                        "l2": "inputs larger than L2 (no flush needed)"},
-            "eigenpairs": {"verified": int(n_ok), "returned": int(n_all), "worst_rel_err_vs_fp64": worst},
+            "eigenpairs": {"verified": int(tot_ok), "returned": int(tot_all), "worst_rel_err_vs_fp64": worst,
+                           "distinct_verified": int(tot_distinct) if n_distinct is not None else None},
             "fp64_gpu": {"value": fp64_pairs / (fp64_ms / 1e3) if fp64_ms > 0 else None, "unit": UNIT,
                          "ms_per_step": fp64_ms / max(len(timed), 1)},
             "e2e": {"value": tot_ok / t_wall if t_wall > 0 else 0.0, "unit": UNIT,

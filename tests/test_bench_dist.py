@@ -52,3 +52,19 @@ def test_two_ranks_shard_and_reduce():
     assert all(r[1] == 2 for r in res)
     assert all(r[3] == 2.5 for r in res)                       # max over ranks
     assert all(r[4] == float(len(bench.RPMS)) for r in res)   # sum over ranks
+
+
+def test_distinct_verified_counts_each_pair_once():
+    """Degenerate harmonics return every eigenpair twice (positions 2q, 2q+1); standing ones once."""
+    import bench
+
+    class R:
+        def __init__(self, k, f, w, conv=True):
+            self.harmonic_index, self.frequencies, self.whirl_direction, self.converged = k, np.array(f), np.array(w), conv
+
+    ref = [R(0, [10.0, 20.0, 30.0], [0, 0, 0]), R(1, [11.0, 11.0, 21.0, 21.0, 31.0], [1, -1, 1, -1, 1]),
+           R(2, [12.0, 12.0], [1, -1])]
+    mix = [R(0, [10.0, 20.0, 30.5], [0, 0, 0]), R(1, [11.0, 11.0, 21.0, 21.0, 31.0], [1, -1, 1, -1, 1]),
+           R(2, [12.0, 12.0], [1, -1], conv=False)]
+    assert bench.count_distinct_verified(mix, ref) == 2 + 3
+    assert bench.count_verified(mix, ref)[0] == 2 + 5
