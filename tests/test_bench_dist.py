@@ -68,3 +68,21 @@ def test_distinct_verified_counts_each_pair_once():
            R(2, [12.0, 12.0], [1, -1], conv=False)]
     assert bench.count_distinct_verified(mix, ref) == 2 + 3
     assert bench.count_verified(mix, ref)[0] == 2 + 5
+
+
+def test_reference_arm_prints_its_line():
+    """bench.py --impl reference (the reference's CPU algorithm, timed on the host cores) prints one
+    JSON line with the contract's keys; it needs no GPU."""
+    import json
+    import subprocess
+    import sys
+
+    from conftest import ROOT
+
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0"],
+                         cwd=ROOT, check=True, capture_output=True, text=True, timeout=600).stdout
+    line = json.loads(out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["higher_is_better"] is True
+    assert line["e2e"]["value"] == line["value"] and line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["metric"] and line["unit"] and line["config"]["workload"]
