@@ -422,6 +422,12 @@ struct tmg_context {
     std::vector<int64_t> gpT;
     Pattern GpfH;
     UnionMaps WG0;
+    // Refinement deflation across the speeds of a sweep (off unless the environment sets
+    // TMG_DEFLATE when the context is created): the DEFL_M lowest eigenvectors of every complex
+    // harmonic from the last solve, valid while the operator pattern keeps `recycle_key`.
+    bool deflate = false;
+    std::string recycle_key;
+    std::map<int, DVec<zd>> recycle;
     struct Qep {
         DVec<int64_t> sk, sm, sg, sk2, sm2, sg2;
         DVec<int8_t> blk, blk2;
@@ -1125,6 +1131,26 @@ __global__ void k_ir_update(int64_t n, T* __restrict__ x, const T* __restrict__ 
     x[p * n + i] += d[p * n + i];
 }
 
+// y[p] = sgn * Einv[p] h[p] for the m x m (column-major) matrix of every problem (deflation)
+template <typename T>
+__global__ void k_small_mv(int m, const T* __restrict__ Einv, const T* __restrict__ h, T* __restrict__ y, double sgn) {
+    const int64_t p = blockIdx.x;
+    const int i = threadIdx.x;
+    if (i >= m) return;
+    T acc = zero_of<T>();
+    for (int j = 0; j < m; j++) acc += Einv[p * m * m + (int64_t)j * m + i] * h[p * m + j];
+    y[p * m + i] = sgn * acc;
+}
+
+inline std::complex<double> to_std(double v) { return {v, 0.0}; }
+inline std::complex<double> to_std(zd v) { return {v.x, v.y}; }
+template <typename T> T from_std(std::complex<double> v);
+template <> inline double from_std<double>(std::complex<double> v) { return v.real(); }
+template <> inline zd from_std<zd>(std::complex<double> v) { return zd{v.real(), v.imag()}; }
+
+// eigenvectors kept per complex harmonic to deflate the refinement at the next speed
+constexpr int DEFL_M = 8;
+
 // ---- shift-invert operator of a batch ----------------------------------------------------
 template <typename Tv, typename Tf>
 struct ShiftInvertB {
@@ -1146,6 +1172,11 @@ struct ShiftInvertB {
     std::vector<int> skip;        // problems finished or failed: refinement leaves them alone
     std::vector<std::string> failed;   // per problem: why its factorisation failed ("" = fine)
     int64_t solves = 0, applies = 0, max_its = 0;
+    // Deflation of the refinement CG (off unless set_deflation is called): W holds mdef vectors
+    // per problem (n x mdef, problem stride n * mdef), AW = A W, Einv = (W^H A W)^-1 per problem
+    // (mdef x mdef, column-major).
+    int mdef = 0;
+    DVec<Tv> W, AW, Einv, hdef, ydef, pdef;
     cudaGraphExec_t gexec = nullptr;
     int64_t launches_per_solve = 0;
     ~ShiftInvertB() { if (gexec) cudaGraphExecDestroy(gexec); }
@@ -1202,6 +1233,69 @@ struct ShiftInvertB {
         worst.assign(B, 0.0);
     }
     Batch<Tf> batch() const { return Batch<Tf>{B, L.p, nullptr, D->l_entries, 0}; }
+
+    // Deflate the CG of every later mixed apply with m vectors per problem (Wsrc: B x n x m,
+    // problem stride n * m), which should approximate the operator's lowest eigenvectors (the
+    // eigenvectors of the previous speed of a sweep).  Only for the CG path (every pivot positive).
+    void set_deflation(const Tv* Wsrc, int m) {
+        mdef = 0;
+        if (!mixed || !spd || m <= 0 || m > 32) return;
+        const int64_t nm = (int64_t)n * m;
+        W.alloc((size_t)B * nm);
+        AW.alloc((size_t)B * nm);
+        TMG_CUDA(cudaMemcpyAsync(W.p, Wsrc, (size_t)B * nm * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
+        lz_spmv<Tv>(c->st, B, A, W.p, nm, AW.p, nm, m, n);
+        pdef.alloc((size_t)B * m * LZ_DOT_BLOCKS);
+        hdef.alloc((size_t)B * m);
+        ydef.alloc((size_t)B * m);
+        // E = W^H A W column by column, inverted on the host (Gauss-Jordan, partial pivoting)
+        std::vector<std::complex<double>> E((size_t)B * m * m);
+        std::vector<Tv> col((size_t)B * m);
+        for (int v = 0; v < m; v++) {
+            lz_multidot<Tv>(c->st, B, n, W.p, nm, n, m, AW.p + (int64_t)v * n, nm, pdef.p, hdef.p);
+            TMG_CUDA(cudaMemcpyAsync(col.data(), hdef.p, col.size() * sizeof(Tv), cudaMemcpyDeviceToHost, c->st));
+            TMG_CUDA(cudaStreamSynchronize(c->st));
+            for (int p = 0; p < B; p++)
+                for (int k = 0; k < m; k++) E[((size_t)p * m + v) * m + k] = to_std(col[(size_t)p * m + k]);
+        }
+        std::vector<Tv> inv((size_t)B * m * m);
+        for (int p = 0; p < B; p++) {
+            std::vector<std::complex<double>> a(E.begin() + (size_t)p * m * m, E.begin() + (size_t)(p + 1) * m * m);
+            std::vector<std::complex<double>> x((size_t)m * m, 0.0);
+            for (int i = 0; i < m; i++) x[(size_t)i * m + i] = 1.0;
+            for (int c0 = 0; c0 < m; c0++) {
+                int piv = c0;
+                for (int r = c0 + 1; r < m; r++)
+                    if (std::abs(a[(size_t)c0 * m + r]) > std::abs(a[(size_t)c0 * m + piv])) piv = r;
+                if (std::abs(a[(size_t)c0 * m + piv]) == 0.0) return;   // singular: no deflation
+                for (int j = 0; j < m; j++) {
+                    std::swap(a[(size_t)j * m + c0], a[(size_t)j * m + piv]);
+                    std::swap(x[(size_t)j * m + c0], x[(size_t)j * m + piv]);
+                }
+                const std::complex<double> d = a[(size_t)c0 * m + c0];
+                for (int j = 0; j < m; j++) { a[(size_t)j * m + c0] /= d; x[(size_t)j * m + c0] /= d; }
+                for (int r = 0; r < m; r++) {
+                    if (r == c0) continue;
+                    const std::complex<double> f = a[(size_t)c0 * m + r];
+                    if (f == 0.0) continue;
+                    for (int j = 0; j < m; j++) {
+                        a[(size_t)j * m + r] -= f * a[(size_t)j * m + c0];
+                        x[(size_t)j * m + r] -= f * x[(size_t)j * m + c0];
+                    }
+                }
+            }
+            for (size_t q = 0; q < (size_t)m * m; q++) inv[(size_t)p * m * m + q] = from_std<Tv>(x[q]);
+        }
+        Einv.upload(inv);
+        mdef = m;
+    }
+    // z -= W Einv (AW^H z) for every problem
+    void deflate(Tv* z) {
+        const int64_t nm = (int64_t)n * mdef;
+        lz_multidot<Tv>(c->st, B, n, AW.p, nm, n, mdef, z, n, pdef.p, hdef.p);
+        TMG_LAUNCH(k_small_mv<Tv>, B, 32, 0, c->st, mdef, Einv.p, hdef.p, ydef.p, 1.0);
+        lz_gemv_sub<Tv>(c->st, B, n, mdef, W.p, nm, ydef.p, mdef, z, n);
+    }
 
     // the permute / supernodal sweeps / permute sequence of one batched solve is captured
     // once into a CUDA graph over fixed buffers and replayed for every solve
@@ -1282,7 +1376,15 @@ struct ShiftInvertB {
             // CG on A x = b preconditioned by the FP32 factor; FP64 operator and vectors
             TMG_CUDA(cudaMemsetAsync(x, 0, (size_t)B * n * sizeof(Tv), c->st));
             lz_copy<Tv>(c->st, (int64_t)B * n, b, r.p);
+            if (mdef > 0) {   // deflated start x0 = W Einv W^H b, r0 = b - A x0
+                const int64_t nm = (int64_t)n * mdef;
+                lz_multidot<Tv>(c->st, B, n, W.p, nm, n, mdef, b, n, pdef.p, hdef.p);
+                TMG_LAUNCH(k_small_mv<Tv>, B, 32, 0, c->st, mdef, Einv.p, hdef.p, ydef.p, -1.0);
+                lz_gemv_sub<Tv>(c->st, B, n, mdef, W.p, nm, ydef.p, mdef, x, n);
+                lz_spmv<Tv>(c->st, B, A, x, n, r.p, n, 1, n, true);
+            }
             solve1(r.p, z.p);
+            if (mdef > 0) deflate(z.p);
             lz_copy<Tv>(c->st, (int64_t)B * n, z.p, pp.p);
             lz_multidot<Tv>(c->st, B, n, r.p, n, n, 1, z.p, n, d.p, sc.p);           // rz
             for (it = 1; it <= max_iter; it++) {
@@ -1291,6 +1393,7 @@ struct ShiftInvertB {
                 TMG_LAUNCH(k_pcg_xr<Tv>, dim3(nblk(n), B), 256, 0, c->st, n, x, r.p, pp.p, q.p, sc.p, sc.p + B, ddone.p);
                 if (check()) break;
                 solve1(r.p, z.p);
+                if (mdef > 0) deflate(z.p);
                 lz_multidot<Tv>(c->st, B, n, r.p, n, n, 1, z.p, n, d.p, sc.p + 2 * B);  // rz_new
                 TMG_LAUNCH(k_pcg_p<Tv>, dim3(nblk(n), B), 256, 0, c->st, n, pp.p, z.p, sc.p + 2 * B, sc.p, ddone.p);
                 TMG_CUDA(cudaMemcpyAsync(sc.p, sc.p + 2 * B, B * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
@@ -1593,7 +1696,8 @@ void finish_qep(tmg_context* c, const Problem& pr, const EigOut<zd>& eo, int num
 template <typename Tv, typename Tf>
 void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os, const UnionMaps& um,
                const Tv* vals_csc, const DevCsr<Tv>& M, int nev, int ncv, double shift, int max_restarts, bool mixed,
-               int num_modes, double min_frequency, const std::vector<double>* shifts = nullptr, bool qep = false) {
+               int num_modes, double min_frequency, const std::vector<double>* shifts = nullptr, bool qep = false,
+               const Tv* Wdef = nullptr, int mdef = 0) {
     cudaStream_t st = c->st;
     const int B = (int)probs.size();
     const int64_t nl = (int64_t)um.lower2csc.n, nU = um.U.nnz();
@@ -1609,6 +1713,7 @@ void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os
     auto t0 = std::chrono::steady_clock::now();
     op.factor(lower.p);
     lower.release();
+    if (Wdef && mdef > 0) op.set_deflation(Wdef, mdef);
     auto t1 = std::chrono::steady_clock::now();
     DVec<double> dsh;
     if (shifts) dsh.upload(*shifts);
@@ -1616,6 +1721,20 @@ void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os
     auto t2 = std::chrono::steady_clock::now();
     c->phase_ms[1] += std::chrono::duration<double, std::milli>(t1 - t0).count();
     c->phase_ms[2] += std::chrono::duration<double, std::milli>(t2 - t1).count();
+    if constexpr (std::is_same<Tv, zd>::value) {
+        if (c->deflate && !qep) {   // keep the lowest eigenvectors for the next speed
+            if (c->recycle_key != c->symC_key) {
+                c->recycle.clear();
+                c->recycle_key = c->symC_key;
+            }
+            for (int p = 0; p < B; p++)
+                if (eo[p].failed.empty() && eo[p].ne >= DEFL_M) {
+                    DVec<zd>& w = c->recycle[probs[p].k];
+                    w.alloc((size_t)op.n * DEFL_M);
+                    TMG_CUDA(cudaMemcpyAsync(w.p, eo[p].X.p, w.bytes(), cudaMemcpyDeviceToDevice, st));
+                }
+        }
+    }
     c->phase_ms[5] += (double)op.solves;
     c->phase_ms[6] += (double)op.applies;
     c->phase_ms[7] = std::max(c->phase_ms[7], (double)op.max_its);
@@ -1976,10 +2095,28 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
             DevCsr<zd> M;
             M.nrows = S.n_free; M.nnz = mu.U.nnz(); M.rowptr = mu.csr_rowptr.p; M.col = mu.csr_col.p; M.val = mcsr.p;
             M.vstride = mu.U.nnz();
+            // previous speed's eigenvectors of every harmonic of the batch, when all are kept
+            DVec<zd> Wd;
+            int md = 0;
+            if (mixed && c->deflate && c->recycle_key == c->symC_key) {
+                bool all = true;
+                for (const Problem& pr : grp) {
+                    auto it = c->recycle.find(pr.k);
+                    all = all && it != c->recycle.end() && it->second.n == (size_t)S.n_free * DEFL_M;
+                }
+                if (all) {
+                    const size_t nm = (size_t)S.n_free * DEFL_M;
+                    Wd.alloc((size_t)B * nm);
+                    for (int p = 0; p < B; p++)
+                        TMG_CUDA(cudaMemcpyAsync(Wd.p + p * nm, c->recycle[grp[p].k].p, nm * sizeof(zd),
+                                                 cudaMemcpyDeviceToDevice, st));
+                    md = DEFL_M;
+                }
+            }
             try {
                 if (mixed)
                     run_batch<zd, zf>(c, grp, c->symC, um, vals.p, M, nev, ncv, shift, 1000, true, num_modes,
-                                      min_frequency);
+                                      min_frequency, nullptr, false, md ? Wd.p : nullptr, md);
                 else
                     run_batch<zd, zd>(c, grp, c->symC, um, vals.p, M, nev, ncv, shift, 1000, false, num_modes,
                                       min_frequency);
@@ -2049,6 +2186,7 @@ int tmg_create(int device, size_t mem_budget_bytes, tmg_context** out) {
         }
     }
     c->budget = mem_budget_bytes ? mem_budget_bytes : (size_t)(0.9 * (double)device_free_bytes(device));
+    c->deflate = std::getenv("TMG_DEFLATE") != nullptr;
     *out = c;
     return TMG_OK;
 }
