@@ -140,3 +140,28 @@ def test_wedge_modes_m_orthogonal_and_deterministic(oracle, model, wedge):
     assert np.all(d > 0)
     off = np.abs(G - np.diag(np.diag(G)))
     assert np.all(off <= 1e-6 * np.sqrt(np.outer(d, d)))
+
+
+def test_wedge_assembly_cases(oracle, wedge):
+    """tests/test_assembler.cpp WedgeSectorDimensions, WedgeSectorMPositiveSemiDefinite,
+    WedgeSectorKNonNegativeEigenvalues, KScalesWithE, MScalesWithRho, MIndependentOfE (on the wedge
+    rather than one element)."""
+    from turbomodal_gb300.meshgen import Material
+
+    def km(E, rho):
+        om = oracle.OracleModel(wedge, Material(E, 0.3, rho))
+        return om.matrix("K").toarray(), om.matrix("M").toarray()
+
+    K, M = km(200e9, 7850.0)
+    ndof = wedge.num_dof()
+    assert K.shape == (ndof, ndof) and M.shape == (ndof, ndof)
+    em = np.linalg.eigvalsh(M)
+    ek = np.linalg.eigvalsh(K)
+    assert em.min() > -1e-10 * em.max()
+    assert ek.min() > -1e-6 * ek.max()
+    assert np.sum(np.abs(ek) <= 1e-9 * ek.max()) == 6       # six rigid-body modes of the free sector
+    K2, M2 = km(400e9, 7850.0)
+    assert np.allclose(K2, 2.0 * K, rtol=1e-10, atol=1e-10 * np.abs(K).max())
+    assert np.array_equal(M2, M)
+    _, M3 = km(200e9, 15700.0)
+    assert np.allclose(M3, 2.0 * M, rtol=1e-10, atol=0)
