@@ -228,3 +228,82 @@ def test_symbolic_valid(oracle, cfg0_mesh):
     assert np.all((parent == -1) | (parent > np.arange(n)))
     # fill of the AMD order is far below the natural order's
     assert cc.sum() < 0.5 * n * n / 2
+
+
+@pytest.mark.parametrize("X", [REF_TET, 3.0 * REF_TET + np.array([10.0, -5.0, 2.0]), skewed_tet()])
+def test_element_internal_force_from_constant_stress(oracle, X):
+    """InternalForceFromConstantStress (tests/test_element.cpp), against the closed form instead of
+    a second quadrature: for a straight-sided quadratic tetrahedron under constant stress sigma the
+    consistent nodal forces are zero at the corners and V (grad L_a + grad L_b) . sigma at the
+    mid-edge node of edge (a, b), L the barycentric coordinates."""
+    E, nu = STEEL.E, STEEL.nu
+    Ke = oracle.element(X, STEEL, 0)
+    eps = np.array([[1e-3, 1.5e-4, 1e-4], [1.5e-4, -2e-4, -0.5e-4], [1e-4, -0.5e-4, 5e-4]])   # symmetric strain
+    u = (X @ eps.T).ravel()                      # u_i = eps_ij x_j
+    lam, mu = E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))
+    sig = lam * np.trace(eps) * np.eye(3) + 2 * mu * eps
+    C = X[:4]
+    T = np.vstack([np.ones(4), C.T])             # barycentric: T @ L = [1, x, y, z]
+    G = np.linalg.inv(T)[:, 1:]                  # row a = grad L_a
+    V = abs(np.linalg.det(C[1:] - C[0])) / 6
+    f = (Ke @ u).reshape(10, 3)
+    scale = np.abs(f).max()
+    assert np.abs(f[:4]).max() <= 1e-9 * scale
+    for node, (a, b) in zip(range(4, 10), [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]):
+        assert np.abs(f[node] - V * sig @ (G[a] + G[b])).max() <= 1e-9 * scale
+
+
+@pytest.mark.parametrize("X", [REF_TET, skewed_tet()])
+def test_element_mass_closed_form(oracle, X):
+    """Consistent mass of a straight-sided quadratic tetrahedron in closed form: rho * integral of
+    N_a N_b with N = L_a (2 L_a - 1) at corners and 4 L_a L_b at mid-edges, integrated exactly by
+    integral(L0^a L1^b L2^c L3^d) = 6 V a! b! c! d! / (a + b + c + d + 3)!; the reference's 14-point
+    rule (src/element.cpp:36-69, :337-371) integrates this quartic exactly."""
+    from math import factorial
+
+    rho = STEEL.rho
+    Me = oracle.element(X, STEEL, 1)
+    V = abs(np.linalg.det(X[1:4] - X[0])) / 6
+
+    def poly(node):
+        e = [0, 0, 0, 0]
+        if node < 4:
+            e2 = list(e); e2[node] = 2
+            e1 = list(e); e1[node] = 1
+            return {tuple(e2): 2.0, tuple(e1): -1.0}
+        a, b = [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)][node - 4]
+        e[a] += 1; e[b] += 1
+        return {tuple(e): 4.0}
+
+    def integral(p, q):
+        s = 0.0
+        for ea, ca in p.items():
+            for eb, cb in q.items():
+                k = [x + y for x, y in zip(ea, eb)]
+                s += ca * cb * 6 * V * np.prod([factorial(x) for x in k]) / factorial(sum(k) + 3)
+        return s
+
+    ref = np.zeros((30, 30))
+    for a in range(10):
+        for b in range(10):
+            v = rho * integral(poly(a), poly(b))
+            for i in range(3):
+                ref[3 * a + i, 3 * b + i] = v
+    assert np.abs(Me - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_rotating_element_matrices_from_mass(oracle, axis):
+    """Spin softening and gyroscopic element matrices (src/rotating_effects.cpp:140-226) are the
+    consistent-mass integrals with (I - a a^T) and [a x]: K_omega = omega^2 P M P with P the
+    projector normal to the axis, and G = m (x) [a x] with m the scalar mass block."""
+    X = skewed_tet()
+    M = oracle.element(X, STEEL, 1)
+    w = 523.6
+    a = np.eye(3)[axis]
+    P = np.kron(np.eye(10), np.eye(3) - np.outer(a, a))
+    ax = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    Kw = oracle.element(X, STEEL, 2, omega=w, axis=axis)
+    G = oracle.element(X, STEEL, 3, axis=axis)
+    assert np.abs(Kw - w * w * P @ M @ P).max() <= 1e-14 * np.abs(Kw).max()
+    assert np.abs(G - np.kron(M[0::3, 0::3], ax)).max() <= 1e-14 * np.abs(G).max()
