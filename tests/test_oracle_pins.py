@@ -307,3 +307,49 @@ def test_rotating_element_matrices_from_mass(oracle, axis):
     G = oracle.element(X, STEEL, 3, axis=axis)
     assert np.abs(Kw - w * w * P @ M @ P).max() <= 1e-14 * np.abs(Kw).max()
     assert np.abs(G - np.kron(M[0::3, 0::3], ax)).max() <= 1e-14 * np.abs(G).max()
+
+
+@pytest.mark.parametrize("X", [REF_TET, skewed_tet()])
+def test_stress_stiffening_closed_form(oracle, X):
+    """Stress stiffening (src/rotating_effects.cpp:53-138) under a linear displacement: the
+    prestress S = D B u is constant and K_sigma(a, b) = I3 * integral of grad N_a^T S grad N_b,
+    with grad N = (4 L_a - 1) grad L_a at corners and 4 (L_b grad L_a + L_a grad L_b) at
+    mid-edges, integrated exactly in barycentric monomials."""
+    from math import factorial
+
+    E, nu = STEEL.E, STEEL.nu
+    eps = np.array([[1e-3, 1.5e-4, 1e-4], [1.5e-4, -2e-4, -0.5e-4], [1e-4, -0.5e-4, 5e-4]])
+    u = (X @ eps.T).ravel()
+    Ks = oracle.element(X, STEEL, 4, ue=u)
+    lam, mu = E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))
+    S = lam * np.trace(eps) * np.eye(3) + 2 * mu * eps
+    C = X[:4]
+    G = np.linalg.inv(np.vstack([np.ones(4), C.T]))[:, 1:]
+    V = abs(np.linalg.det(C[1:] - C[0])) / 6
+    one = (0, 0, 0, 0)
+
+    def lin(k):                                   # monomial L_k
+        e = [0, 0, 0, 0]; e[k] = 1
+        return tuple(e)
+
+    def grad_terms(node):                          # list of (polynomial, k): grad N = sum poly * grad L_k
+        if node < 4:
+            return [({lin(node): 4.0, one: -1.0}, node)]
+        a, b = [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)][node - 4]
+        return [({lin(b): 4.0}, a), ({lin(a): 4.0}, b)]
+
+    def integral(p, q):
+        s = 0.0
+        for ea, ca in p.items():
+            for eb, cb in q.items():
+                k = [x + y for x, y in zip(ea, eb)]
+                s += ca * cb * 6 * V * np.prod([factorial(x) for x in k]) / factorial(sum(k) + 3)
+        return s
+
+    ref = np.zeros((30, 30))
+    for a in range(10):
+        for b in range(10):
+            v = sum(integral(pa, pb) * (G[ka] @ S @ G[kb]) for pa, ka in grad_terms(a) for pb, kb in grad_terms(b))
+            for i in range(3):
+                ref[3 * a + i, 3 * b + i] = v
+    assert np.abs(Ks - ref).max() <= 1e-9 * np.abs(ref).max()
