@@ -353,3 +353,27 @@ def test_stress_stiffening_closed_form(oracle, X):
             for i in range(3):
                 ref[3 * a + i, 3 * b + i] = v
     assert np.abs(Ks - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("axis", [0, 2])
+def test_centrifugal_load_four_point_rule(oracle, axis):
+    """Centrifugal element load (src/rotating_effects.cpp:5-51): rho omega^2 sum over the symmetric
+    4-point rule (barycentric points (alpha, beta, beta, beta) and permutations, alpha =
+    (5 + 3 sqrt 5) / 20, beta = (5 - sqrt 5) / 20, weight 1/24 in reference volume) of N_a r_perp
+    |det J|.  The integrand is cubic, so the rule is restated rather than replaced by the exact
+    integral."""
+    X = skewed_tet()
+    w = 700.0
+    f = oracle.element(X, STEEL, 5, omega=w, axis=axis).reshape(10, 3)
+    al, be = (5 + 3 * np.sqrt(5)) / 20, (5 - np.sqrt(5)) / 20
+    C = X[:4]
+    detJ = abs(np.linalg.det(C[1:] - C[0]))
+    edges = [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]
+    ref = np.zeros((10, 3))
+    for g in range(4):
+        L = np.full(4, be); L[g] = al
+        N = np.concatenate([L * (2 * L - 1), [4 * L[a] * L[b] for a, b in edges]])
+        x = L @ C
+        r = x.copy(); r[axis] = 0.0
+        ref += STEEL.rho * w * w * np.outer(N, r) * detJ / 24.0
+    assert np.abs(f - ref).max() <= 1e-12 * np.abs(ref).max()
