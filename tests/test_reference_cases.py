@@ -184,3 +184,27 @@ def test_split_projection_equals_direct_projection(oracle, wedge, k):
         D = (T.conj().T @ A @ T).tocsc()[free][:, free].toarray()
         S = om.matrix(split, k=k).toarray()
         assert np.abs(D - S).max() <= 1e-12 * np.abs(D).max()
+
+
+def test_static_prestress_solve_against_sparse_direct(oracle, wedge):
+    """static_centrifugal (src/cyclic_solver.cpp:456-558): the prestress displacement solves the
+    k = 0 cyclic system with the hub DOFs removed, (T0^T K T0)_free u_cyc = (T0^T F)_free, u = T0 u_cyc.
+    Checked against scipy's sparse direct solve of the same system (1e-10 relative)."""
+    import scipy.sparse.linalg as spla
+    from turbomodal_gb300.meshgen import Material
+
+    om = oracle.OracleModel(wedge, Material(**MAT))
+    rpm = 10000.0
+    om.prepare(rpm)
+    omega = rpm * 2 * np.pi / 60
+    T = om.matrix("T", k=0).tocsc().real
+    K = om.matrix("K").tocsc()
+    F = om.centrifugal(omega)
+    free = om.free_map()
+    Kc = (T.T @ K @ T).tocsc()[free][:, free]
+    Fc = (T.T @ F)[free]
+    uc = np.zeros(T.shape[1])
+    uc[free] = spla.spsolve(Kc.tocsc(), Fc)
+    u = T @ uc
+    got = om.static_u()
+    assert np.abs(got - u).max() <= 1e-10 * np.abs(u).max()
