@@ -149,3 +149,46 @@ def test_reused_contexts_give_fresh_results():
         assert sorted(alone) == sorted(got)
         for k, a in alone.items():
             np.testing.assert_allclose(got[k].frequencies, a.frequencies, rtol=1e-9)
+
+
+def test_failed_request_context_is_not_kept():
+    """A request that fails mid-solve is reported and its context closed instead of cached; the next
+    request on the same sector gets a fresh context, a successful one is kept and reused."""
+    from turbomodal_gb300.meshgen import TITANIUM, sector_mesh
+    from turbomodal_gb300.serve import ModalServer, Request
+
+    closed, made = [], []
+
+    class FakeSolver:
+        def __init__(self):
+            self.id = len(made)
+            made.append(self)
+
+        def set_memory_budget(self, n):
+            pass
+
+        def prepare(self, rpm):
+            pass
+
+        def symbolic_stats(self, kind=0):
+            return {"n": 100.0, "l_entries": 1e3, "u_entries": 1e3, "lower_entries": 500.0}
+
+        def solve_at_rpm(self, rpm, num_modes, ks, precision=None):
+            if rpm < 0:
+                raise RuntimeError("planted failure")
+            return []
+
+        def close(self):
+            closed.append(self.id)
+
+    mesh = sector_mesh(4, 3, 1, num_sectors=24, seed=1)
+    srv = ModalServer(budget_bytes=1 << 40, max_inflight=1, solver_factory=lambda m, mat, p: FakeSolver())
+    bad = srv._run(Request(0, mesh, TITANIUM, -1.0, 5, [1]), 0.0)
+    assert bad.error.startswith("RuntimeError") and closed == [0] and srv.cached_contexts() == 0
+    ok = srv._run(Request(1, mesh, TITANIUM, 1000.0, 5, [1]), 0.0)
+    assert not ok.error and not ok.reused and srv.cached_contexts() == 1
+    again = srv._run(Request(2, mesh, TITANIUM, 2000.0, 5, [1]), 0.0)
+    assert not again.error and again.reused and len(made) == 2
+    assert srv._used == 0
+    srv.close()
+    assert sorted(closed) == [0, 1]
