@@ -2,8 +2,8 @@
 (turbomodal_gb300/csrc/sym.cpp) replayed with the device kernels' index arithmetic
 (tests/native/solve_schedule_check.cpp) must stay inside every panel, front vector and solution
 vector and reproduce a plain supernodal solve to roundoff (1e-12 relative), and every column's
-fill must lie inside its supernode's front, for fundamental and for relaxed supernodes (chain
-merges of analyze(relax > 0), which the solver does not use yet)."""
+fill must lie inside its supernode's front, for fundamental and for relaxed supernodes
+(amalgamation by analyze(relax > 0), which the solver does not use yet)."""
 
 import os
 import subprocess

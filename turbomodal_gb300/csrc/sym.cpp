@@ -512,15 +512,17 @@ Symbolic analyze(const Pattern& lower, double relax, int32_t relax_max_width) {
     for (int32_t s = 0; s < ns; s++)
         for (int32_t j = first[s]; j < first[s + 1]; j++) col2sn[j] = s;
     if (relax > 0.0) {
-        // merge s into s+1 when s+1 is s's parent, s is its parent's only... chain merge:
-        // the merged front has width w1+w2 and height m1 (the child's front); the cost is
-        // the explicit zeros added to the parent's columns.
+        // Amalgamation: a run of supernodes [start, end) takes in the next supernode t when t is
+        // the parent of the run's last column (t's first column == end in postorder, so the
+        // merged columns stay contiguous; t may have other children, which then update the
+        // merged front) and the explicit zeros stay within `relax` of the stored entries.  The
+        // merged front holds the run's columns plus t's front rows (the run's fill below t is
+        // inside t's front), so its height at the first column is (end - start) + cc[first[t]] + 1.
         std::vector<int32_t> nf;
         int32_t s = 0;
         while (s < ns) {
             int32_t start = first[s];
             int32_t end = first[s + 1];
-            int32_t m_start = cc[start] + 1;
             while (true) {
                 const int32_t t = col2sn[end - 1] + 1;   // next supernode
                 if (t >= ns) break;
@@ -528,20 +530,13 @@ Symbolic analyze(const Pattern& lower, double relax, int32_t relax_max_width) {
                 const int32_t wt = first[t + 1] - first[t];
                 const int32_t w = end - start;
                 if (relax_max_width > 0 && w + wt > relax_max_width) break;
-                // exact entries of merged columns vs stored m_start x (w+wt) trapezoid
+                const double H = (double)w + cc[first[t]] + 1;
                 double stored = 0, real = 0;
                 for (int32_t j = start; j < first[t + 1]; j++) {
-                    stored += m_start - (j - start);
+                    stored += H - (j - start);
                     real += cc[j] + 1;
                 }
                 if (stored - real > relax * stored) break;
-                // the next supernode must have no other children besides this chain
-                bool only_child = true;
-                int32_t kids = 0;
-                for (int32_t j = first[t]; j < first[t + 1]; j++) kids += nchild[j];
-                kids -= (first[t + 1] - first[t] - 1);   // internal chain links
-                if (kids != 1) only_child = false;
-                if (!only_child) break;
                 end = first[t + 1];
             }
             nf.push_back(start);
