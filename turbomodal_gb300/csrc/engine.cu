@@ -6,6 +6,9 @@
 //   cyclic projections Kc/Kp/Mc/Mp (+Gc/Gp): two-stage gathers with pruning      [device]
 //   per harmonic: operator K_k - sigma M_k formed on the union pattern, scattered
 //   into fronts, multifrontal LDL^H (FP64, or FP32 + FP64 refinement), Lanczos    [device]
+//   small sectors (n <= 200): dense generalized eigensolver, one CTA per problem   [device]
+//   with Coriolis, k > 0: the Lancaster pencil on the 2n block pattern, dense or
+//   shift-invert Lanczos, forward / backward selection                            [device]
 // Host work is pattern-only (symbolic analysis, cached per pattern) plus the small
 // per-restart control decisions.
 #include <algorithm>
