@@ -2,6 +2,7 @@
 test cases (tests/test_cyclic.cpp:451-535), Campbell arrays and the CSV exports."""
 
 import numpy as np
+import pytest
 
 from turbomodal_gb300.solver import (ModalResult, campbell_data, compute_stationary_frame, export_campbell_csv,
                                      export_zzenf_csv)
@@ -93,3 +94,36 @@ def test_solve_parametric_is_solve_at_rpm_per_condition():
     assert out == [[3000.0], [0.0], [9000.0]]
     assert [c[:6] for c in calls] == [(r, 7, [1, 2], 3, True, 5.0) for r in (3000.0, 0.0, 9000.0)]
     assert [p["completed"] for p in prog] == [1, 2, 3] and all(p["harmonic_k"] == -1 for p in prog)
+
+
+def test_module_functions_take_the_reference_parameters():
+    """tm.solve and tm.rpm_sweep keep the reference's parameter names, order and defaults
+    (python/turbomodal/solver.py:237-255 and :499-514), so positional calls mean the same; the
+    GPU path's own options are keyword-only at the end."""
+    import inspect
+
+    from turbomodal_gb300 import solver as m
+
+    solve_ref = [("mesh", None), ("material", None), ("rpm", 0.0), ("num_modes", 20), ("fluid", None),
+                 ("config", None), ("verbose", m.PROGRESS), ("harmonic_indices", None), ("max_threads", 0),
+                 ("hub_constraint", "fixed"), ("include_coriolis", False), ("min_frequency", 0.0),
+                 ("temperature", None), ("condition", None), ("boundary_conditions", None),
+                 ("show_convergence", False), ("memory_reserve_fraction", 0.2)]
+    sweep_ref = [("mesh", None), ("material", None), ("rpm_values", None), ("num_modes", 20), ("fluid", None),
+                 ("verbose", m.SILENT), ("harmonic_indices", None), ("max_threads", 0), ("hub_constraint", "fixed"),
+                 ("include_coriolis", False), ("min_frequency", 0.0), ("temperature", None),
+                 ("boundary_conditions", None), ("memory_reserve_fraction", 0.2)]
+    for fn, ref in ((m.solve, solve_ref), (m.rpm_sweep, sweep_ref)):
+        ps = [p for p in inspect.signature(fn).parameters.values() if p.kind != p.KEYWORD_ONLY]
+        assert [p.name for p in ps] == [n for n, _ in ref]
+        for p, (_, d) in zip(ps, ref):
+            if d is not None or p.default is not inspect.Parameter.empty:
+                assert p.default == d, p.name
+    assert (m.SILENT, m.PROGRESS, m.DETAILED) == (0, 1, 2)
+
+
+def test_solve_rejects_constraint_groups():
+    from turbomodal_gb300.solver import solve
+
+    with pytest.raises(NotImplementedError):
+        solve(None, None, boundary_conditions=[object()], verbose=0)

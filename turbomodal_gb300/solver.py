@@ -12,6 +12,7 @@ from __future__ import annotations
 import ctypes as C
 import logging
 import sys
+import time
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -281,35 +282,104 @@ def _validate(results):
     return results
 
 
+SILENT = 0
+PROGRESS = 1
+DETAILED = 2
+
+
+def _header(mesh, hi, include_coriolis, temperature):
+    nd = f"ND {hi}" if hi else f"ND 0..{mesh.num_sectors // 2}"
+    cor = " [Coriolis]" if include_coriolis else ""
+    tmp = f"  T={temperature:.1f}K" if temperature is not None else ""
+    return nd, cor, tmp
+
+
+def _unsupported(boundary_conditions):
+    if boundary_conditions is not None:
+        raise NotImplementedError("boundary_conditions (constraint groups) are not on the GPU path")
+
+
 def solve(mesh: Mesh, material: Material, rpm: float = 0.0, num_modes: int = 20, fluid=None, config=None,
-          verbose: int = 0, harmonic_indices=None, max_threads: int = 0, hub_constraint: str = "fixed",
+          verbose: int = PROGRESS, harmonic_indices=None, max_threads: int = 0, hub_constraint: str = "fixed",
           include_coriolis: bool = False, min_frequency: float = 0.0, temperature: float | None = None,
-          memory_reserve_fraction: float = 0.2, precision: str = "fp64", solver: CyclicSymmetrySolver | None = None):
-    """tm.solve on the GPU path; returns EnrichedModalResult per harmonic index."""
+          condition=None, boundary_conditions=None, show_convergence: bool = False,
+          memory_reserve_fraction: float = 0.2, *, precision: str = "fp64",
+          solver: CyclicSymmetrySolver | None = None):
+    """tm.solve (python/turbomodal/solver.py:237-375) on the GPU path, with the reference's parameters
+    in its order; one EnrichedModalResult per harmonic index.  `condition` supplies rpm and (unless
+    given) temperature; `config` is accepted and unused, as in the reference.  Constraint groups
+    (`boundary_conditions`) and fluid coupling are not on the GPU path and raise
+    NotImplementedError; `show_convergence` (a live plot) is not available and only warns.
+    Keyword-only: `precision` ("fp64" or "mixed") and a `solver` to reuse."""
+    if condition is not None:
+        rpm = condition.rpm
+        if temperature is None:
+            temperature = condition.temperature
+    _unsupported(boundary_conditions)
+    if show_convergence:
+        logger.warning("show_convergence: no live plot on this path; solving without it")
     if temperature is not None:
         material = material.at_temperature(temperature)
+    hi = list(harmonic_indices or [])
+    if verbose >= PROGRESS:
+        nd, cor, tmp = _header(mesh, hi, include_coriolis, temperature)
+        print(f"Solving at {rpm:.0f} RPM{cor}{tmp}  ({mesh.num_nodes()} nodes, {mesh.num_elements()} elements, "
+              f"{mesh.num_sectors} sectors, {nd}, {num_modes} modes/ND)")
+    t0 = time.perf_counter()
     s = solver or CyclicSymmetrySolver(mesh, material, fluid, hub_constraint == "fixed", precision=precision)
-    res = s.solve_at_rpm(rpm, num_modes, harmonic_indices or [], max_threads, include_coriolis, min_frequency,
+    res = s.solve_at_rpm(rpm, num_modes, hi, max_threads, include_coriolis, min_frequency,
                          memory_reserve_fraction=memory_reserve_fraction, precision=precision)
+    if verbose >= PROGRESS:
+        print(f"  Solved {len(res)} harmonic indices in {time.perf_counter() - t0:.1f}s")
     res = _validate(res)
     M = s.assemble("M")
     masses = _modal_mass_from_M(M, res, mesh.num_sectors)
-    return [EnrichedModalResult(_result=r, modal_mass_kg=m) for r, m in zip(res, masses)]
+    out = [EnrichedModalResult(_result=r, modal_mass_kg=m) for r, m in zip(res, masses)]
+    if verbose >= DETAILED:
+        for r in out:
+            freqs = ", ".join(f"{f:.1f}" for f in r.frequencies[:4])
+            mm = ", ".join(f"{m:.4e}" for m in r.modal_mass_kg[:4])
+            print(f"    ND={r.harmonic_index:2d}: [{freqs}] Hz (rotating frame)")
+            print(f"           modal mass [kg]: [{mm}]")
+    return out
 
 
-def rpm_sweep(mesh: Mesh, material: Material, rpm_values, num_modes: int = 10, harmonic_indices=None,
-              include_coriolis: bool = False, min_frequency: float = 0.0, precision: str = "fp64", verbose: int = 0,
-              hub_constraint: str = "fixed"):
-    """tm.rpm_sweep on the GPU path: one solver (sector assembly and symbolic analysis
-    reused across speeds), one solve per speed."""
-    s = CyclicSymmetrySolver(mesh, material, None, hub_constraint == "fixed", precision=precision)
+def rpm_sweep(mesh: Mesh, material: Material, rpm_values, num_modes: int = 20, fluid=None, verbose: int = SILENT,
+              harmonic_indices=None, max_threads: int = 0, hub_constraint: str = "fixed",
+              include_coriolis: bool = False, min_frequency: float = 0.0, temperature: float | None = None,
+              boundary_conditions=None, memory_reserve_fraction: float = 0.2, *, precision: str = "fp64"):
+    """tm.rpm_sweep (python/turbomodal/solver.py:499-628) on the GPU path, with the reference's
+    parameters in its order: one solver (sector assembly and symbolic analysis reused across
+    speeds), one solve per speed, modal masses from one mass assembly."""
+    _unsupported(boundary_conditions)
+    if temperature is not None:
+        material = material.at_temperature(temperature)
+    hi = list(harmonic_indices or [])
+    rpms = np.asarray(rpm_values, dtype=np.float64)
+    if verbose >= PROGRESS and len(rpms):
+        nd, cor, tmp = _header(mesh, hi, include_coriolis, temperature)
+        print(f"RPM sweep{cor}{tmp}: {len(rpms)} points [{rpms[0]:.0f} .. {rpms[-1]:.0f}] RPM")
+        print(f"  Mesh: {mesh.num_nodes()} nodes, {mesh.num_elements()} elements, {mesh.num_sectors} sectors")
+        print(f"  Solving {nd}, {num_modes} modes/ND")
+        print()
+    s = CyclicSymmetrySolver(mesh, material, fluid, hub_constraint == "fixed", precision=precision)
     M = s.assemble("M")
     out = []
-    for rpm in np.asarray(rpm_values, dtype=np.float64):
-        res = s.solve_at_rpm(float(rpm), num_modes, harmonic_indices or [], 0, include_coriolis, min_frequency,
-                             precision=precision)
+    t_start = time.perf_counter()
+    for i, rpm in enumerate(rpms):
+        t0 = time.perf_counter()
+        res = _validate(s.solve_at_rpm(float(rpm), num_modes, hi, max_threads, include_coriolis, min_frequency,
+                                       memory_reserve_fraction=memory_reserve_fraction, precision=precision))
         masses = _modal_mass_from_M(M, res, mesh.num_sectors)
         out.append([EnrichedModalResult(_result=r, modal_mass_kg=m) for r, m in zip(res, masses)])
+        if verbose >= DETAILED:
+            print(f"  [{i + 1}/{len(rpms)}] {rpm:.0f} RPM  ({len(res)} harmonics, {time.perf_counter() - t0:.1f}s)")
+            for r in res:
+                freqs = ", ".join(f"{f:.1f}" for f in r.frequencies[:3])
+                print(f"      ND={r.harmonic_index:2d}: [{freqs}] Hz")
+    if verbose >= PROGRESS and len(rpms):
+        total = time.perf_counter() - t_start
+        print(f"  Sweep complete in {total:.1f}s ({total / len(rpms):.1f}s/point avg)")
     return out
 
 
