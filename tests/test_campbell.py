@@ -93,7 +93,7 @@ def test_solve_parametric_is_solve_at_rpm_per_condition():
     out = s.solve_parametric(conds, 7, [1, 2], 3, True, 5.0, progress_cb=prog.append)
     assert out == [[3000.0], [0.0], [9000.0]]
     assert [c[:6] for c in calls] == [(r, 7, [1, 2], 3, True, 5.0) for r in (3000.0, 0.0, 9000.0)]
-    assert [p["completed"] for p in prog] == [1, 2, 3] and all(p["harmonic_k"] == -1 for p in prog)
+    assert [p.completed for p in prog] == [1, 2, 3] and all(p.harmonic_k == -1 and p.total == 3 for p in prog)
 
 
 def test_module_functions_take_the_reference_parameters():

@@ -52,6 +52,24 @@ class ModalResult:
 
 
 @dataclass
+class SolverProgress:
+    """Callback data of solve_at_rpm's progress_cb (include/turbomodal/cyclic_solver.hpp:16-28,
+    python/turbomodal/_core.pyi:150-161)."""
+
+    completed: int = 0
+    total: int = 0
+    harmonic_k: int = 0
+    converged: bool = True
+    iterations: int = 0
+    num_converged: int = 0
+    num_modes: int = 0
+    max_residual: float = 0.0
+    min_freq_hz: float = 0.0
+    max_freq_hz: float = 0.0
+    elapsed_s: float = 0.0
+
+
+@dataclass
 class ParametricCondition:
     """Operating condition of solve_parametric (include/turbomodal/cyclic_solver.hpp:58-62,
     src/python_bindings.cpp:300-318)."""
@@ -100,6 +118,7 @@ class CyclicSymmetrySolver:
         """Modal solve at one speed (src/python_bindings.cpp:332-361).  With include_coriolis,
         harmonics k > 0 solve the Lancaster QEP and carry whirl directions +1 / -1."""
         prec = _lib.PREC[precision or self.precision]
+        t_call = time.perf_counter()
         hi = np.asarray(list(harmonic_indices or []), dtype=np.int32)
         nres = C.c_int32()
         L, h = self.ctx.L, self.ctx.h
@@ -131,8 +150,13 @@ class CyclicSymmetrySolver:
                 sys.stderr.write(f"[CyclicSolver] WARNING: k={r.harmonic_index} eigenvalue solve did not fully converge\n")
             out.append(r)
             if progress_cb is not None:
-                progress_cb(dict(completed=len(out), total=nres.value, harmonic_k=r.harmonic_index,
-                                 converged=r.converged, num_modes=m))
+                progress_cb(SolverProgress(completed=len(out), total=nres.value, harmonic_k=r.harmonic_index,
+                                           converged=r.converged, iterations=r.iterations,
+                                           num_converged=m if r.converged else 0, num_modes=m,
+                                           max_residual=r.max_residual,
+                                           min_freq_hz=float(f.min()) if m else 0.0,
+                                           max_freq_hz=float(f.max()) if m else 0.0,
+                                           elapsed_s=time.perf_counter() - t_call))
         return out
 
     def solve_parametric(self, conditions, num_modes_per_harmonic: int, harmonic_indices=(), max_threads: int = 0,
@@ -145,12 +169,14 @@ class CyclicSymmetrySolver:
         effect; this mirror returns the same.  progress_cb gets one call per condition
         (harmonic_k = -1)."""
         out = []
+        t0 = time.perf_counter()
         for i, cond in enumerate(conditions):
             out.append(self.solve_at_rpm(float(cond.rpm), num_modes_per_harmonic, harmonic_indices, max_threads,
                                          include_coriolis, min_frequency, None, allow_condensation,
                                          memory_reserve_fraction))
             if progress_cb is not None:
-                progress_cb(dict(completed=i + 1, total=len(conditions), harmonic_k=-1, converged=True, num_modes=0))
+                progress_cb(SolverProgress(completed=i + 1, total=len(conditions), harmonic_k=-1, converged=True,
+                                           elapsed_s=time.perf_counter() - t0))
         return out
 
     def solve_rpm_sweep(self, rpm_values, num_modes_per_harmonic: int, harmonic_indices=(), max_threads: int = 0,
