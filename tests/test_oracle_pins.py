@@ -377,3 +377,25 @@ def test_centrifugal_load_four_point_rule(oracle, axis):
         r = x.copy(); r[axis] = 0.0
         ref += STEEL.rho * w * w * np.outer(N, r) * detJ / 24.0
     assert np.abs(f - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("k", [1, 18])
+def test_config0_harmonics_against_scipy_eigsh(oracle, cfg0_mesh, k):
+    """The oracle's shift-invert Lanczos at full config-0 size (n = 5,760 per harmonic, 10000 rpm)
+    against scipy's independent ARPACK shift-invert (sigma = 1, the reference's shift) on the same
+    K_k, M_k: the lowest frequencies within 1e-9 relative.  k = 1 is complex (degenerate, each
+    eigenvalue returned twice), k = N/2 real."""
+    import scipy.sparse.linalg as spla
+
+    om = oracle.OracleModel(cfg0_mesh, Material(114e9, 0.34, 4430.0))
+    om.prepare(10000.0)
+    res = om.solve(10000.0, 6, harmonic_indices=[k], max_threads=4, with_shapes=False)[0]
+    K, M = om.matrix("Kk", k=k).tocsc(), om.matrix("Mk", k=k).tocsc()
+    if k == 18:
+        K, M = K.real, M.real
+    nev = 3 if k == 1 else 6
+    w = spla.eigsh(K, k=nev, M=M, sigma=1.0, which="LM", return_eigenvectors=False, tol=1e-12)
+    f_ref = np.sort(np.sqrt(w)) / (2 * np.pi)
+    f = res["frequencies"]
+    f_unique = f[::2] if k == 1 else f
+    assert np.max(np.abs(f_unique[:nev] - f_ref) / f_ref) <= 1e-9
