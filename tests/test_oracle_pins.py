@@ -383,19 +383,30 @@ def test_centrifugal_load_four_point_rule(oracle, axis):
 def test_config0_harmonics_against_scipy_eigsh(oracle, cfg0_mesh, k):
     """The oracle's shift-invert Lanczos at full config-0 size (n = 5,760 per harmonic, 10000 rpm)
     against scipy's independent ARPACK shift-invert (sigma = 1, the reference's shift) on the same
-    K_k, M_k: the lowest frequencies within 1e-9 relative.  k = 1 is complex (degenerate, each
-    eigenvalue returned twice), k = N/2 real."""
+    K_k, M_k: the lowest frequencies within 1e-9 relative and the expanded mode shapes with MAC
+    >= 1 - 1e-9.  k = 1 is complex (degenerate, each eigenvalue returned twice), k = N/2 real."""
     import scipy.sparse.linalg as spla
 
     om = oracle.OracleModel(cfg0_mesh, Material(114e9, 0.34, 4430.0))
     om.prepare(10000.0)
-    res = om.solve(10000.0, 6, harmonic_indices=[k], max_threads=4, with_shapes=False)[0]
+    res = om.solve(10000.0, 6, harmonic_indices=[k], max_threads=4)[0]
     K, M = om.matrix("Kk", k=k).tocsc(), om.matrix("Mk", k=k).tocsc()
     if k == 18:
         K, M = K.real, M.real
     nev = 3 if k == 1 else 6
-    w = spla.eigsh(K, k=nev, M=M, sigma=1.0, which="LM", return_eigenvectors=False, tol=1e-12)
-    f_ref = np.sort(np.sqrt(w)) / (2 * np.pi)
+    w, X = spla.eigsh(K, k=nev, M=M, sigma=1.0, which="LM", tol=1e-12)
+    order = np.argsort(w)
+    f_ref = np.sqrt(w[order]) / (2 * np.pi)
     f = res["frequencies"]
-    f_unique = f[::2] if k == 1 else f
+    pick = slice(0, None, 2) if k == 1 else slice(None)     # degenerate pairs: one of each
+    f_unique = f[pick]
     assert np.max(np.abs(f_unique[:nev] - f_ref) / f_ref) <= 1e-9
+    # mode shapes: ARPACK's free-space vectors expanded by T(k) (right rows times e^{ik alpha})
+    T = om.matrix("T", k=k).tocsc()
+    free = om.free_map()
+    shapes = res["mode_shapes"][:, pick]
+    for q in range(nev):
+        u = T[:, free] @ X[:, order[q]]
+        v = shapes[:, q]
+        mac = abs(np.vdot(u, v)) ** 2 / (np.vdot(u, u).real * np.vdot(v, v).real)
+        assert mac >= 1 - 1e-9
