@@ -34,7 +34,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 RPMS = np.linspace(0.0, 15000.0, 24)
-METRIC = "converged eigenpairs/s @1e-6 rel freq err (mixed FP32 LDL^H + FP64 refinement, 1 GB300)"
+METRIC = "converged eigenpairs/s @1e-6 rel freq err, config-1 bladed-disk rpm sweep"
 UNIT = "eigenpairs/s"
 WORKLOAD = "config-1 bladed-disk sector rpm sweep (57,897 nodes, 24 speeds x 19 harmonics, 10 modes)"
 
@@ -48,6 +48,11 @@ def parse():
     ap.add_argument("--harmonics", default="all", help="comma list or 'all'")
     ap.add_argument("--num-modes", type=int, default=10)
     ap.add_argument("--no-verify", action="store_true", help="skip the FP64 verification pass")
+    ap.add_argument("--verify-steps", type=int, default=4,
+                    help="timed speeds (spread over the sweep) re-solved on the plain FP64 GPU path")
+    ap.add_argument("--wall-budget", type=float, default=1200.0,
+                    help="seconds after start beyond which the optional legs (serving sample, CPU baseline) "
+                         "are skipped")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the served request-stream sample")
     ap.add_argument("--serve-requests", type=int, default=12)
@@ -182,62 +187,186 @@ def count_verified(mixed, fp64, tol=1e-6):
     return n_ok, n_all, worst
 
 
-def cpu_baseline_sample(rpm: float, F_target: float, threads: int = 1, all_harmonics: bool = False):
-    """Oracle (CPU restatement of the reference path) on a bounded sample: harmonic k=1 (or
-    every harmonic, over `threads` host threads as the reference's thread pool does) of a
-    config-1-family sector small enough for ~10-60 s of CPU work, full pipeline (assembly,
-    prestress, projections, simplicial LDL^H, Lanczos).  The eigenpairs/s is scaled to the
-    config-1 problem by the ratio of factorisation flops (the dominant CPU cost)."""
-    from oracle import orc
-    from turbomodal_gb300.meshgen import TITANIUM, sector_mesh
-    import scipy.sparse as sp
+def mem_available_bytes() -> int:
+    """Host memory this process may still use: MemAvailable, capped by the cgroup limit."""
+    avail = 8 << 30
+    try:
+        with open("/proc/meminfo") as fh:
+            for line in fh:
+                if line.startswith("MemAvailable:"):
+                    avail = int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    for lim, use in (("/sys/fs/cgroup/memory.max", "/sys/fs/cgroup/memory.current"),
+                     ("/sys/fs/cgroup/memory/memory.limit_in_bytes", "/sys/fs/cgroup/memory/memory.usage_in_bytes")):
+        try:
+            with open(lim) as fh:
+                raw = fh.read().strip()
+            if raw == "max":
+                continue
+            with open(use) as fh:
+                used = int(fh.read().strip())
+            avail = min(avail, max(0, int(raw) - used))
+        except (OSError, ValueError):
+            continue
+    return avail
 
-    if all_harmonics:   # all 19 harmonics: a smaller sector keeps a step to ~30 s of host time
-        m = sector_mesh(14, 8, 3, num_sectors=36, jitter=0.02, seed=11,
-                        blade=dict(ns=9, nc=4, nb=2, span=0.12, chord=0.05, thick=0.004, twist_deg=30.0))
-    else:
-        m = sector_mesh(18, 10, 4, num_sectors=36, jitter=0.02, seed=11,
-                        blade=dict(ns=12, nc=5, nb=2, span=0.12, chord=0.05, thick=0.004, twist_deg=30.0))
-    om = orc.OracleModel(m, TITANIUM)
+
+class ReferenceSample:
+    """The reference's CPU path for one speed of the config-1 sweep, measured on the config-1
+    operator itself in bounded samples (the oracle restates it; the reference needs Eigen and
+    Spectra, which cannot be built here).
+
+    Per speed the reference assembles and projects the sector, then solves the 19 harmonics on
+    a std::thread pool (src/cyclic_solver.cpp:1226-1332): for each, Eigen's up-looking
+    SimplicialLDLT of K_k - M_k and the shift-invert Lanczos.  One factorisation of the config-1
+    operator takes ~20 min on one core, so it is measured in row windows
+    (oracle/orc_window.hpp): the rows are cut into W windows of equal loop work, and every
+    sample runs one window of the numeric loop on the real structure of L, `threads` windows at
+    once on separate threads (each its own copy of L, as the pool runs one harmonic per thread),
+    each followed by one whole triangular solve.  Estimates:
+      T_fact  = W x mean window time   (every window has the same work)
+      T_harm  = T_fact + 40 x T_solve  (ncv = 40 shift-invert applications; no restarts)
+      T_speed = T_prep + (17 T_harm + 2 T_harm / 4) / threads
+    T_prep is the oracle's assembly and cyclic projections at rest, timed once.  Left out, which
+    favours the CPU: the prestress solve at speed, Lanczos restarts and reorthogonalisation,
+    M products; the real harmonics k = 0, 18 are counted at a quarter of a complex one, and the
+    pool at perfect load balance."""
+
+    PAIRS_PER_SPEED = 190     # 19 harmonics x 10 modes, as the GPU arm counts them
+
+    def __init__(self, threads: int | None = None, target_window_s: float = 4.0, planned_samples: int = 0,
+                 mesh=None):
+        from oracle import orc
+        from turbomodal_gb300.meshgen import TITANIUM, config_mesh
+
+        orc.build()
+        t0 = time.perf_counter()
+        self.mesh = mesh if mesh is not None else config_mesh(1)
+        om = orc.OracleModel(self.mesh, TITANIUM)
+        om.prepare(0.0)
+        self.t_prep = time.perf_counter() - t0
+        A = (om.matrix("Kk", k=1) - om.matrix("Mk", k=1)).tocsc()
+        del om
+        self.lw = orc.LdlWindows(A)
+        self.n = self.lw.n
+        slot_bytes = 16 * self.lw.nnz_l + 64 * self.n
+        want = threads or os.cpu_count() or 1
+        fit = max(1, int(0.6 * mem_available_bytes() // slot_bytes))
+        self.threads = max(1, min(want, 17, fit))
+        for _ in range(self.threads - 1):
+            self.lw.add_slot()
+        self.cum = self.lw.cumwork()
+        # probe: one window of 1/4000 of the loop work on one thread sets the window count
+        b = int(np.searchsorted(self.cum, self.cum[-1] / 4000.0))
+        tf, _ = self.lw.run([0], [0], [max(b, 1)], solve=False)
+        est = max(tf[0], 1e-6) * 4000.0
+        self.W = max(1, planned_samples, int(round(est / target_window_s)))
+        self.bnd = np.searchsorted(self.cum, np.linspace(0, self.cum[-1], self.W + 1))
+        self.bnd[0], self.bnd[-1] = 0, self.n
+        self.planned = max(1, planned_samples)
+        self.next = 0
+        self.t_fact, self.t_solve = [], []
+        self.setup_s = time.perf_counter() - t0
+
+    def step(self, record: bool = True) -> float:
+        """One sample round: `threads` windows at once, each followed by one solve; returns its
+        wall time."""
+        idx = [(self.next + t) % self.planned for t in range(self.threads)]
+        if record:
+            self.next += self.threads
+        win = [min(self.W - 1, int((q + 0.5) * self.W / self.planned)) for q in idx]
+        a = [int(self.bnd[w]) for w in win]
+        b = [int(self.bnd[w + 1]) for w in win]
+        t0 = time.perf_counter()
+        tf, ts = self.lw.run(list(range(self.threads)), a, b, solve=True)
+        dt = time.perf_counter() - t0
+        if record:
+            self.t_fact += list(tf)
+            self.t_solve += list(ts)
+        return dt
+
+    def estimate(self) -> dict:
+        t_fact = self.W * float(np.mean(self.t_fact))
+        t_solve = float(np.mean(self.t_solve))
+        t_harm = t_fact + 40.0 * t_solve
+        t_speed = self.t_prep + (17.0 * t_harm + 2.0 * t_harm / 4.0) / self.threads
+        return {"value": self.PAIRS_PER_SPEED / t_speed, "t_speed_s": t_speed, "t_fact_s": t_fact,
+                "t_solve_s": t_solve, "t_prep_s": self.t_prep}
+
+    def describe(self, sampled_s: float) -> str:
+        e = self.estimate()
+        return (f"oracle (Eigen SimplicialLDLT + Lanczos restated) on the config-1 harmonic operator "
+                f"(n={self.n}, nnz(L)={self.lw.nnz_l}): {len(self.t_fact)} of {self.W} equal-work row windows "
+                f"of the up-looking LDL^H timed, {self.threads} at once on {self.threads} threads, plus "
+                f"{len(self.t_solve)} whole solves ({sampled_s:.0f} s sampled); per harmonic factor "
+                f"{e['t_fact_s']:.0f} s + 40 solves x {e['t_solve_s']:.2f} s, assembly+projections "
+                f"{e['t_prep_s']:.0f} s; one speed = {e['t_speed_s']:.0f} s on {self.threads} threads "
+                f"(prestress solve, restarts and reorthogonalisation left out, real harmonics at 1/4)")
+
+
+def cpu_baseline_sample(threads: int | None = None, windows: int = 2):
+    """The GPU arm's cpu_baseline: a short ReferenceSample (`windows` sample rounds)."""
+    rs = ReferenceSample(threads=threads, planned_samples=windows * (threads or os.cpu_count() or 1))
     t0 = time.perf_counter()
-    om.prepare(rpm)
-    ks = list(range(m.num_sectors // 2 + 1)) if all_harmonics else [1]
-    res = om.solve(rpm, 10, harmonic_indices=ks, max_threads=threads, with_shapes=True)
-    t = time.perf_counter() - t0
-    n_pairs = sum(len(r["frequencies"]) for r in res)
-    Kk, Mk = om.matrix("Kk", k=1), om.matrix("Mk", k=1)
-    P = sp.tril(sp.csc_matrix((abs(Kk) + abs(Mk)) > 0, dtype=float)).tocsc()
-    _, _, cc = orc.ldl_symbolic(P)
-    F_sample = 4.0 * float(np.sum(cc.astype(np.float64) ** 2))
-    t_scaled = t * F_target / F_sample
-    which = f"harmonics 0..{m.num_sectors // 2} on {threads} threads" if all_harmonics else "harmonic k=1 on 1 thread"
-    return {"value": n_pairs / t_scaled, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": (f"oracle, {which} at {rpm:.0f} rpm of a {m.num_nodes()}-node config-1-family sector "
-                       f"({t:.1f} s, {n_pairs} eigenpairs), time scaled by factorisation flops "
-                       f"{F_target:.3g}/{F_sample:.3g} to the config-1 problem"),
-            "sample_seconds": t}
+    for _ in range(windows):
+        rs.step()
+    sampled = time.perf_counter() - t0
+    e = rs.estimate()
+    return {"value": e["value"], "unit": UNIT, "cores": rs.threads, "kind": "port",
+            "sample": rs.describe(sampled), "sample_seconds": sampled + rs.setup_s}
 
 
 def run_reference(args, ws, rank, pg):
     """Reference arm: the reference's CPU algorithm (the oracle restatement; the reference itself
-    needs Eigen and Spectra, which are not available) on the same workload family."""
+    needs Eigen and Spectra, which are not available) on the config-1 sweep, sampled as
+    ReferenceSample describes: every timed step is one round of concurrent row windows, and the
+    line's value is the eigenpairs/s of one speed estimated from all timed rounds."""
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    # factorisation flops of the config-1 harmonic operator (host symbolic analysis only)
-    F_target = 3.79696e12
-    vals = []
-    for _ in range(args.warmup + args.steps):
-        vals.append(cpu_baseline_sample(RPMS[1], F_target, threads=cores, all_harmonics=True))
-    v = float(np.mean([x["value"] for x in vals[args.warmup:]]))
-    ms = float(np.mean([x["sample_seconds"] for x in vals[args.warmup:]])) * 1e3
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+    rs = ReferenceSample(threads=cores, planned_samples=args.steps * min(cores, 17))
+    log(f"reference sample: setup {rs.setup_s:.1f} s, {rs.threads} threads, {rs.W} windows")
+    for i in range(args.warmup):
+        rs.step(record=False)
+    step_s = []
+    for i in range(args.steps):
+        step_s.append(rs.step())
+        log(f"reference step {i + 1}/{args.steps}: {step_s[-1]:.1f} s")
+    e = rs.estimate()
+    v = e["value"]
+    ms = 1e3 * float(np.mean(step_s))
+    sample = rs.describe(sum(step_s))
+    line = {"impl": "reference",
+            "metric": METRIC,
+            "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "l2": "inputs larger than L2"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": vals[-1]["sample"]},
+            "config": {"workload": WORKLOAD, "path": "reference CPU path (oracle): simplicial LDL^H + Lanczos, FP64, "
+                                                     f"{rs.threads} host threads",
+                       "l2": "inputs larger than L2",
+                       "step": "one round of concurrent row-window samples of the config-1 factorisation"},
+            "reference_estimate": e,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": rs.threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+T_START = time.perf_counter()
+
+
+def log(msg: str) -> None:
+    """Progress on stderr (the JSON line alone goes to stdout)."""
+    sys.stderr.write(f"[bench {time.perf_counter() - T_START:7.1f} s] {msg}\n")
+    sys.stderr.flush()
+
+
+def verify_indices(n_timed: int, n_verify: int) -> list[int]:
+    """Timed steps re-solved on the FP64 path: n_verify of them spread evenly over the sweep
+    (first and last included)."""
+    if n_timed <= 0 or n_verify <= 0:
+        return []
+    return sorted({int(round(x)) for x in np.linspace(0, n_timed - 1, min(n_verify, n_timed))})
 
 
 def main():
@@ -262,47 +391,54 @@ def main():
     solver = CyclicSymmetrySolver(mesh, TITANIUM, device=local, precision="mixed")
     order = list(my_rpms) * (1 + (args.warmup + args.steps) // max(1, len(my_rpms)))
     warm, timed = order[: args.warmup], order[args.warmup: args.warmup + args.steps]
-    for rpm in warm:
+    log(f"config-1 mesh {mesh.num_nodes()} nodes; {len(warm)} warm-up and {len(timed)} timed speeds")
+    for i, rpm in enumerate(warm):
+        t0 = time.perf_counter()
         solver.solve_at_rpm(rpm, args.num_modes, hi, precision="mixed")
+        log(f"warm-up {i + 1}/{len(warm)} at {rpm:.0f} rpm: {time.perf_counter() - t0:.1f} s")
     torch.cuda.synchronize()
     barrier(pg)
     clocks = ClockSampler(local)
     clocks.start()
-    dev_ms, wall_s, results, launches, d2h = [], [], [], 0, 0
+    dev_ms, wall_s, results, launches, d2h = [], [], [], 0, []
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_push("timed")
-    for rpm in timed:
+    for i, rpm in enumerate(timed):
         t0 = time.perf_counter()
         res = solver.solve_at_rpm(rpm, args.num_modes, hi, precision="mixed")
         wall_s.append(time.perf_counter() - t0)
         tm = solver.last_timing()
         dev_ms.append(tm["device_ms"])
         launches += int(tm["kernel_launches"])
-        d2h += sum(r.frequencies.nbytes + r.mode_shapes.nbytes + r.whirl_direction.nbytes for r in res)
+        d2h.append(sum(r.frequencies.nbytes + r.mode_shapes.nbytes + r.whirl_direction.nbytes for r in res))
         results.append(res)
+        log(f"timed {i + 1}/{len(timed)} at {rpm:.0f} rpm: {tm['device_ms'] / 1e3:.2f} s device, "
+            f"{wall_s[-1]:.2f} s wall, {sum(len(r.frequencies) for r in res)} eigenpairs")
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     clk = clocks.stop()
     barrier(pg)
-    # verification against the plain FP64 GPU path (untimed) and its own throughput
-    n_ok = n_all = 0
-    n_distinct = None
+    # verification of a stated subset of the timed speeds against the plain FP64 GPU path
+    # (untimed); value and e2e count the verified eigenpairs of exactly those speeds
+    vidx = [] if args.no_verify else verify_indices(len(timed), args.verify_steps)
+    n_ok = n_all = n_distinct = 0
     worst = 0.0
-    fp64_ms = 0.0
-    fp64_pairs = 0
-    if not args.no_verify:
-        n_distinct = 0
-        for rpm, res in zip(timed, results):
-            ref = solver.solve_at_rpm(rpm, args.num_modes, hi, precision="fp64")
-            fp64_ms += solver.last_timing()["device_ms"]
-            fp64_pairs += sum(len(r.frequencies) for r in ref if r.converged)
-            a, b, w = count_verified(res, ref)
-            n_ok += a
-            n_all += b
-            n_distinct += count_distinct_verified(res, ref)
-            worst = max(worst, w)
-    else:
+    fp64_ms, fp64_pairs = 0.0, 0
+    for q, i in enumerate(vidx):
+        ref = solver.solve_at_rpm(timed[i], args.num_modes, hi, precision="fp64")
+        fp64_ms += solver.last_timing()["device_ms"]
+        fp64_pairs += sum(len(r.frequencies) for r in ref if r.converged)
+        a, b, w = count_verified(results[i], ref)
+        n_ok += a
+        n_all += b
+        n_distinct += count_distinct_verified(results[i], ref)
+        worst = max(worst, w)
+        log(f"verified {q + 1}/{len(vidx)} at {timed[i]:.0f} rpm: {a}/{b} within 1e-6 (worst {w:.2e})")
+    if args.no_verify:   # unverified run: every returned eigenpair of every timed speed
+        vidx = list(range(len(timed)))
         n_ok = n_all = sum(len(r.frequencies) for res in results for r in res)
+    v_dev_s = sum(dev_ms[i] for i in vidx) / 1e3
+    v_wall_s = sum(wall_s[i] for i in vidx)
     # roofline of the dominant kernel: the shift-invert triangular-solve graph of the batch of
     # complex harmonics (HBM bound), timed live with CUDA events in one extra profiled solve
     mesh_k = [k for k in (hi or range(mesh.num_sectors // 2 + 1)) if 0 < k < mesh.num_sectors / 2]
@@ -310,6 +446,7 @@ def main():
     solver.solve_at_rpm(timed[0], args.num_modes, mesh_k, precision="mixed")
     prof = solver.profile_solve()
     solver.set_profiling(False)
+    log(f"profiled solve: {prof['count']} batched triangular solves, {prof['ms']:.1f} ms")
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -327,44 +464,60 @@ def main():
             for line in fh:
                 if line.startswith("dram_bytes_per_solve"):
                     traffic = float(line.split("=")[1])
-    t_dev = max_over_ranks(pg, sum(dev_ms) / 1e3)
-    t_wall = max_over_ranks(pg, sum(wall_s))
+    t_dev_all = max_over_ranks(pg, sum(dev_ms) / 1e3)
+    t_dev = max_over_ranks(pg, v_dev_s)
+    t_wall = max_over_ranks(pg, v_wall_s)
     tot_ok = sum_over_ranks(pg, n_ok)
     tot_all = sum_over_ranks(pg, n_all)
-    tot_distinct = sum_over_ranks(pg, n_distinct or 0)
+    tot_distinct = sum_over_ranks(pg, n_distinct)
+    tot_returned = sum_over_ranks(pg, sum(len(r.frequencies) for res in results for r in res))
+    skipped = []
     serving = None
     if rank == 0 and not args.no_serve:
-        # served request stream (Poisson arrivals, mixed sizes, admission by memory budget)
-        from turbomodal_gb300.serve import ModalServer, latency_summary, request_stream
+        if time.perf_counter() - T_START > args.wall_budget:
+            skipped.append("serving")
+        else:
+            # served request stream (Poisson arrivals, mixed sizes, admission by memory budget)
+            from turbomodal_gb300.serve import ModalServer, latency_summary, request_stream
 
-        reqs = request_stream(args.serve_requests, seed=2024, rate_hz=20.0, min_nodes=2000,
-                              max_nodes=args.serve_max_nodes)
-        srv = ModalServer(device=local, budget_bytes=150 << 30, max_inflight=4)
-        done = srv.serve(reqs)
-        srv.close()
-        serving = latency_summary(done)
-        serving["sample"] = (f"{len(reqs)} requests, Poisson 20 req/s, config-0/1-style sectors of 2000-"
-                             f"{args.serve_max_nodes} nodes (log-uniform), 24/36/48 sectors, rpm U(0,15000), "
-                             "5-20 modes, 1-19 random harmonics, mixed precision, 150 GB budget, 4 in flight")
+            reqs = request_stream(args.serve_requests, seed=2024, rate_hz=20.0, min_nodes=2000,
+                                  max_nodes=args.serve_max_nodes)
+            srv = ModalServer(device=local, budget_bytes=150 << 30, max_inflight=4)
+            done = srv.serve(reqs)
+            srv.close()
+            serving = latency_summary(done)
+            serving["sample"] = (f"{len(reqs)} requests, Poisson 20 req/s, config-0/1-style sectors of 2000-"
+                                 f"{args.serve_max_nodes} nodes (log-uniform), 24/36/48 sectors, rpm U(0,15000), "
+                                 "5-20 modes, 1-19 random harmonics, mixed precision, 150 GB budget, 4 in flight")
+            log(f"serving sample: p50 {serving.get('p50_s')} s, p99 {serving.get('p99_s')} s")
     if rank == 0:
         cpu = None
         if ws == 1 and not args.no_cpu_baseline:
-            st = solver.symbolic_stats(0)
-            cpu = cpu_baseline_sample(RPMS[1], st["flops"])
+            if time.perf_counter() - T_START > args.wall_budget:
+                skipped.append("cpu_baseline")
+            else:
+                cpu = cpu_baseline_sample(threads=None, windows=2)
+                log(f"cpu baseline: {cpu['value']:.4g} eigenpairs/s ({cpu['sample_seconds']:.1f} s sampled)")
         line = {
             "metric": METRIC, "value": tot_ok / t_dev if t_dev > 0 else 0.0, "unit": UNIT, "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / max(len(timed), 1),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev_all / max(len(timed), 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "harmonics": args.harmonics, "num_modes": args.num_modes,
-                       "speeds": [float(r) for r in timed], "parallelism": f"replicas x{ws} (speeds sharded)",
+            "config": {"workload": WORKLOAD, "path": "mixed FP32 supernodal LDL^H + FP64 refinement, 1 GB300",
+                       "harmonics": args.harmonics, "num_modes": args.num_modes,
+                       "speeds": [float(r) for r in timed],
+                       "verified_speeds": [float(timed[i]) for i in vidx],
+                       "parallelism": f"replicas x{ws} (speeds sharded)",
                        "l2": "inputs larger than L2 (no flush needed)"},
-            "eigenpairs": {"verified": int(tot_ok), "returned": int(tot_all), "worst_rel_err_vs_fp64": worst,
-                           "distinct_verified": int(tot_distinct) if n_distinct is not None else None},
+            "eigenpairs": {"verified": int(tot_ok), "returned_on_verified_speeds": int(tot_all),
+                           "returned_all_speeds": int(tot_returned), "worst_rel_err_vs_fp64": worst,
+                           "distinct_verified": int(tot_distinct),
+                           "returned_per_s_all_speeds": tot_returned / t_dev_all if t_dev_all > 0 else None},
             "fp64_gpu": {"value": fp64_pairs / (fp64_ms / 1e3) if fp64_ms > 0 else None, "unit": UNIT,
-                         "ms_per_step": fp64_ms / max(len(timed), 1)},
+                         "ms_per_step": fp64_ms / max(len(vidx), 1), "speeds": len(vidx) if not args.no_verify else 0},
             "e2e": {"value": tot_ok / t_wall if t_wall > 0 else 0.0, "unit": UNIT,
-                    "h2d_bytes_per_step": 8 + 4 * max(len(hi), 19), "d2h_bytes_per_step": int(d2h / max(len(timed), 1))},
+                    "h2d_bytes_per_step": 8 + 4 * max(len(hi), 19),
+                    "d2h_bytes_per_step": int(np.mean(d2h)) if d2h else 0},
             "gpu_launches": launches,
             "roofline": {"kernel": f"shift-invert triangular solve of the {len(mesh_k)} complex harmonics "
                                    "(supernodal sweeps, one CUDA graph per batched solve)",
@@ -374,8 +527,11 @@ def main():
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
             "cpu_baseline": cpu,
             "serving": serving,
+            "skipped": skipped,
             "clocks": clk,
         }
+        if line["fp64_gpu"]["value"]:
+            line["mixed_over_fp64_gpu"] = line["value"] / line["fp64_gpu"]["value"]
         print(json.dumps(line), flush=True)
 
 

@@ -97,6 +97,19 @@ int tmg_create(int device, size_t mem_budget_bytes, tmg_context** out);
  * memory_reserve_fraction argument of solve_at_rpm (python_bindings.cpp:340-360,
  * cyclic_solver.cpp:1226-1273). */
 int tmg_set_memory_budget(tmg_context* ctx, size_t mem_budget_bytes);
+
+/* Options of later solves (tmg_set_option / tmg_get_option).
+ * TMG_OPT_SHIFT: the shift sigma of the standard path's shift-invert operator K_k - sigma M_k
+ *   (default 1.0, the value the reference hardcodes at cyclic_solver.cpp:1017).  An extension
+ *   of the reference, which has no such argument.
+ * TMG_OPT_DEFLATE: 1 = deflate the FP64 refinement CG of a mixed solve with the lowest
+ *   eigenvectors each complex harmonic found at the previous speed of the same operator
+ *   pattern (default 0).  Method change only: results equal the undeflated ones to the
+ *   refinement tolerance. */
+#define TMG_OPT_SHIFT 0
+#define TMG_OPT_DEFLATE 1
+int tmg_set_option(tmg_context* ctx, int option, double value);
+int tmg_get_option(tmg_context* ctx, int option, double* value);
 int tmg_destroy(tmg_context* ctx);
 const char* tmg_last_error(const tmg_context* ctx);
 
@@ -182,8 +195,10 @@ int tmg_profile_solve(tmg_context* ctx, double* out);
  *  - One scratch array per device is shared by every context on that device: calls that
  *    overlap in time on one device (two host threads, or two contexts) race on it.  The call
  *    synchronises its stream before returning, so calls made one after another are safe.
- *  - The first call on a device looks the array's address up (cudaGetSymbolAddress, with the
- *    context's device current); make that first call before any stream capture begins.
+ *  - Every call made outside a stream capture looks the array's address up
+ *    (cudaGetSymbolAddress, with the context's device current), so a primary context that was
+ *    reset and re-created is followed; a call made during a capture reuses the address of the
+ *    last call outside one.  Make the first call on a device before any stream capture begins.
  * Pass NULL arrays to query *nnz and *n. */
 int tmg_projection_harmonic_static(tmg_context* ctx, int which, int k, int64_t* nnz, int32_t* n,
                                    int32_t* colptr, int32_t* rowidx, double* values);

@@ -59,6 +59,14 @@ def lib():
         L.orc_solve.restype = C.c_int
         L.orc_result_info.argtypes = [C.c_void_p, C.c_int, _I, C.POINTER(C.c_double)]
         L.orc_result_copy.argtypes = [C.c_void_p, C.c_int, _D, C.c_void_p, _I]
+        L.orc_lw_create.restype = C.c_void_p
+        L.orc_lw_create.argtypes = [C.c_int, _I, _I, _D]
+        L.orc_lw_add_slot.restype = C.c_int
+        L.orc_lw_add_slot.argtypes = [C.c_void_p]
+        L.orc_lw_free.argtypes = [C.c_void_p]
+        L.orc_lw_info.argtypes = [C.c_void_p, _D]
+        L.orc_lw_cumwork.argtypes = [C.c_void_p, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")]
+        L.orc_lw_run.argtypes = [C.c_void_p, C.c_int, _I, _I, _I, _D, C.c_void_p]
         _LIB = L
     return _LIB
 
@@ -192,3 +200,60 @@ def lanczos(K: sp.csc_matrix, M: sp.csc_matrix, nev: int, ncv: int = 0, shift: f
                         maxit, ev, vec, info)
     m = int(info[0])
     return ev[:m], vec[: 2 * n * m].view(np.complex128).reshape(m, n).T, info
+
+
+def _lower_z(A):
+    A = sp.csc_matrix(sp.tril(sp.csc_matrix(A, dtype=np.complex128)))
+    A.sort_indices()
+    return (A.shape[0], A.indptr.astype(np.int32), A.indices.astype(np.int32),
+            np.ascontiguousarray(A.data).view(np.float64))
+
+
+class LdlWindows:
+    """Timing samples of the reference's up-looking LDL^H (Eigen SimplicialLDLT, restated in
+    orc_amd.hpp) on one operator: the complete structure of L from the symbolic analysis, one
+    slot of L values per thread, row windows of the numeric loop and whole solves timed on
+    concurrent threads (orc_window.hpp)."""
+
+    def __init__(self, A):
+        n, p, i, x = _lower_z(A)
+        self._h = lib().orc_lw_create(n, p, i, x)
+        if not self._h:
+            raise RuntimeError("orc_lw_create failed")
+        info = self.info()
+        self.n = int(info[0])
+        self.nnz_l = int(info[1])
+        self.total_work = int(info[2])
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_lw_free(self._h)
+            self._h = None
+
+    def add_slot(self) -> int:
+        """One more slot (own L values, shared operator); returns the number of slots."""
+        r = lib().orc_lw_add_slot(self._h)
+        if r < 0:
+            raise MemoryError("orc_lw_add_slot failed")
+        return r
+
+    def info(self) -> np.ndarray:
+        out = np.zeros(4)
+        lib().orc_lw_info(self._h, out)
+        return out
+
+    def cumwork(self) -> np.ndarray:
+        cum = np.zeros(self.n + 1, np.int64)
+        lib().orc_lw_cumwork(self._h, cum)
+        return cum
+
+    def run(self, slots, a, b, solve: bool = True):
+        """Concurrent samples: thread t times rows [a[t], b[t]) of the numeric loop on slot
+        slots[t], then (solve=True) one solve; returns (factor seconds, solve seconds)."""
+        slots = np.ascontiguousarray(slots, dtype=np.int32)
+        a = np.ascontiguousarray(a, dtype=np.int32)
+        b = np.ascontiguousarray(b, dtype=np.int32)
+        tf = np.zeros(len(slots))
+        ts = np.zeros(len(slots))
+        lib().orc_lw_run(self._h, len(slots), slots, a, b, tf, ts.ctypes.data if solve else None)
+        return tf, ts

@@ -4,6 +4,7 @@
 #include <cstring>
 
 #include "orc_cyclic.hpp"
+#include "orc_window.hpp"
 
 using namespace orc;
 
@@ -206,6 +207,45 @@ void orc_result_copy(void* hv, int idx, double* freqs, double* shapes, int* whir
     std::memcpy(freqs, r.frequencies.data(), sizeof(double) * r.frequencies.size());
     if (shapes) std::memcpy(shapes, r.mode_shapes.data(), sizeof(double) * 2 * r.mode_shapes.size());
     std::memcpy(whirl, r.whirl.data(), sizeof(int) * r.whirl.size());
+}
+
+// ---- timing samples of the reference's factorisation (orc_window.hpp) ----
+// Operator given by its lower triangle (CSC, complex interleaved values).
+void* orc_lw_create(int n, const int* p, const int* i, const double* x) {
+    auto* w = new LdlWindows();
+    try {
+        w->analyze(csc_z(n, p, i, x));
+    } catch (...) { delete w; return nullptr; }
+    return w;
+}
+
+int orc_lw_add_slot(void* h) {
+    auto* w = static_cast<LdlWindows*>(h);
+    try {
+        w->add_slot();
+    } catch (...) { return -1; }
+    return (int)w->slots.size();
+}
+
+void orc_lw_free(void* h) { delete static_cast<LdlWindows*>(h); }
+
+// out: [0] n, [1] nnz(L), [2] total inner-loop updates, [3] slots
+void orc_lw_info(void* h, double* out) {
+    auto* w = static_cast<LdlWindows*>(h);
+    out[0] = w->n;
+    out[1] = (double)w->nnz_l();
+    out[2] = (double)w->cum[w->n];
+    out[3] = (double)w->slots.size();
+}
+
+// cum[0..n]: inner-loop updates of the rows before each row
+void orc_lw_cumwork(void* h, long long* cum) {
+    auto* w = static_cast<LdlWindows*>(h);
+    for (int k = 0; k <= w->n; k++) cum[k] = w->cum[k];
+}
+
+void orc_lw_run(void* h, int nt, const int* slot, const int* a, const int* b, double* t_fact, double* t_solve) {
+    static_cast<LdlWindows*>(h)->run(nt, slot, a, b, t_fact, t_solve);
 }
 
 }  // extern "C"

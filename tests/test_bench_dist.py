@@ -70,19 +70,53 @@ def test_distinct_verified_counts_each_pair_once():
     assert bench.count_verified(mix, ref)[0] == 2 + 5
 
 
-def test_reference_arm_prints_its_line():
-    """bench.py --impl reference (the reference's CPU algorithm, timed on the host cores) prints one
-    JSON line with the contract's keys; it needs no GPU."""
+def test_reference_arm_prints_its_line(monkeypatch, capsys):
+    """bench.py --impl reference (the reference's CPU algorithm sampled on the host cores) prints
+    one JSON line with the contract's keys; it needs no GPU.  The sampler runs here on the
+    config-0 sector to keep the CPU suite short (the bench uses the config-1 sector)."""
     import json
-    import subprocess
-    import sys
 
-    from conftest import ROOT
+    import bench
+    from turbomodal_gb300.meshgen import config_mesh
 
-    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0"],
-                         cwd=ROOT, check=True, capture_output=True, text=True, timeout=600).stdout
-    line = json.loads(out.strip().splitlines()[-1])
+    small = config_mesh(0)
+
+    class Small(bench.ReferenceSample):
+        def __init__(self, threads=None, target_window_s=4.0, planned_samples=0, mesh=None):
+            super().__init__(threads=2, target_window_s=0.05, planned_samples=planned_samples, mesh=small)
+
+    monkeypatch.setattr(bench, "ReferenceSample", Small)
+    args = bench.argparse.Namespace(gpus=1, steps=2, warmup=1)
+    bench.run_reference(args, 1, 0, None)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["value"] > 0 and line["higher_is_better"] is True
+    assert line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
     assert line["e2e"]["value"] == line["value"] and line["e2e"]["h2d_bytes_per_step"] == 0
-    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
-    assert line["metric"] and line["unit"] and line["config"]["workload"]
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] == 2
+    assert line["steps"] == 2 and line["ms_per_step"] > 0 and line["config"]["workload"]
+
+
+def test_window_samples_add_up_to_the_whole_factorisation():
+    """The reference sampler's estimate of one factorisation (W equal-work row windows of the
+    up-looking LDL^H, each timed alone) against the same loop run over all rows at once, on the
+    config-0 harmonic operator: within 30 % (the windows start with cold caches), and the loop
+    work the symbolic pass counts equals sum_j c_j (c_j + 1) / 2 over the column counts."""
+    import scipy.sparse as sp
+
+    from oracle import orc
+    from turbomodal_gb300.meshgen import TITANIUM, config_mesh
+
+    om = orc.OracleModel(config_mesh(0), TITANIUM)
+    om.prepare(0.0)
+    A = (om.matrix("Kk", k=1) - om.matrix("Mk", k=1)).tocsc()
+    lw = orc.LdlWindows(A)
+    _, _, cc = orc.ldl_symbolic(sp.tril(A).tocsc())
+    assert lw.total_work == int(np.sum(cc.astype(np.int64) * (cc + 1) // 2))
+    cum = lw.cumwork()
+    assert cum[0] == 0 and cum[-1] == lw.total_work and np.all(np.diff(cum) >= 0)
+    full = min(lw.run([0], [0], [lw.n], solve=False)[0][0] for _ in range(3))
+    W = 16
+    bnd = np.searchsorted(cum, np.linspace(0, cum[-1], W + 1))
+    bnd[0], bnd[-1] = 0, lw.n
+    parts = [min(lw.run([0], [bnd[j]], [bnd[j + 1]], solve=False)[0][0] for _ in range(3)) for j in range(W)]
+    assert 0.7 * full <= sum(parts) <= 1.3 * full, (full, sum(parts))

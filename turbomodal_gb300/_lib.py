@@ -27,7 +27,9 @@ STATIC_SCRATCH_ENTRIES = 524288   # TMG_STATIC_SCRATCH_ENTRIES
 EXPORTED = ["tmg_create", "tmg_destroy", "tmg_last_error", "tmg_upload_sector", "tmg_assemble",
             "tmg_prepare", "tmg_projection", "tmg_symbolic", "tmg_solve_at_rpm", "tmg_result_info",
             "tmg_result_copy", "tmg_last_timing", "tmg_symbolic_stats",
-            "tmg_set_profiling", "tmg_profile_solve", "tmg_projection_harmonic_static", "tmg_set_memory_budget"]
+            "tmg_set_profiling", "tmg_profile_solve", "tmg_projection_harmonic_static", "tmg_set_memory_budget",
+            "tmg_set_option", "tmg_get_option"]
+OPT = {"shift": 0, "deflate": 1}
 
 
 class SectorDesc(C.Structure):
@@ -83,6 +85,8 @@ def load(build_if_missing: bool = True):
     L.tmg_profile_solve.argtypes = [P, DP]
     L.tmg_projection_harmonic_static.argtypes = [P, C.c_int, C.c_int, I64P, I32P, I32P, I32P, DP]
     L.tmg_set_memory_budget.argtypes = [P, C.c_size_t]
+    L.tmg_set_option.argtypes = [P, C.c_int, C.c_double]
+    L.tmg_get_option.argtypes = [P, C.c_int, DP]
     _lib = L
     return L
 

@@ -429,6 +429,7 @@ struct tmg_context {
     // TMG_DEFLATE when the context is created): the DEFL_M lowest eigenvectors of every complex
     // harmonic from the last solve, valid while the operator pattern keeps `recycle_key`.
     bool deflate = false;
+    double shift = 1.0;           // sigma of the standard path (cyclic_solver.cpp:1017)
     std::string recycle_key;
     std::map<int, DVec<zd>> recycle;
     struct Qep {
@@ -1921,7 +1922,7 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
     const int N = S.ns, max_k = N / 2;
     const double alpha = 2.0 * PI / N;
     const bool mixed = precision == TMG_PREC_MIXED;
-    const double shift = 1.0;
+    const double shift = c->shift;
     results.assign(ks.size(), ResultHost{});
     std::vector<Problem> cplx, real0, realh, dense, qep;
     for (size_t q = 0; q < ks.size(); q++) {
@@ -2189,7 +2190,6 @@ int tmg_create(int device, size_t mem_budget_bytes, tmg_context** out) {
         }
     }
     c->budget = mem_budget_bytes ? mem_budget_bytes : (size_t)(0.9 * (double)device_free_bytes(device));
-    c->deflate = std::getenv("TMG_DEFLATE") != nullptr;
     *out = c;
     return TMG_OK;
 }
@@ -2200,6 +2200,31 @@ int tmg_set_memory_budget(tmg_context* c, size_t mem_budget_bytes) {
         c->budget = mem_budget_bytes ? mem_budget_bytes : (size_t)(0.9 * (double)device_free_bytes(c->device));
         return TMG_OK;
     });
+}
+
+int tmg_set_option(tmg_context* c, int option, double value) {
+    if (!c) return TMG_ERR_ARG;
+    switch (option) {
+        case TMG_OPT_SHIFT:
+            if (!std::isfinite(value)) return set_err(c, TMG_ERR_ARG, "shift must be finite");
+            c->shift = value;
+            return TMG_OK;
+        case TMG_OPT_DEFLATE:
+            c->deflate = value != 0.0;
+            if (!c->deflate) c->recycle.clear();
+            return TMG_OK;
+        default:
+            return set_err(c, TMG_ERR_ARG, "unknown option " + std::to_string(option));
+    }
+}
+
+int tmg_get_option(tmg_context* c, int option, double* value) {
+    if (!c || !value) return TMG_ERR_ARG;
+    switch (option) {
+        case TMG_OPT_SHIFT: *value = c->shift; return TMG_OK;
+        case TMG_OPT_DEFLATE: *value = c->deflate ? 1.0 : 0.0; return TMG_OK;
+        default: return set_err(c, TMG_ERR_ARG, "unknown option " + std::to_string(option));
+    }
 }
 
 int tmg_destroy(tmg_context* c) {
@@ -2511,13 +2536,17 @@ constexpr int kMaxScratchDevices = 64;
 std::mutex g_scratch_mu;
 void* g_scratch_addr[kMaxScratchDevices] = {};
 
-// Address of this device's copy of the scratch array, looked up once per device with the
-// device current (the caller made it current).
-zd* static_scratch(int device) {
+// Address of this device's copy of the scratch array, with the device current (the caller
+// made it current).  It is looked up again on every call made outside a stream capture, so a
+// primary context that was reset and re-created gets its new address; a call made while the
+// stream is being captured uses the address recorded by the last call outside a capture.
+zd* static_scratch(int device, cudaStream_t st) {
     if (device < 0 || device >= kMaxScratchDevices)
         throw std::invalid_argument("device ordinal beyond the static-scratch table");
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) cs = cudaStreamCaptureStatusNone;
     std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_addr[device]) {
+    if (!g_scratch_addr[device] || cs == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_harmonic_scratch);
         if (e != cudaSuccess)
@@ -2561,7 +2590,7 @@ extern "C" int tmg_projection_harmonic_static(tmg_context* c, int which, int k, 
                                                std::to_string((long long)TMG_STATIC_SCRATCH_ENTRIES) +
                                                " (use tmg_projection)");
         if (!colptr) return TMG_OK;
-        zd* out = static_scratch(c->device);
+        zd* out = static_scratch(c->device, c->st);
         const double alpha = 2.0 * PI / S.ns;
         if (ne)
             TMG_LAUNCH(k_form_csum_static, nblk(ne), 256, 0, c->st, ne, w.maps[0].p, w.maps[1].p, w.maps[2].p, cc.sv.p,

@@ -155,7 +155,7 @@ __global__ void k_beta_scale(int64_t n, int j, const T* __restrict__ dot, const 
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i == 0) {
         beta[p * ldab + j] = b;
-        if (b < 1e-14 && flag[p] == 0) flag[p] = j + 1;
+        if (!(b >= 1e-14) && flag[p] == 0) flag[p] = j + 1;   // NaN counts as a breakdown
     }
     if (i >= n) return;
     const double ib = 1.0 / b;
@@ -222,6 +222,7 @@ __global__ void __launch_bounds__(256) k_tridiag(int m, int ldab, int nev, doubl
                 if (fabs(e[mm]) <= eps * tst1) break;
                 mm++;
             }
+            if (mm >= m) mm = m - 1;   // NaN in alpha / beta: no split found, stay inside d[], e[]
             s_m = mm;
             s_go = (mm > l) ? 1 : 0;
         }

@@ -86,11 +86,12 @@ class CyclicSymmetrySolver:
     """GPU cyclic-symmetry modal solver for one sector mesh and material."""
 
     def __init__(self, mesh: Mesh, material: Material, fluid=None, apply_hub_constraint: bool = True,
-                 device: int = 0, precision: str = "fp64", mem_budget_bytes: int = 0):
+                 device: int = 0, precision: str = "fp64", mem_budget_bytes: int = 0, deflate: bool = False):
         if fluid is not None and getattr(fluid, "type", None) not in (None, 0, "NONE"):
             raise NotImplementedError("fluid coupling is not part of the GPU path")
         self.mesh = mesh
         self.material = material
+        self.apply_hub_constraint = bool(apply_hub_constraint)
         self.precision = precision
         self.ctx = _lib.Context(device, mem_budget_bytes)
         hub = mesh.find_node_set("hub_constraint") if apply_hub_constraint else None
@@ -109,14 +110,38 @@ class CyclicSymmetrySolver:
             len(k["left"]), _lib.ptr(k["left"], C.c_int32), len(k["right"]), _lib.ptr(k["right"], C.c_int32),
             len(mesh.matched_pairs), _lib.ptr(k["pairs"], C.c_int32), len(k["hub"]), _lib.ptr(k["hub"], C.c_int32))
         self.ctx.check(self.ctx.L.tmg_upload_sector(self.ctx.h, C.byref(d)), "tmg_upload_sector")
+        if deflate:
+            self.set_option("deflate", 1.0)
+
+    def set_option(self, name: str, value: float) -> None:
+        """tmg_set_option: "shift" (sigma of the standard path, default 1.0 as the reference's
+        src/cyclic_solver.cpp:1017) or "deflate" (1 = deflate the mixed refinement CG with the
+        previous speed's eigenvectors)."""
+        self.ctx.check(self.ctx.L.tmg_set_option(self.ctx.h, _lib.OPT[name], float(value)), "tmg_set_option")
+
+    def get_option(self, name: str) -> float:
+        v = C.c_double()
+        self.ctx.check(self.ctx.L.tmg_get_option(self.ctx.h, _lib.OPT[name], C.byref(v)), "tmg_get_option")
+        return v.value
 
     # --- modal solve -------------------------------------------------------------------
     def solve_at_rpm(self, rpm: float, num_modes_per_harmonic: int, harmonic_indices=(), max_threads: int = 0,
                      include_coriolis: bool = False, min_frequency: float = 0.0, progress_cb=None,
                      allow_condensation: bool = False, memory_reserve_fraction: float = 0.2,
-                     precision: str | None = None) -> list[ModalResult]:
+                     precision: str | None = None, shift: float | None = None) -> list[ModalResult]:
         """Modal solve at one speed (src/python_bindings.cpp:332-361).  With include_coriolis,
-        harmonics k > 0 solve the Lancaster QEP and carry whirl directions +1 / -1."""
+        harmonics k > 0 solve the Lancaster QEP and carry whirl directions +1 / -1.  Extensions,
+        defaulting to the reference's behaviour: `precision`, and `shift` (sigma of the standard
+        path for this call; the reference uses 1.0)."""
+        if shift is not None:
+            old = self.get_option("shift")
+            self.set_option("shift", shift)
+            try:
+                return self.solve_at_rpm(rpm, num_modes_per_harmonic, harmonic_indices, max_threads, include_coriolis,
+                                         min_frequency, progress_cb, allow_condensation, memory_reserve_fraction,
+                                         precision)
+            finally:
+                self.set_option("shift", old)
         prec = _lib.PREC[precision or self.precision]
         t_call = time.perf_counter()
         hi = np.asarray(list(harmonic_indices or []), dtype=np.int32)
@@ -336,7 +361,8 @@ def solve(mesh: Mesh, material: Material, rpm: float = 0.0, num_modes: int = 20,
     given) temperature; `config` is accepted and unused, as in the reference.  Constraint groups
     (`boundary_conditions`) and fluid coupling are not on the GPU path and raise
     NotImplementedError; `show_convergence` (a live plot) is not available and only warns.
-    Keyword-only: `precision` ("fp64" or "mixed") and a `solver` to reuse."""
+    Keyword-only: `precision` ("fp64" or "mixed") and a `solver` to reuse, which must have been
+    built for this mesh, material (after `temperature`) and hub constraint (else ValueError)."""
     if condition is not None:
         rpm = condition.rpm
         if temperature is None:
@@ -352,6 +378,8 @@ def solve(mesh: Mesh, material: Material, rpm: float = 0.0, num_modes: int = 20,
         print(f"Solving at {rpm:.0f} RPM{cor}{tmp}  ({mesh.num_nodes()} nodes, {mesh.num_elements()} elements, "
               f"{mesh.num_sectors} sectors, {nd}, {num_modes} modes/ND)")
     t0 = time.perf_counter()
+    if solver is not None:
+        _check_reused_solver(solver, mesh, material, hub_constraint == "fixed")
     s = solver or CyclicSymmetrySolver(mesh, material, fluid, hub_constraint == "fixed", precision=precision)
     res = s.solve_at_rpm(rpm, num_modes, hi, max_threads, include_coriolis, min_frequency,
                          memory_reserve_fraction=memory_reserve_fraction, precision=precision)
@@ -368,6 +396,21 @@ def solve(mesh: Mesh, material: Material, rpm: float = 0.0, num_modes: int = 20,
             print(f"    ND={r.harmonic_index:2d}: [{freqs}] Hz (rotating frame)")
             print(f"           modal mass [kg]: [{mm}]")
     return out
+
+
+def _check_reused_solver(solver, mesh, material, apply_hub: bool) -> None:
+    """A solver passed to solve() keeps the sector, material and hub constraint it was built
+    with; a call asking for different ones (another mesh, a temperature that changes E, another
+    hub_constraint) would otherwise be answered for the solver's own, so it is refused."""
+    if solver.mesh is not mesh:
+        raise ValueError("solve(..., solver=s): s was built for another mesh")
+    a, b = solver.material, material
+    if not all(np.isclose(getattr(a, f), getattr(b, f), rtol=1e-12, atol=0.0) for f in ("E", "nu", "rho")):
+        raise ValueError(f"solve(..., solver=s): s was built for material (E={a.E:g}, nu={a.nu:g}, rho={a.rho:g}); "
+                         f"this call asks for (E={b.E:g}, nu={b.nu:g}, rho={b.rho:g}) (temperature or material "
+                         "differ); build a new solver")
+    if solver.apply_hub_constraint != apply_hub:
+        raise ValueError("solve(..., solver=s): s was built with another hub_constraint")
 
 
 def rpm_sweep(mesh: Mesh, material: Material, rpm_values, num_modes: int = 20, fluid=None, verbose: int = SILENT,
