@@ -105,9 +105,13 @@ int tmg_set_memory_budget(tmg_context* ctx, size_t mem_budget_bytes);
  * TMG_OPT_DEFLATE: 1 = deflate the FP64 refinement CG of a mixed solve with the lowest
  *   eigenvectors each complex harmonic found at the previous speed of the same operator
  *   pattern (default 0).  Method change only: results equal the undeflated ones to the
- *   refinement tolerance. */
+ *   refinement tolerance.
+ * TMG_OPT_TENSOR_CORES: 1 = the complex FP32 factorisation of the mixed path runs its large
+ *   trailing Schur updates on the tensor cores (3xTF32, tcgen05); 0 = on the FP32 SIMT pipe
+ *   (default 1).  Method change only, as above. */
 #define TMG_OPT_SHIFT 0
 #define TMG_OPT_DEFLATE 1
+#define TMG_OPT_TENSOR_CORES 2
 int tmg_set_option(tmg_context* ctx, int option, double value);
 int tmg_get_option(tmg_context* ctx, int option, double* value);
 int tmg_destroy(tmg_context* ctx);
@@ -159,16 +163,34 @@ int tmg_symbolic_stats(tmg_context* ctx, int kind, double* out);
 int tmg_solve_at_rpm(tmg_context* ctx, double rpm, int num_modes, const int32_t* harmonics, int nh,
                      int coriolis, double min_frequency, int precision, int32_t* num_results);
 
+/* Modal solves at several speeds; replaces CyclicSymmetrySolver::solve_rpm_sweep
+ * (cyclic_solver.cpp:1359-1373), which calls solve_at_rpm once per speed.  On the standard path
+ * the harmonics of several speeds (consecutive speeds with the same operator pattern, as many
+ * as the memory budget holds) are factorised and iterated as one batch; each result equals
+ * what tmg_solve_at_rpm returns at its speed.  Results: speed-major in the order of rpms,
+ * harmonics ascending within a speed (tmg_result_info gives each one's rpm and k); a failed
+ * harmonic keeps its place with a nonzero status. */
+int tmg_solve_sweep(tmg_context* ctx, const double* rpms, int nrpm, int num_modes, const int32_t* harmonics, int nh,
+                    int coriolis, double min_frequency, int precision, int32_t* num_results);
+
 /* Result access (ModalResult fields, modal_solver.hpp:8-15).  shapes: num_dof x num_modes
  * complex interleaved, column-major; NULL skips the copy. */
 int tmg_result_info(tmg_context* ctx, int idx, tmg_result_meta* info);
 int tmg_result_copy(tmg_context* ctx, int idx, double* freqs, double* shapes, int32_t* whirl);
 
+/* Modal mass of every mode of a result, N * Re(phi^H M_sector phi) in kg over the full annulus,
+ * computed on the device from the expanded shapes and the sector mass matrix.  Replaces the
+ * reference's _modal_mass_from_M over a second host assembly (python/turbomodal/solver.py:91-114).
+ * mass: num_modes doubles. */
+int tmg_result_modal_mass(tmg_context* ctx, int idx, double* mass);
+
 /* Time (ms) of the phases of the last tmg_solve_at_rpm: [0] prepare (assembly, prestress,
  * projections), [1] factorisations, [2] Lanczos, [3] post-processing, [4] the whole call
  * measured with CUDA events on the context's stream; counts: [5] batched triangular solves,
- * [6] shift-invert applications, [7] most refinement iterations of one application; and the
- * number of this library's kernel launches in it. */
+ * [6] shift-invert applications, [7] most refinement iterations of one application, [8] problems
+ * of a mixed-precision batch solved again on the FP64 path (an FP32 zero pivot, a breakdown or
+ * a refinement that stalled; cyclic_solver.cpp:1334-1342 retries failed harmonics likewise); and
+ * the number of this library's kernel launches in it. */
 int tmg_last_timing(tmg_context* ctx, double* phase_ms, int nphase, int64_t* kernel_launches);
 
 /* Profiling mode (measurement only; it synchronises after every triangular solve): CUDA-event

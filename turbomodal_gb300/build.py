@@ -27,6 +27,7 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-I" + CSRC]
 UNITS = [
     ("fe.cu", ["--fmad=false"]),
     ("mf.cu", []),
+    ("mf_tc.cu", []),
     ("lz.cu", []),
     ("engine.cu", []),
     ("dense.cu", []),

@@ -154,6 +154,45 @@ __global__ void k_expand(int32_t nfull, const int64_t* __restrict__ rp, const in
     out[v * ldo + i] = isr[i] ? s * P : s;
 }
 
+// Modal mass N Re(phi^H M phi) of every expanded mode (python/turbomodal/solver.py:91-103): one
+// warp per sector column j forms (M phi)_j over the candidate pattern (M is symmetric, so its
+// CSC columns are its rows) and multiplies by conj(phi_j); each CTA writes its partial sum,
+// and k_mass_sum adds the partials in a fixed order (deterministic).
+constexpr int MASS_BLOCKS = 304;
+__global__ void __launch_bounds__(256) k_mass_part(int32_t ndof, const int64_t* __restrict__ cp,
+                                                   const int32_t* __restrict__ ci, const double* __restrict__ mv,
+                                                   const zd* __restrict__ phi, int64_t ldp, double* __restrict__ part) {
+    __shared__ double red[8];
+    const int64_t v = blockIdx.y;
+    const zd* f = phi + v * ldp;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double acc = 0.0;
+    for (int64_t j = (int64_t)blockIdx.x * 8 + warp; j < ndof; j += (int64_t)gridDim.x * 8) {
+        zd y{0.0, 0.0};
+        for (int64_t q = cp[j] + lane; q < cp[j + 1]; q += 32) y += mv[q] * f[ci[q]];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            y.x += __shfl_xor_sync(0xffffffffu, y.x, o);
+            y.y += __shfl_xor_sync(0xffffffffu, y.y, o);
+        }
+        acc += f[j].x * y.x + f[j].y * y.y;   // Re(conj(phi_j) y_j)
+    }
+    if (lane == 0) red[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < 8; q++) t += red[q];
+        part[v * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+__global__ void k_mass_sum(int nb, const double* __restrict__ part, double scale, double* __restrict__ out) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    double t = 0.0;
+    for (int q = 0; q < nb; q++) t += part[(int64_t)v * nb + q];
+    out[v] = scale * t;
+}
+
 __global__ void k_real_to_complex(int64_t n, const double* __restrict__ a, zd* __restrict__ b) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) b[i] = zd{a[i], 0.0};
@@ -370,6 +409,7 @@ struct ResultHost {
     std::vector<double> freqs;
     std::vector<int32_t> whirl;
     std::vector<zd> shapes;          // ndof x m
+    std::vector<double> modal_mass;  // N Re(phi^H M phi) per mode (full annulus)
     int32_t converged = 0, iterations = 0, status = 0;
     double max_residual = 0.0, refine_residual = 0.0;
     int64_t solves = 0, applies = 0;
@@ -430,6 +470,7 @@ struct tmg_context {
     // harmonic from the last solve, valid while the operator pattern keeps `recycle_key`.
     bool deflate = false;
     double shift = 1.0;           // sigma of the standard path (cyclic_solver.cpp:1017)
+    bool tensor_cores = true;     // tcgen05 trailing updates in the complex FP32 factorisation
     std::string recycle_key;
     std::map<int, DVec<zd>> recycle;
     struct Qep {
@@ -440,7 +481,7 @@ struct tmg_context {
         std::string key;
     } qep;
     std::vector<ResultHost> results;
-    double phase_ms[8] = {0};
+    double phase_ms[9] = {0};
     int64_t launches = 0;
     // expansion maps (CSR of T(0), right-DOF flags, reduced -> free)
     DVec<int64_t> dT0_rp;
@@ -1206,7 +1247,7 @@ struct ShiftInvertB {
         DVec<int> status;
         status.alloc(2 * B);
         status.zero(c->st);
-        mf_factor<Tf>(c->st, *D, bt, status.p);
+        mf_factor<Tf>(c->st, *D, bt, status.p, c->tensor_cores);
         mf_count_nonpos<Tf>(c->st, *D, bt, status.p + B);
         std::vector<int> hs(2 * B);
         TMG_CUDA(cudaMemcpyAsync(hs.data(), status.p, 2 * B * sizeof(int), cudaMemcpyDeviceToHost, c->st));
@@ -1571,7 +1612,19 @@ void expand_to_sector(tmg_context* c, const Problem& pr, const zd* X, int nm, Re
                        c->d_isr.p, c->d_r2free.p, X, (int64_t)S.n_free, pr.P, full.p, (int64_t)ndof);
     TMG_CHECK_LAUNCH();
     R.shapes.resize((size_t)ndof * nm);
+    R.modal_mass.assign(nm, 0.0);
     if (nm) {
+        // modal masses on the sector mass matrix (the one the solve assembled)
+        assemble_KM(c);
+        if (!S.dcand_i.p) S.dcand_i.upload(S.cand.i);
+        DVec<double> part, mm;
+        part.alloc((size_t)nm * MASS_BLOCKS);
+        mm.alloc(nm);
+        TMG_LAUNCH(k_mass_part, dim3(MASS_BLOCKS, nm), 256, 0, st, ndof, S.dcand_p.p, S.dcand_i.p, c->M.v.p, full.p,
+                   (int64_t)ndof, part.p);
+        TMG_LAUNCH(k_mass_sum, 1, nm, 0, st, MASS_BLOCKS, part.p, (double)S.ns, mm.p);
+        TMG_CHECK_LAUNCH();
+        TMG_CUDA(cudaMemcpyAsync(R.modal_mass.data(), mm.p, nm * sizeof(double), cudaMemcpyDeviceToHost, st));
         TMG_CUDA(cudaMemcpyAsync(R.shapes.data(), full.p, R.shapes.size() * sizeof(zd), cudaMemcpyDeviceToHost, st));
         TMG_CUDA(cudaStreamSynchronize(st));
     }
@@ -1915,6 +1968,28 @@ void solve_qep(tmg_context* c, std::vector<Problem>& probs, int num_modes, doubl
     }
 }
 
+// Problems of a mixed batch that the mixed path could not finish: an FP32 zero pivot or a
+// Lanczos breakdown (status TMG_ERR_NUMERIC), or refined solves that stalled above 100x their
+// target residual.  They are solved again on the plain FP64 path, as the reference retries the
+// harmonics that failed in its thread pool (src/cyclic_solver.cpp:1334-1342).
+std::vector<Problem> mixed_failures(tmg_context* c, const std::vector<Problem>& grp) {
+    std::vector<Problem> out;
+    for (const Problem& pr : grp) {
+        ResultHost& R = *pr.R;
+        if (R.status == TMG_ERR_NUMERIC || (R.status == TMG_OK && R.refine_residual > 1e-8)) {
+            ResultHost fresh;
+            fresh.k = R.k;
+            fresh.rpm = R.rpm;
+            R = fresh;
+            out.push_back(pr);
+        }
+    }
+    c->phase_ms[8] += (double)out.size();
+    if (!out.empty() && std::getenv("TMG_VERBOSE"))
+        std::fprintf(stderr, "[tmg] %zu problem(s) of a mixed batch solved again in FP64\n", out.size());
+    return out;
+}
+
 void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double min_frequency, int precision,
                std::vector<ResultHost>& results) {
     Sector& S = *c->sec;
@@ -2064,6 +2139,30 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
                 for (auto& pr : grp) pr.R->status = TMG_ERR_NUMERIC;
                 c->err = e.what();
             }
+            if (mixed) {
+                std::vector<Problem> again = mixed_failures(c, grp);
+                if (!again.empty()) {
+                    // the retried problems' operator and mass values, compacted to the batch's front
+                    DVec<double> v2, m2;
+                    v2.alloc((size_t)again.size() * nU);
+                    m2.alloc((size_t)again.size() * nMU);
+                    for (size_t q = 0; q < again.size(); q++) {
+                        size_t src = 0;
+                        while (grp[src].R != again[q].R) src++;
+                        if (nU) lz_copy<double>(st, nU, vals.p + src * nU, v2.p + q * nU);
+                        if (nMU) lz_copy<double>(st, nMU, mcsr.p + src * nMU, m2.p + q * nMU);
+                    }
+                    DevCsr<double> M2 = M;
+                    M2.val = m2.p;
+                    try {
+                        run_batch<double, double>(c, again, c->pairSym, um, v2.p, M2, nev, ncv, shift, 1000, false,
+                                                  num_modes, min_frequency);
+                    } catch (const numeric_error& e) {
+                        for (auto& pr : again) pr.R->status = TMG_ERR_NUMERIC;
+                        c->err = e.what();
+                    }
+                }
+            }
         }
     }
     // complex harmonics: one shared symbolic analysis, batched under the memory budget
@@ -2128,9 +2227,264 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
                 for (auto& pr : grp) pr.R->status = TMG_ERR_NUMERIC;
                 c->err = e.what();
             }
+            if (mixed) {
+                std::vector<Problem> again = mixed_failures(c, grp);
+                if (!again.empty()) {
+                    const int64_t nU = um.U.nnz(), nMU = mu.U.nnz();
+                    DVec<zd> v2, m2;
+                    v2.alloc((size_t)again.size() * nU);
+                    m2.alloc((size_t)again.size() * nMU);
+                    for (size_t q = 0; q < again.size(); q++) {
+                        size_t src = 0;
+                        while (grp[src].R != again[q].R) src++;
+                        if (nU) lz_copy<zd>(st, nU, vals.p + src * nU, v2.p + q * nU);
+                        if (nMU) lz_copy<zd>(st, nMU, mcsr.p + src * nMU, m2.p + q * nMU);
+                    }
+                    DevCsr<zd> M2 = M;
+                    M2.val = m2.p;
+                    try {
+                        run_batch<zd, zd>(c, again, c->symC, um, v2.p, M2, nev, ncv, shift, 1000, false, num_modes,
+                                          min_frequency);
+                    } catch (const numeric_error& e) {
+                        for (auto& pr : again) pr.R->status = TMG_ERR_NUMERIC;
+                        c->err = e.what();
+                    }
+                }
+            }
         }
     }
     if (!qep.empty()) solve_qep(c, qep, num_modes, min_frequency);
+    TMG_CUDA(cudaStreamSynchronize(st));
+}
+
+// Several speeds of a sweep in one pass (src/cyclic_solver.cpp:1359-1373 solves them one after
+// another).  The speeds are taken in groups that share the operator pattern (rest and speed
+// differ) and fit the device-memory budget; each speed of a group is prepared in turn and the
+// operator and mass values of its harmonics are formed into one multi-speed batch, so every
+// factorisation and Lanczos launch covers the harmonics of all speeds of the group.  Dense
+// (n <= 200) and Coriolis problems keep the per-speed path.  results: speed-major, harmonics in
+// the order of ks.
+void solve_sweep(tmg_context* c, const std::vector<double>& rpms, const std::vector<int>& ks, int num_modes,
+                 double min_frequency, int precision, std::vector<ResultHost>& results) {
+    Sector& S = *c->sec;
+    cudaStream_t st = c->st;
+    const int N = S.ns, max_k = N / 2;
+    const double alpha = 2.0 * PI / N;
+    const bool mixed = precision == TMG_PREC_MIXED;
+    const double shift = c->shift;
+    const size_t nk = ks.size();
+    results.assign(rpms.size() * nk, ResultHost{});
+    if (S.n_free <= 200) {   // dense path: per speed
+        for (size_t g = 0; g < rpms.size(); g++) {
+            prepare(c, rpms[g], false);
+            std::vector<ResultHost> r;
+            solve_set(c, ks, num_modes, min_frequency, precision, r);
+            std::copy(r.begin(), r.end(), results.begin() + g * nk);
+        }
+        return;
+    }
+    const int n_extra = min_frequency > 0.0 ? 6 : 0;
+    size_t g0 = 0;
+    while (g0 < rpms.size()) {
+        // the group: speeds after g0 with the pattern of g0 whose problems fit one batch
+        prepare(c, rpms[g0], false);
+        if (!c->symC.valid) analyze_op(c->symC, c->opC);
+        if (!c->pairSym.valid) analyze_op(c->pairSym, c->pairOp);
+        const std::string key = c->symC_key;
+        std::vector<int> cks, rks;
+        for (int k : ks) {
+            const bool is_real = (k == 0) || (N % 2 == 0 && k == max_k);
+            (is_real ? rks : cks).push_back(k);
+        }
+        int nev_c = 1, nev_r = 1;
+        for (int k : cks) nev_c = std::max(nev_c, std::min((num_modes + 1) / 2 + n_extra, S.n_free - 1));
+        for (int k : rks) nev_r = std::max(nev_r, std::min(num_modes + n_extra, S.n_free - 1));
+        (void)nev_r;
+        const int ncv_c = std::min(std::max(4 * nev_c + 1, 40), S.n_free);
+        UnionMaps& um = c->opC;
+        UnionMaps& mu = c->opMC;
+        const int64_t nU = um.U.nnz(), nMU = mu.U.nnz();
+        int per_speed = (int)cks.size();
+        int bmax = per_speed ? batch_size(c, c->symC, um, mu.U.nnz(), ncv_c, true, mixed, 1 << 20) : 1 << 20;
+        // value buffers of the group count against the same budget: one speed at least
+        const int gmax = std::max(1, per_speed ? bmax / std::max(1, per_speed) : (int)rpms.size());
+        std::vector<size_t> group{g0};
+        for (size_t g = g0 + 1; g < rpms.size() && (int)group.size() < gmax; g++) {
+            if ((rpms[g] == 0.0) != (rpms[g0] == 0.0)) break;   // rest and speed have different patterns
+            group.push_back(g);
+        }
+        const int G = (int)group.size();
+        const int Bc = G * per_speed, Br = G * (int)rks.size();
+        DVec<zd> cvals, cm;
+        DVec<double> rvals, rm;
+        cvals.alloc((size_t)std::max(1, Bc) * std::max<int64_t>(nU, 1));
+        cm.alloc((size_t)std::max(1, Bc) * std::max<int64_t>(nMU, 1));
+        const int64_t rnU = c->pairOp.U.nnz(), rnM = c->pairM.U.nnz();
+        rvals.alloc((size_t)std::max(1, Br) * std::max<int64_t>(rnU, 1));
+        rm.alloc((size_t)std::max(1, Br) * std::max<int64_t>(rnM, 1));
+        std::vector<Problem> cplx, real;
+        for (int gi = 0; gi < G; gi++) {
+            const size_t g = group[gi];
+            if (gi > 0) prepare(c, rpms[g], false);
+            if (c->symC_key != key) throw numeric_error("operator pattern changed inside a speed group");
+            for (size_t q = 0; q < nk; q++) {
+                const int k = ks[q];
+                ResultHost& R = results[g * nk + q];
+                R.k = k;
+                R.rpm = rpms[g];
+                Problem pr;
+                pr.k = k;
+                pr.P = zd{std::cos(k * alpha), std::sin(k * alpha)};
+                pr.R = &R;
+                pr.degenerate = (k > 0) && !(N % 2 == 0 && k == max_k);
+                pr.nev_target = pr.degenerate ? (num_modes + 1) / 2 : num_modes;
+                const bool is_real = (k == 0) || (N % 2 == 0 && k == max_k);
+                if (!is_real) {
+                    const int slot = (int)cplx.size();
+                    DVec<double> dph;
+                    dph.upload(std::vector<double>{pr.P.x, pr.P.y});
+                    if (nU)
+                        TMG_LAUNCH(k_form_complex, dim3(nblk(nU), 1), 256, 0, st, nU, um.maps[0].p, um.maps[1].p,
+                                   um.maps[2].p, um.maps[3].p, um.maps[4].p, um.maps[5].p, c->Kcf.sv.p, c->Kpf.sv.p,
+                                   c->Mcf.sv.p, c->Mpf.sv.p, dph.p, shift, cvals.p + (int64_t)slot * nU);
+                    if (nMU) {
+                        DVec<zd> mv;
+                        mv.alloc(nMU);
+                        TMG_LAUNCH(k_form_csum, dim3(nblk(nMU), 1), 256, 0, st, nMU, mu.maps[0].p, mu.maps[1].p,
+                                   mu.maps[2].p, c->Mcf.sv.p, c->Mpf.sv.p, dph.p, mv.p);
+                        TMG_LAUNCH(k_gather_b<zd>, dim3(nblk(nMU), 1), 256, 0, st, nMU, mu.csr2csc.p, mv.p, nMU,
+                                   cm.p + (int64_t)slot * nMU, nMU);
+                    }
+                    TMG_CUDA(cudaStreamSynchronize(st));   // dph, mv are freed at scope end
+                    cplx.push_back(pr);
+                } else {
+                    const auto& Rr = c->real[k == 0 ? 0 : 1];
+                    if (!Rr.valid) { R.status = TMG_ERR_STATE; continue; }
+                    const int slot = (int)real.size();
+                    if (rnU)
+                        TMG_LAUNCH(k_form_real_op, nblk(rnU), 256, 0, st, rnU, c->pairOp.maps[0].p, c->pairOp.maps[1].p,
+                                   Rr.Ks.p, Rr.Ms.p, shift, 1.0, rvals.p + (int64_t)slot * rnU);
+                    if (rnM) {
+                        DVec<double> mc;
+                        mc.alloc(rnM);
+                        TMG_LAUNCH(k_form_real_op, nblk(rnM), 256, 0, st, rnM, c->pairM.maps[0].p, c->pairM.maps[0].p,
+                                   Rr.Ms.p, Rr.Ms.p, 0.0, 1.0, mc.p);
+                        TMG_LAUNCH(k_gather_b<double>, dim3(nblk(rnM), 1), 256, 0, st, rnM, c->pairM.csr2csc.p, mc.p,
+                                   rnM, rm.p + (int64_t)slot * rnM, rnM);
+                        TMG_CUDA(cudaStreamSynchronize(st));
+                    }
+                    real.push_back(pr);
+                }
+            }
+        }
+        // real harmonics of the group: one batch (problem stride rnU / rnM)
+        if (!real.empty()) {
+            const int nev = std::min(real[0].nev_target + n_extra, S.n_free - 1);
+            const int ncv = std::min(std::max(4 * nev + 1, 40), S.n_free);
+            DevCsr<double> M;
+            M.nrows = S.n_free; M.nnz = rnM; M.rowptr = c->pairM.csr_rowptr.p; M.col = c->pairM.csr_col.p;
+            M.val = rm.p; M.vstride = rnM;
+            try {
+                if (mixed)
+                    run_batch<double, float>(c, real, c->pairSym, c->pairOp, rvals.p, M, nev, ncv, shift, 1000, true,
+                                             num_modes, min_frequency);
+                else
+                    run_batch<double, double>(c, real, c->pairSym, c->pairOp, rvals.p, M, nev, ncv, shift, 1000, false,
+                                              num_modes, min_frequency);
+            } catch (const numeric_error& e) {
+                for (auto& pr : real) pr.R->status = TMG_ERR_NUMERIC;
+                c->err = e.what();
+            }
+            if (mixed) {
+                std::vector<Problem> again = mixed_failures(c, real);
+                if (!again.empty()) {
+                    DVec<double> v2, m2;
+                    v2.alloc((size_t)again.size() * rnU);
+                    m2.alloc((size_t)again.size() * rnM);
+                    for (size_t q = 0; q < again.size(); q++) {
+                        size_t src = 0;
+                        while (real[src].R != again[q].R) src++;
+                        if (rnU) lz_copy<double>(st, rnU, rvals.p + src * rnU, v2.p + q * rnU);
+                        if (rnM) lz_copy<double>(st, rnM, rm.p + src * rnM, m2.p + q * rnM);
+                    }
+                    DevCsr<double> M2 = M;
+                    M2.val = m2.p;
+                    try {
+                        run_batch<double, double>(c, again, c->pairSym, c->pairOp, v2.p, M2, nev, ncv, shift, 1000,
+                                                  false, num_modes, min_frequency);
+                    } catch (const numeric_error& e) {
+                        for (auto& pr : again) pr.R->status = TMG_ERR_NUMERIC;
+                        c->err = e.what();
+                    }
+                }
+            }
+        }
+        rvals.release();
+        rm.release();
+        // complex harmonics of the group, in batches of at most bmax problems
+        for (size_t b0 = 0; b0 < cplx.size(); b0 += bmax) {
+            std::vector<Problem> grp(cplx.begin() + b0, cplx.begin() + std::min(cplx.size(), b0 + (size_t)bmax));
+            const int B = (int)grp.size();
+            const int nev = std::min(grp[0].nev_target + n_extra, S.n_free - 1);
+            const int ncv = std::min(std::max(4 * nev + 1, 40), S.n_free);
+            DevCsr<zd> M;
+            M.nrows = S.n_free; M.nnz = nMU; M.rowptr = mu.csr_rowptr.p; M.col = mu.csr_col.p;
+            M.val = cm.p + (int64_t)b0 * nMU; M.vstride = nMU;
+            const zd* vals = cvals.p + (int64_t)b0 * nU;
+            DVec<zd> Wd;
+            int md = 0;
+            if (mixed && c->deflate && c->recycle_key == c->symC_key) {
+                bool all = true;
+                for (const Problem& pr : grp) {
+                    auto it = c->recycle.find(pr.k);
+                    all = all && it != c->recycle.end() && it->second.n == (size_t)S.n_free * DEFL_M;
+                }
+                if (all) {
+                    const size_t nm = (size_t)S.n_free * DEFL_M;
+                    Wd.alloc((size_t)B * nm);
+                    for (int p = 0; p < B; p++)
+                        TMG_CUDA(cudaMemcpyAsync(Wd.p + p * nm, c->recycle[grp[p].k].p, nm * sizeof(zd),
+                                                 cudaMemcpyDeviceToDevice, st));
+                    md = DEFL_M;
+                }
+            }
+            try {
+                if (mixed)
+                    run_batch<zd, zf>(c, grp, c->symC, um, vals, M, nev, ncv, shift, 1000, true, num_modes,
+                                      min_frequency, nullptr, false, md ? Wd.p : nullptr, md);
+                else
+                    run_batch<zd, zd>(c, grp, c->symC, um, vals, M, nev, ncv, shift, 1000, false, num_modes,
+                                      min_frequency);
+            } catch (const numeric_error& e) {
+                for (auto& pr : grp) pr.R->status = TMG_ERR_NUMERIC;
+                c->err = e.what();
+            }
+            if (mixed) {
+                std::vector<Problem> again = mixed_failures(c, grp);
+                if (!again.empty()) {
+                    DVec<zd> v2, m2;
+                    v2.alloc((size_t)again.size() * nU);
+                    m2.alloc((size_t)again.size() * nMU);
+                    for (size_t q = 0; q < again.size(); q++) {
+                        size_t src = 0;
+                        while (grp[src].R != again[q].R) src++;
+                        if (nU) lz_copy<zd>(st, nU, vals + src * nU, v2.p + q * nU);
+                        if (nMU) lz_copy<zd>(st, nMU, M.val + src * nMU, m2.p + q * nMU);
+                    }
+                    DevCsr<zd> M2 = M;
+                    M2.val = m2.p;
+                    try {
+                        run_batch<zd, zd>(c, again, c->symC, um, v2.p, M2, nev, ncv, shift, 1000, false, num_modes,
+                                          min_frequency);
+                    } catch (const numeric_error& e) {
+                        for (auto& pr : again) pr.R->status = TMG_ERR_NUMERIC;
+                        c->err = e.what();
+                    }
+                }
+            }
+        }
+        g0 = group.back() + 1;
+    }
     TMG_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -2213,6 +2567,9 @@ int tmg_set_option(tmg_context* c, int option, double value) {
             c->deflate = value != 0.0;
             if (!c->deflate) c->recycle.clear();
             return TMG_OK;
+        case TMG_OPT_TENSOR_CORES:
+            c->tensor_cores = value != 0.0;
+            return TMG_OK;
         default:
             return set_err(c, TMG_ERR_ARG, "unknown option " + std::to_string(option));
     }
@@ -2223,6 +2580,7 @@ int tmg_get_option(tmg_context* c, int option, double* value) {
     switch (option) {
         case TMG_OPT_SHIFT: *value = c->shift; return TMG_OK;
         case TMG_OPT_DEFLATE: *value = c->deflate ? 1.0 : 0.0; return TMG_OK;
+        case TMG_OPT_TENSOR_CORES: *value = c->tensor_cores ? 1.0 : 0.0; return TMG_OK;
         default: return set_err(c, TMG_ERR_ARG, "unknown option " + std::to_string(option));
     }
 }
@@ -2474,6 +2832,52 @@ int tmg_solve_at_rpm(tmg_context* c, double rpm, int num_modes, const int32_t* h
     });
 }
 
+int tmg_solve_sweep(tmg_context* c, const double* rpms, int nrpm, int num_modes, const int32_t* harmonics, int nh,
+                    int coriolis, double min_frequency, int precision, int32_t* num_results) {
+    if (!c || !num_results || (nrpm > 0 && !rpms) || nrpm < 0) return TMG_ERR_ARG;
+    if (!c->sec) return set_err(c, TMG_ERR_STATE, "no sector uploaded");
+    if (num_modes <= 0) return set_err(c, TMG_ERR_ARG, "num_modes must be positive");
+    return guarded(c, [&]() {
+        for (double& p : c->phase_ms) p = 0.0;
+        const int64_t l0 = g_kernel_launches;
+        cudaEvent_t ev0, ev1;
+        TMG_CUDA(cudaEventCreate(&ev0));
+        TMG_CUDA(cudaEventCreate(&ev1));
+        TMG_CUDA(cudaEventRecord(ev0, c->st));
+        Sector& S = *c->sec;
+        const int max_k = S.ns / 2;
+        std::vector<int> hs;
+        if (!harmonics || nh == 0) for (int k = 0; k <= max_k; k++) hs.push_back(k);
+        else for (int q = 0; q < nh; q++) if (harmonics[q] >= 0 && harmonics[q] <= max_k) hs.push_back(harmonics[q]);
+        std::sort(hs.begin(), hs.end());
+        hs.erase(std::unique(hs.begin(), hs.end()), hs.end());
+        std::vector<double> rs(rpms, rpms + nrpm);
+        c->results.clear();
+        c->err.clear();
+        if (coriolis) {   // the QEP keeps the per-speed path
+            for (double rpm : rs) {
+                prepare(c, rpm, true);
+                std::vector<ResultHost> r;
+                solve_set(c, hs, num_modes, min_frequency, precision, r);
+                std::sort(r.begin(), r.end(), [](const ResultHost& a, const ResultHost& b) { return a.k < b.k; });
+                c->results.insert(c->results.end(), r.begin(), r.end());
+            }
+        } else {
+            solve_sweep(c, rs, hs, num_modes, min_frequency, precision, c->results);
+        }
+        *num_results = (int32_t)c->results.size();
+        c->launches = g_kernel_launches - l0;
+        TMG_CUDA(cudaEventRecord(ev1, c->st));
+        TMG_CUDA(cudaEventSynchronize(ev1));
+        float ms = 0.f;
+        TMG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        c->phase_ms[4] = ms;
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+        return TMG_OK;
+    });
+}
+
 int tmg_result_info(tmg_context* c, int idx, tmg_result_meta* info) {
     if (!c || !info || idx < 0 || idx >= (int)c->results.size()) return TMG_ERR_ARG;
     const ResultHost& R = c->results[idx];
@@ -2485,6 +2889,15 @@ int tmg_result_info(tmg_context* c, int idx, tmg_result_meta* info) {
     info->rpm = R.rpm;
     info->max_residual = R.max_residual;
     info->refine_residual = R.refine_residual;
+    return TMG_OK;
+}
+
+int tmg_result_modal_mass(tmg_context* c, int idx, double* mass) {
+    if (!c || !mass) return TMG_ERR_ARG;
+    if (idx < 0 || idx >= (int)c->results.size()) return set_err(c, TMG_ERR_ARG, "result index out of range");
+    const ResultHost& R = c->results[idx];
+    if (R.modal_mass.size() != R.freqs.size()) return set_err(c, TMG_ERR_STATE, "no modal masses for this result");
+    std::copy(R.modal_mass.begin(), R.modal_mass.end(), mass);
     return TMG_OK;
 }
 
@@ -2516,7 +2929,7 @@ int tmg_profile_solve(tmg_context* c, double* out) {
 
 int tmg_last_timing(tmg_context* c, double* phase_ms, int nphase, int64_t* kernel_launches) {
     if (!c) return TMG_ERR_ARG;
-    for (int q = 0; q < nphase && q < 8; q++) phase_ms[q] = c->phase_ms[q];
+    for (int q = 0; q < nphase && q < 9; q++) phase_ms[q] = c->phase_ms[q];
     if (kernel_launches) *kernel_launches = c->launches;
     return TMG_OK;
 }

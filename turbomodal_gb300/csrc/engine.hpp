@@ -140,6 +140,7 @@ struct Sector {
     DVec<double> dX;
     DVec<int32_t> dconn, pair_col, pair_pos, clist, nlist;
     DVec<int64_t> dnadj_p, cptr, dcand_p, nptr;
+    DVec<int32_t> dcand_i;             // candidate-pattern row indices (uploaded for the modal masses)
     DVec<double> Kel, Mel, Fe;
     // transformation T(0) (complex with zero imaginary part) and its real filtered copy
     Pattern T0, T0t, Tr, Trt;

@@ -13,10 +13,13 @@
 // simplicial up-looking LDL^T (src/hermitian_lanczos.cpp:12-56); the supernodal form has the
 // same L and D in exact arithmetic.
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 
 #include "mf.cuh"
+#include "mf_tc.cuh"
 
 namespace tmg {
 
@@ -828,6 +831,7 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
     // factorisation schedule
     std::vector<int32_t> it;
     steps.clear();
+    tc_rows = 0;
     for (int l = 0; l < nlev; l++) {
         int maxw = 0, maxch = 0;
         for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
@@ -893,24 +897,80 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
                     }
             }
             st.trail_off = (int64_t)it.size();
-            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-                const int s = S.level_sn[q];
-                const int w = S.sn_first[s + 1] - S.sn_first[s];
-                if (w <= kb * MF_NB) continue;
-                const int64_t m = S.sn_row_ptr[s + 1] - S.sn_row_ptr[s];
-                const int64_t kend = std::min<int64_t>((int64_t)(kb + 1) * MF_NB, w);
-                const bool sb_end = kend == w || kend % MF_SB == 0;   // this pivot block closes a super-block
-                if (!sb_end) continue;
-                for (int64_t j0 = kend; j0 < m; j0 += MF_TILE)
-                    for (int64_t i0 = j0; i0 < m; i0 += MF_TILE) {
-                        it.push_back(s); it.push_back((int32_t)i0); it.push_back((int32_t)j0);
-                        st.trail_cnt++;
+            std::vector<int> tcf;   // fronts of this step that qualify for the tensor-core update
+            for (int pass = 0; pass < 2; pass++)
+                for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+                    const int s = S.level_sn[q];
+                    const int w = S.sn_first[s + 1] - S.sn_first[s];
+                    if (w <= kb * MF_NB) continue;
+                    const int64_t m = S.sn_row_ptr[s + 1] - S.sn_row_ptr[s];
+                    const int64_t kend = std::min<int64_t>((int64_t)(kb + 1) * MF_NB, w);
+                    const bool sb_end = kend == w || kend % MF_SB == 0;   // this pivot block closes a super-block
+                    if (!sb_end) continue;
+                    const bool tc = m - kend >= MF_TC_MIN_ROWS;
+                    if (tc != (pass == 1)) continue;
+                    if (tc) tcf.push_back(s);
+                    for (int64_t j0 = kend; j0 < m; j0 += MF_TILE)
+                        for (int64_t i0 = j0; i0 < m; i0 += MF_TILE) {
+                            it.push_back(s); it.push_back((int32_t)i0); it.push_back((int32_t)j0);
+                            st.trail_cnt++;
+                        }
+                    if (pass == 0) st.trail_simt = st.trail_cnt;
+                }
+            // tensor-core groups: fronts packed in order while their staged rows fit the group
+            for (size_t f = 0; f < tcf.size();) {
+                Step::TcGroup g;
+                std::vector<std::pair<int, int64_t>> mem;   // (front, staging offset)
+                int64_t rows = 0;
+                while (f < tcf.size()) {
+                    const int s = tcf[f];
+                    const int w = S.sn_first[s + 1] - S.sn_first[s];
+                    const int64_t m = S.sn_row_ptr[s + 1] - S.sn_row_ptr[s];
+                    const int64_t kend = std::min<int64_t>((int64_t)(kb + 1) * MF_NB, w);
+                    if (!mem.empty() && rows + (m - kend) > MF_TC_GROUP_ROWS) break;
+                    mem.push_back({s, rows});
+                    rows += m - kend;
+                    f++;
+                }
+                tc_rows = std::max(tc_rows, rows);
+                g.stage_off = (int64_t)it.size();
+                for (auto [s, off] : mem) {
+                    const int w = S.sn_first[s + 1] - S.sn_first[s];
+                    const int64_t m = S.sn_row_ptr[s + 1] - S.sn_row_ptr[s];
+                    const int64_t kend = std::min<int64_t>((int64_t)(kb + 1) * MF_NB, w);
+                    for (int64_t r0 = kend; r0 < m; r0 += 16) {
+                        it.push_back(s); it.push_back((int32_t)r0); it.push_back((int32_t)(off + r0 - kend));
+                        g.stage_cnt++;
                     }
+                }
+                g.upd_off = (int64_t)it.size();
+                for (auto [s, off] : mem) {
+                    const int w = S.sn_first[s + 1] - S.sn_first[s];
+                    const int64_t m = S.sn_row_ptr[s + 1] - S.sn_row_ptr[s];
+                    const int64_t kend = std::min<int64_t>((int64_t)(kb + 1) * MF_NB, w);
+                    for (int64_t j0 = kend; j0 < m; j0 += MF_TILE)
+                        for (int64_t i0 = j0; i0 < m; i0 += MF_TILE) {
+                            it.push_back(s); it.push_back((int32_t)i0); it.push_back((int32_t)j0);
+                            it.push_back((int32_t)(off + i0 - kend)); it.push_back((int32_t)(off + j0 - kend));
+                            g.upd_cnt++;
+                        }
+                }
+                st.tc.push_back(g);
             }
             steps.push_back(st);
         }
     }
     put(items, it);
+    if (std::getenv("TMG_VERBOSE")) {
+        int64_t simt = 0, tct = 0, groups = 0;
+        for (const auto& st : steps) {
+            simt += st.trail_simt;
+            for (const auto& g : st.tc) { tct += g.upd_cnt; groups++; }
+        }
+        std::fprintf(stderr, "[tmg] factor plan n=%d: %lld trail tiles on the SIMT pipe, %lld on the tensor cores "
+                     "(%lld groups, %lld staging rows)\n", n, (long long)simt, (long long)tct, (long long)groups,
+                     (long long)tc_rows);
+    }
     // triangular-solve schedule (64-wide diagonal blocks)
     std::vector<int32_t> si;
     plan64 = build_solve_plan(S, 64, SV_RR, si);
@@ -940,7 +1000,9 @@ template <typename T>
 void mf_invert_diag(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt);
 
 template <typename T>
-void mf_factor(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, int* status) {
+void mf_factor(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, int* status, bool tensor_cores) {
+    const bool tc = tensor_cores && std::is_same<T, zf>::value && S.tc_rows > 0;
+    TcWork wk;
     const size_t upd_smem = 2 * MF_NB * MF_TILE * sizeof(T);
     static std::once_flag attr_once;
     std::call_once(attr_once, [&]() {
@@ -972,11 +1034,19 @@ void mf_factor(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, int* s
         if (stp.upd_cnt)
             TMG_LAUNCH(k_update<T>, dim3(stp.upd_cnt, B), 256, upd_smem, st, S.items + stp.upd_off, stp.kb * MF_NB, MF_NB,
                        0, sn, bt.L, bt.U, bt.lstride, bt.ustride);
-        if (stp.trail_cnt)
-            TMG_LAUNCH(k_update<T>, dim3(stp.trail_cnt, B), 256, upd_smem, st, S.items + stp.trail_off,
+        const int32_t ntrail = tc ? stp.trail_simt : stp.trail_cnt;
+        if (ntrail)
+            TMG_LAUNCH(k_update<T>, dim3(ntrail, B), 256, upd_smem, st, S.items + stp.trail_off,
                        (stp.kb * MF_NB / MF_SB) * MF_SB, MF_SB, 1, sn, bt.L, bt.U, bt.lstride, bt.ustride);
+        if constexpr (std::is_same<T, zf>::value) {
+            if (tc) mf_trail_tc(st, S, bt, stp, wk);
+        }
     }
     TMG_CHECK_LAUNCH();
+    if (tc) {
+        const int e = wk.read_error(st);
+        if (e) throw cuda_error("tensor-core Schur update: a bounded wait expired (code " + std::to_string(e) + ")");
+    }
     mf_invert_diag<T>(st, S, bt);
 }
 
@@ -1074,7 +1144,7 @@ void mf_count_nonpos(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, 
 }
 
 #define TMG_INST(T)                                                                          \
-    template void mf_factor<T>(cudaStream_t, const DevSymbolic&, const Batch<T>&, int*);     \
+    template void mf_factor<T>(cudaStream_t, const DevSymbolic&, const Batch<T>&, int*, bool); \
     template void mf_scatter<T>(cudaStream_t, const DevSymbolic&, const Batch<T>&, const T*); \
     template void mf_solve<T>(cudaStream_t, const DevSymbolic&, const Batch<T>&, T*, T*, const int*); \
     template void mf_count_nonpos<T>(cudaStream_t, const DevSymbolic&, const Batch<T>&, int*);

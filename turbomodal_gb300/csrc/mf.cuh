@@ -20,6 +20,8 @@ constexpr int MF_TILE = 64;    // Schur-update tile
 constexpr int MF_SB = 256;     // super-block: pivot blocks update inside it, one trailing update after it
 constexpr int SV_RR = 64;      // rows per CTA of the forward rectangle products
 constexpr int SV_CH = 2048;    // gathered solution entries staged per pass (backward rectangles)
+constexpr int MF_TC_MIN_ROWS = 192;    // rows right of a super-block for the tensor-core trail update
+constexpr int64_t MF_TC_GROUP_ROWS = 8192;   // staging rows per tc group (more only for one larger front)
 
 // Width of the diagonal blocks that the triangular solves treat as dense units (the factor
 // stores each block's explicit unit-lower inverse).
@@ -67,8 +69,18 @@ struct DevSymbolic {
         std::vector<int32_t> ext_cnt, ext_max;
         int64_t diag_off = 0, panel_off = 0, upd_off = 0, trail_off = 0;
         int32_t diag_cnt = 0, panel_cnt = 0, upd_cnt = 0, trail_cnt = 0;
+        // The trail items of fronts that qualify for the tensor-core update (at least
+        // MF_TC_MIN_ROWS rows right of the super-block) come last: trail_simt of them belong to
+        // the other fronts.  The complex FP32 factor runs those last items as tc groups instead.
+        int32_t trail_simt = 0;
+        struct TcGroup {
+            int64_t stage_off = 0, upd_off = 0;   // items: (s, r0, dst) and (s, i0, j0, abase, bbase)
+            int32_t stage_cnt = 0, upd_cnt = 0;
+        };
+        std::vector<TcGroup> tc;
     };
     std::vector<Step> steps;
+    int64_t tc_rows = 0;       // staging rows (complex) per problem of the largest tc group
     using SolveLevel = tmg::SolveLevel;
     using SolvePlan = tmg::SolvePlan;
     SolvePlan plan64;          // the solve schedule for 64-wide diagonal blocks
@@ -101,8 +113,10 @@ void mf_scatter(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, const
 // On return every diagonal block of width sv_nb<T>() of every panel holds, below its
 // diagonal, the strict lower part of the block's unit-lower inverse (the diagonal keeps D),
 // which is the form mf_solve reads.
+// tensor_cores: the complex FP32 factor runs its large trailing updates on tcgen05 (mf_tc.cu);
+// other types ignore it.
 template <typename T>
-void mf_factor(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, int* status);
+void mf_factor(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, int* status, bool tensor_cores = true);
 
 // x (B x n, factor numbering, factor precision) <- L^-H D^-1 L^-1 x ; tbuf: B x t_entries.
 // skip (device, B flags, may be null): problems with a nonzero flag are left untouched.

@@ -39,6 +39,8 @@ class ModalResult:
         self.iterations = 0
         self.max_residual = 0.0
         self.refine_residual = 0.0
+        # full-annulus modal mass per mode (kg), computed on the device with the result
+        self.modal_mass_kg = np.zeros(len(self.frequencies))
 
     def wave_propagation_velocity(self, radius: float) -> np.ndarray:
         k = self.harmonic_index
@@ -115,8 +117,9 @@ class CyclicSymmetrySolver:
 
     def set_option(self, name: str, value: float) -> None:
         """tmg_set_option: "shift" (sigma of the standard path, default 1.0 as the reference's
-        src/cyclic_solver.cpp:1017) or "deflate" (1 = deflate the mixed refinement CG with the
-        previous speed's eigenvectors)."""
+        src/cyclic_solver.cpp:1017), "deflate" (1 = deflate the mixed refinement CG with the
+        previous speed's eigenvectors) or "tensor_cores" (1 = tcgen05 trailing updates in the
+        complex FP32 factorisation, the default)."""
         self.ctx.check(self.ctx.L.tmg_set_option(self.ctx.h, _lib.OPT[name], float(value)), "tmg_set_option")
 
     def get_option(self, name: str) -> float:
@@ -151,9 +154,16 @@ class CyclicSymmetrySolver:
                                 _lib.ptr(hi, C.c_int32) if hi.size else None, int(hi.size),
                                 int(include_coriolis), float(min_frequency), prec, C.byref(nres))
         self.ctx.check(rc, "tmg_solve_at_rpm")
+        return self._collect(nres.value, progress_cb, t_call)
+
+    def _collect(self, nres: int, progress_cb=None, t_call: float = 0.0, index: list | None = None) -> list[ModalResult]:
+        """Copy the context's results to host ModalResults; failed harmonics are reported on
+        stderr and omitted, as the reference does (src/cyclic_solver.cpp:1217-1223).  index, if
+        given, receives the context's result index of every returned result."""
+        L, h = self.ctx.L, self.ctx.h
         out = []
         ndof = self.mesh.num_dof()
-        for idx in range(nres.value):
+        for idx in range(nres):
             meta = _lib.ResultMeta()
             L.tmg_result_info(h, idx, C.byref(meta))
             if meta.status != _lib.TMG_OK:
@@ -171,11 +181,17 @@ class CyclicSymmetrySolver:
             r.iterations = meta.iterations
             r.max_residual = meta.max_residual
             r.refine_residual = meta.refine_residual
+            mm = np.zeros(m)
+            if m:
+                self.ctx.check(L.tmg_result_modal_mass(h, idx, _lib.ptr(mm, C.c_double)), "tmg_result_modal_mass")
+            r.modal_mass_kg = mm
+            if index is not None:
+                index.append(idx)
             if not r.converged:
                 sys.stderr.write(f"[CyclicSolver] WARNING: k={r.harmonic_index} eigenvalue solve did not fully converge\n")
             out.append(r)
             if progress_cb is not None:
-                progress_cb(SolverProgress(completed=len(out), total=nres.value, harmonic_k=r.harmonic_index,
+                progress_cb(SolverProgress(completed=len(out), total=nres, harmonic_k=r.harmonic_index,
                                            converged=r.converged, iterations=r.iterations,
                                            num_converged=m if r.converged else 0, num_modes=m,
                                            max_residual=r.max_residual,
@@ -205,17 +221,37 @@ class CyclicSymmetrySolver:
         return out
 
     def solve_rpm_sweep(self, rpm_values, num_modes_per_harmonic: int, harmonic_indices=(), max_threads: int = 0,
-                        include_coriolis: bool = False, min_frequency: float = 0.0, precision: str | None = None):
-        return [self.solve_at_rpm(r, num_modes_per_harmonic, harmonic_indices, max_threads, include_coriolis,
-                                  min_frequency, precision=precision) for r in rpm_values]
+                        include_coriolis: bool = False, min_frequency: float = 0.0,
+                        precision: str | None = None) -> list[list[ModalResult]]:
+        """One result list per speed, in order (src/cyclic_solver.cpp:1359-1373).  On the standard
+        path the harmonics of several speeds are factorised and iterated as one batch
+        (tmg_solve_sweep); each speed's results equal solve_at_rpm's at that speed."""
+        rpms = np.ascontiguousarray(np.asarray(list(rpm_values), dtype=np.float64))
+        prec = _lib.PREC[precision or self.precision]
+        hi = np.asarray(list(harmonic_indices or []), dtype=np.int32)
+        nres = C.c_int32()
+        L, h = self.ctx.L, self.ctx.h
+        if rpms.size == 0:
+            return []
+        rc = L.tmg_solve_sweep(h, _lib.ptr(rpms, C.c_double), int(rpms.size), int(num_modes_per_harmonic),
+                               _lib.ptr(hi, C.c_int32) if hi.size else None, int(hi.size), int(include_coriolis),
+                               float(min_frequency), prec, C.byref(nres))
+        self.ctx.check(rc, "tmg_solve_sweep")
+        idx = []
+        flat = self._collect(nres.value, index=idx)
+        per = nres.value // rpms.size   # the context keeps every speed's harmonics, failed ones included
+        out = [[] for _ in range(rpms.size)]
+        for i, r in zip(idx, flat):
+            out[i // per].append(r)
+        return out
 
     def last_timing(self):
-        ph = np.zeros(8)
+        ph = np.zeros(9)
         nl = C.c_int64()
-        self.ctx.L.tmg_last_timing(self.ctx.h, _lib.ptr(ph, C.c_double), 8, C.byref(nl))
+        self.ctx.L.tmg_last_timing(self.ctx.h, _lib.ptr(ph, C.c_double), 9, C.byref(nl))
         return dict(prepare_ms=float(ph[0]), factor_ms=float(ph[1]), lanczos_ms=float(ph[2]), post_ms=float(ph[3]),
                     device_ms=float(ph[4]), solves=int(ph[5]), applies=int(ph[6]), max_refine_iters=int(ph[7]),
-                    kernel_launches=nl.value)
+                    retried_fp64=int(ph[8]), kernel_launches=nl.value)
 
     def set_profiling(self, on: bool) -> None:
         self.ctx.check(self.ctx.L.tmg_set_profiling(self.ctx.h, int(on)), "tmg_set_profiling")
@@ -386,9 +422,7 @@ def solve(mesh: Mesh, material: Material, rpm: float = 0.0, num_modes: int = 20,
     if verbose >= PROGRESS:
         print(f"  Solved {len(res)} harmonic indices in {time.perf_counter() - t0:.1f}s")
     res = _validate(res)
-    M = s.assemble("M")
-    masses = _modal_mass_from_M(M, res, mesh.num_sectors)
-    out = [EnrichedModalResult(_result=r, modal_mass_kg=m) for r, m in zip(res, masses)]
+    out = [EnrichedModalResult(_result=r, modal_mass_kg=r.modal_mass_kg) for r in res]
     if verbose >= DETAILED:
         for r in out:
             freqs = ", ".join(f"{f:.1f}" for f in r.frequencies[:4])
@@ -419,7 +453,8 @@ def rpm_sweep(mesh: Mesh, material: Material, rpm_values, num_modes: int = 20, f
               boundary_conditions=None, memory_reserve_fraction: float = 0.2, *, precision: str = "fp64"):
     """tm.rpm_sweep (python/turbomodal/solver.py:499-628) on the GPU path, with the reference's
     parameters in its order: one solver (sector assembly and symbolic analysis reused across
-    speeds), one solve per speed, modal masses from one mass assembly."""
+    speeds), the speeds solved as batches of several speeds on the device (solve_rpm_sweep), and
+    modal masses computed on the device with each result."""
     _unsupported(boundary_conditions)
     if temperature is not None:
         material = material.at_temperature(temperature)
@@ -432,15 +467,15 @@ def rpm_sweep(mesh: Mesh, material: Material, rpm_values, num_modes: int = 20, f
         print(f"  Solving {nd}, {num_modes} modes/ND")
         print()
     s = CyclicSymmetrySolver(mesh, material, fluid, hub_constraint == "fixed", precision=precision)
-    M = s.assemble("M")
     out = []
     t_start = time.perf_counter()
+    # all speeds in one batched sweep call; the per-speed report follows it
+    t0 = time.perf_counter()
+    sweep = s.solve_rpm_sweep([float(r) for r in rpms], num_modes, hi, max_threads, include_coriolis, min_frequency,
+                              precision=precision)
     for i, rpm in enumerate(rpms):
-        t0 = time.perf_counter()
-        res = _validate(s.solve_at_rpm(float(rpm), num_modes, hi, max_threads, include_coriolis, min_frequency,
-                                       memory_reserve_fraction=memory_reserve_fraction, precision=precision))
-        masses = _modal_mass_from_M(M, res, mesh.num_sectors)
-        out.append([EnrichedModalResult(_result=r, modal_mass_kg=m) for r, m in zip(res, masses)])
+        res = _validate(sweep[i])
+        out.append([EnrichedModalResult(_result=r, modal_mass_kg=r.modal_mass_kg) for r in res])
         if verbose >= DETAILED:
             print(f"  [{i + 1}/{len(rpms)}] {rpm:.0f} RPM  ({len(res)} harmonics, {time.perf_counter() - t0:.1f}s)")
             for r in res:
