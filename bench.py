@@ -6,15 +6,17 @@ Workload: the batched rpm sweep on the rotating bladed-disk sector (config-1 mes
 linspace(0, 15000) rpm x harmonic indices 0..18, num_modes = 10, rotating effects (spin
 softening + stress stiffening), standard Hermitian shift-invert path.  A step is one speed
 of the sweep (all 19 harmonic problems: assembly, prestress, projections, factorisations,
-Lanczos, expansion).  Speeds are taken in order, rank r of N takes speeds r, r+N, ...
-(weak scaling: per-GPU work fixed).
+Lanczos, expansion).  Speeds are taken in order, --sweep-group of them per solve_rpm_sweep
+call (their harmonics are factorised and iterated as one batch; each speed is charged an equal
+share of the call).  Rank r of N takes speeds r, r+N, ... (weak scaling: per-GPU work fixed).
 
-value   eigenpairs/s of the mixed path (FP32 LDL^H + FP64 refinement), counting returned
-        eigenpairs that converged and lie within 1e-6 relative frequency error of the plain
-        FP64 GPU path on the same problem (verified after the timed region), over the device
-        time (CUDA events on the library's stream) of the timed steps.
-e2e     the same count over the wall-clock of the public API call (solve_at_rpm through the
-        C ABI, speed and harmonic list in, frequencies + mode shapes copied back to host).
+value   eigenpairs/s of the mixed path (FP32 LDL^H + FP64 refinement), counting the eigenpairs
+        that converged and lie within 1e-6 relative frequency error of the plain FP64 GPU path,
+        on --verify-steps timed speeds spread over the sweep (re-solved in FP64 after the timed
+        region), over those speeds' device time (CUDA events on the library's stream).
+e2e     the same count over the wall-clock of the public API call (solve_rpm_sweep through the
+        C ABI: speeds and harmonic list in, frequencies, mode shapes and modal masses copied back
+        to host).
 Inputs are larger than L2 (fronts of tens of GB), so no L2 flush is needed.
 """
 
@@ -53,6 +55,8 @@ def parse():
     ap.add_argument("--wall-budget", type=float, default=1200.0,
                     help="seconds after start beyond which the optional legs (serving sample, CPU baseline) "
                          "are skipped")
+    ap.add_argument("--sweep-group", type=int, default=4,
+                    help="speeds per solve_rpm_sweep call (their harmonics are factorised and iterated as one batch)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the served request-stream sample")
     ap.add_argument("--serve-requests", type=int, default=12)
@@ -391,11 +395,13 @@ def main():
     solver = CyclicSymmetrySolver(mesh, TITANIUM, device=local, precision="mixed")
     order = list(my_rpms) * (1 + (args.warmup + args.steps) // max(1, len(my_rpms)))
     warm, timed = order[: args.warmup], order[args.warmup: args.warmup + args.steps]
-    log(f"config-1 mesh {mesh.num_nodes()} nodes; {len(warm)} warm-up and {len(timed)} timed speeds")
-    for i, rpm in enumerate(warm):
+    grp = max(1, args.sweep_group)
+    log(f"config-1 mesh {mesh.num_nodes()} nodes; {len(warm)} warm-up and {len(timed)} timed speeds, "
+        f"{grp} speeds per sweep call")
+    for c0 in range(0, len(warm), grp):
         t0 = time.perf_counter()
-        solver.solve_at_rpm(rpm, args.num_modes, hi, precision="mixed")
-        log(f"warm-up {i + 1}/{len(warm)} at {rpm:.0f} rpm: {time.perf_counter() - t0:.1f} s")
+        solver.solve_rpm_sweep(warm[c0:c0 + grp], args.num_modes, hi, precision="mixed")
+        log(f"warm-up speeds {c0 + 1}-{min(len(warm), c0 + grp)}/{len(warm)}: {time.perf_counter() - t0:.1f} s")
     torch.cuda.synchronize()
     barrier(pg)
     clocks = ClockSampler(local)
@@ -403,17 +409,22 @@ def main():
     dev_ms, wall_s, results, launches, d2h = [], [], [], 0, []
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_push("timed")
-    for i, rpm in enumerate(timed):
+    for c0 in range(0, len(timed), grp):
+        chunk = timed[c0:c0 + grp]
         t0 = time.perf_counter()
-        res = solver.solve_at_rpm(rpm, args.num_modes, hi, precision="mixed")
-        wall_s.append(time.perf_counter() - t0)
+        sweep = solver.solve_rpm_sweep(chunk, args.num_modes, hi, precision="mixed")
+        w = time.perf_counter() - t0
         tm = solver.last_timing()
-        dev_ms.append(tm["device_ms"])
         launches += int(tm["kernel_launches"])
-        d2h.append(sum(r.frequencies.nbytes + r.mode_shapes.nbytes + r.whirl_direction.nbytes for r in res))
-        results.append(res)
-        log(f"timed {i + 1}/{len(timed)} at {rpm:.0f} rpm: {tm['device_ms'] / 1e3:.2f} s device, "
-            f"{wall_s[-1]:.2f} s wall, {sum(len(r.frequencies) for r in res)} eigenpairs")
+        for res in sweep:   # each speed of the call gets an equal share of its time
+            wall_s.append(w / len(chunk))
+            dev_ms.append(tm["device_ms"] / len(chunk))
+            d2h.append(sum(r.frequencies.nbytes + r.mode_shapes.nbytes + r.whirl_direction.nbytes +
+                           r.modal_mass_kg.nbytes for r in res))
+            results.append(res)
+        log(f"timed speeds {c0 + 1}-{c0 + len(chunk)}/{len(timed)} ({', '.join(f'{r:.0f}' for r in chunk)} rpm): "
+            f"{tm['device_ms'] / 1e3:.2f} s device, {w:.2f} s wall, "
+            f"{sum(len(r.frequencies) for res in sweep for r in res)} eigenpairs")
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     clk = clocks.stop()
@@ -505,7 +516,7 @@ def main():
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "path": "mixed FP32 supernodal LDL^H + FP64 refinement, 1 GB300",
                        "harmonics": args.harmonics, "num_modes": args.num_modes,
-                       "speeds": [float(r) for r in timed],
+                       "speeds": [float(r) for r in timed], "speeds_per_call": grp,
                        "verified_speeds": [float(timed[i]) for i in vidx],
                        "parallelism": f"replicas x{ws} (speeds sharded)",
                        "l2": "inputs larger than L2 (no flush needed)"},
@@ -516,7 +527,7 @@ def main():
             "fp64_gpu": {"value": fp64_pairs / (fp64_ms / 1e3) if fp64_ms > 0 else None, "unit": UNIT,
                          "ms_per_step": fp64_ms / max(len(vidx), 1), "speeds": len(vidx) if not args.no_verify else 0},
             "e2e": {"value": tot_ok / t_wall if t_wall > 0 else 0.0, "unit": UNIT,
-                    "h2d_bytes_per_step": 8 + 4 * max(len(hi), 19),
+                    "h2d_bytes_per_step": 8 + 4 * max(len(hi), 19) // grp,
                     "d2h_bytes_per_step": int(np.mean(d2h)) if d2h else 0},
             "gpu_launches": launches,
             "roofline": {"kernel": f"shift-invert triangular solve of the {len(mesh_k)} complex harmonics "

@@ -108,10 +108,15 @@ int tmg_set_memory_budget(tmg_context* ctx, size_t mem_budget_bytes);
  *   refinement tolerance.
  * TMG_OPT_TENSOR_CORES: 1 = the complex FP32 factorisation of the mixed path runs its large
  *   trailing Schur updates on the tensor cores (3xTF32, tcgen05); 0 = on the FP32 SIMT pipe
- *   (default 1).  Method change only, as above. */
+ *   (default 1).  Method change only, as above.
+ * TMG_OPT_AUTOTUNE: 1 = the first solve on a new complex operator pattern times candidate
+ *   supernode shapes (relaxed amalgamation, front width cap, tensor-core row threshold) on its
+ *   own operator values and keeps the fastest, cached per pattern for the process (default 0).
+ *   tmg_tuning_report lists the trials. */
 #define TMG_OPT_SHIFT 0
 #define TMG_OPT_DEFLATE 1
 #define TMG_OPT_TENSOR_CORES 2
+#define TMG_OPT_AUTOTUNE 3
 int tmg_set_option(tmg_context* ctx, int option, double value);
 int tmg_get_option(tmg_context* ctx, int option, double* value);
 int tmg_destroy(tmg_context* ctx);
@@ -177,6 +182,13 @@ int tmg_solve_sweep(tmg_context* ctx, const double* rpms, int nrpm, int num_mode
  * complex interleaved, column-major; NULL skips the copy. */
 int tmg_result_info(tmg_context* ctx, int idx, tmg_result_meta* info);
 int tmg_result_copy(tmg_context* ctx, int idx, double* freqs, double* shapes, int32_t* whirl);
+
+/* Trials of the last supernode-shape tuning (TMG_OPT_AUTOTUNE); no counterpart in the reference,
+ * whose simplicial factorisation has no tile shapes.  *rows = number of trials; out (may be NULL)
+ * receives min(max_rows, *rows) rows of 9 doubles: relax, front width cap, tensor-core row
+ * threshold, factorisation ms, ms per batched triangular solve, score ms, L entries per problem,
+ * supernodes, chosen (1/0). */
+int tmg_tuning_report(tmg_context* ctx, double* out, int max_rows, int* rows);
 
 /* Modal mass of every mode of a result, N * Re(phi^H M_sector phi) in kg over the full annulus,
  * computed on the device from the expanded shapes and the sector mass matrix.  Replaces the

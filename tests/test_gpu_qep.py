@@ -118,11 +118,17 @@ def test_lanczos_qep_reference_structure(small):
         assert np.all(np.isfinite(r.mode_shapes))
 
 
-def test_qep_subspace_limit_is_reported(small):
-    """num_modes > 10 needs a Lanczos subspace above 256 vectors: the harmonic is reported as
-    failed and omitted, the call itself succeeds."""
+def test_qep_twenty_modes_and_subspace_limit(small):
+    """num_modes = 20 (nev = 120, ncv = 481 Lanczos vectors, the reference's sizes at
+    src/modal_solver.cpp:200-312) runs with the reference's structure; num_modes = 22 needs more
+    than 512 vectors: the harmonic is reported as failed and omitted, the call itself succeeds."""
     from turbomodal_gb300.meshgen import TITANIUM
     from turbomodal_gb300.solver import CyclicSymmetrySolver
 
     s = CyclicSymmetrySolver(small, TITANIUM)
-    assert s.solve_at_rpm(RPM, 11, harmonic_indices=[1], include_coriolis=True) == []
+    res = s.solve_at_rpm(RPM, 20, harmonic_indices=[1], include_coriolis=True)
+    assert len(res) == 1 and res[0].harmonic_index == 1
+    r = res[0]
+    assert 0 < len(r.frequencies) <= 20 and set(np.unique(r.whirl_direction).tolist()) <= {-1, 1}
+    assert np.all(np.isfinite(r.frequencies)) and np.all(r.frequencies > 0)
+    assert s.solve_at_rpm(RPM, 22, harmonic_indices=[1], include_coriolis=True) == []

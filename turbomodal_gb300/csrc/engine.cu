@@ -403,6 +403,21 @@ void build_union(UnionMaps& um, const std::vector<const Pattern*>& parts) {
 // =====================================================================================
 using namespace tmg;
 
+// Supernode shapes the autotuner chooses between: relaxed amalgamation of the fundamental
+// supernodes (explicit zeros within `relax` of the stored entries, fronts at most `maxw`
+// columns wide, 0 = no cap) and the row threshold of the tensor-core trailing update.
+struct TuneCand {
+    double relax = 0.0;
+    int32_t maxw = 0;
+    int32_t tc_min = MF_TC_MIN_ROWS;
+};
+struct TuneRow {
+    TuneCand cand;
+    double factor_ms = 0.0, solve_ms = 0.0, score_ms = 0.0;
+    int64_t stored = 0;           // L entries per problem
+    int32_t supernodes = 0;
+};
+
 struct ResultHost {
     int32_t k = 0;
     double rpm = 0.0;
@@ -469,6 +484,11 @@ struct tmg_context {
     // TMG_DEFLATE when the context is created): the DEFL_M lowest eigenvectors of every complex
     // harmonic from the last solve, valid while the operator pattern keeps `recycle_key`.
     bool deflate = false;
+    bool autotune = false;        // tune the complex operator's supernode shapes on first use
+    std::vector<TuneRow> tune_rows;   // trials of the last tuning (empty: none ran)
+    TuneCand tune_choice;         // shapes of the current complex analysis
+    double solves_per_factor = 0.0;   // FP32 solves per factorisation seen in the last mixed batch
+    std::string tuned_key;        // pattern the current complex analysis was tuned for
     double shift = 1.0;           // sigma of the standard path (cyclic_solver.cpp:1017)
     bool tensor_cores = true;     // tcgen05 trailing updates in the complex FP32 factorisation
     std::string recycle_key;
@@ -756,11 +776,13 @@ void assemble_rot(tmg_context* c, double omega) {
 }
 
 // ---- factorisation + solve helpers ---------------------------------------------------
-void analyze_op(OpSymbolic& os, const UnionMaps& um) {
-    os.S = analyze(um.lower, 0.0, 0);
+void analyze_op(OpSymbolic& os, const UnionMaps& um, const TuneCand* cand = nullptr,
+                const std::vector<int32_t>* amd = nullptr) {
+    os.S = analyze(um.lower, cand ? cand->relax : 0.0, cand ? cand->maxw : 0, amd);
     std::vector<int64_t> dest;
     std::vector<uint8_t> cj;
     scatter_map(os.S, um.lower, dest, cj);
+    os.D.tc_min_rows = cand ? cand->tc_min : MF_TC_MIN_ROWS;
     os.D.upload(os.S, dest, cj);
     os.valid = true;
 }
@@ -1793,6 +1815,7 @@ void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os
         }
     }
     c->phase_ms[5] += (double)op.solves;
+    if (mixed && !qep && std::is_same<Tv, zd>::value) c->solves_per_factor = (double)op.solves;
     c->phase_ms[6] += (double)op.applies;
     c->phase_ms[7] = std::max(c->phase_ms[7], (double)op.max_its);
     if (std::getenv("TMG_VERBOSE"))
@@ -1820,6 +1843,98 @@ void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os
     }
     auto t3 = std::chrono::steady_clock::now();
     c->phase_ms[3] += std::chrono::duration<double, std::milli>(t3 - t2).count();
+}
+
+// ---- supernode-shape autotuner ----------------------------------------------------------
+// For a new complex operator pattern (one per sector design and speed regime), each candidate
+// shape is analysed (the AMD order is computed once and shared), factorised on the first batch
+// of real operator values and its batched triangular solve timed, with CUDA events on the
+// context's stream.  Score = factorisation + S x solve, S the FP32 solves per factorisation of
+// the last mixed batch (256 before any, about what a config-1 batch needs; 45 in FP64).  The
+// winner replaces the context's analysis and is cached per pattern fingerprint for every
+// context of the process.
+std::mutex g_tune_mu;
+std::map<std::string, TuneCand> g_tune_cache;
+
+template <typename Tf>
+TuneRow tune_trial(tmg_context* c, OpSymbolic& os, const UnionMaps& um, const zd* vals_csc, int B, bool mixed) {
+    cudaStream_t st = c->st;
+    const int64_t nl = (int64_t)um.lower2csc.n, nU = um.U.nnz();
+    DVec<zd> lower, acsr;
+    lower.alloc((size_t)B * nl);
+    acsr.alloc((size_t)B * nU);
+    if (nl) TMG_LAUNCH(k_gather_b<zd>, dim3(nblk(nl), B), 256, 0, st, nl, um.lower2csc.p, vals_csc, nU, lower.p, nl);
+    if (nU) TMG_LAUNCH(k_gather_b<zd>, dim3(nblk(nU), B), 256, 0, st, nU, um.csr2csc.p, vals_csc, nU, acsr.p, nU);
+    ShiftInvertB<zd, Tf> op;
+    op.c = c; op.D = &os.D; op.um = &um; op.n = um.U.ncols; op.B = B; op.mixed = mixed;
+    op.A.nrows = um.U.ncols; op.A.nnz = nU; op.A.rowptr = um.csr_rowptr.p; op.A.col = um.csr_col.p;
+    op.A.val = acsr.p; op.A.vstride = nU;
+    cudaEvent_t ev[4];
+    for (auto& e : ev) TMG_CUDA(cudaEventCreate(&e));
+    TMG_CUDA(cudaEventRecord(ev[0], st));
+    op.factor(lower.p);
+    TMG_CUDA(cudaEventRecord(ev[1], st));
+    lower.release();
+    op.solve1(op.r.p, op.z.p);   // the first solve captures the graph
+    TMG_CUDA(cudaEventRecord(ev[2], st));
+    const int ns = 4;
+    for (int q = 0; q < ns; q++) op.solve1(op.r.p, op.z.p);
+    TMG_CUDA(cudaEventRecord(ev[3], st));
+    TMG_CUDA(cudaEventSynchronize(ev[3]));
+    TuneRow row;
+    float f_ms = 0.f, s_ms = 0.f;
+    TMG_CUDA(cudaEventElapsedTime(&f_ms, ev[0], ev[1]));
+    TMG_CUDA(cudaEventElapsedTime(&s_ms, ev[2], ev[3]));
+    row.factor_ms = f_ms;
+    row.solve_ms = s_ms / ns;
+    for (auto& e : ev) cudaEventDestroy(e);
+    row.stored = os.D.l_entries;
+    row.supernodes = os.D.ns;
+    return row;
+}
+
+void tune_complex(tmg_context* c, const UnionMaps& um, const zd* vals_csc, int B, bool mixed) {
+    const std::string key = c->symC_key + (mixed ? "|mixed" : "|fp64");
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            const TuneCand& w = it->second;
+            if (w.relax != c->tune_choice.relax || w.maxw != c->tune_choice.maxw || w.tc_min != c->tune_choice.tc_min) {
+                const std::vector<int32_t> amd = c->symC.S.amd;
+                analyze_op(c->symC, um, &w, &amd);
+            }
+            c->tune_choice = w;
+            c->tuned_key = c->symC_key;
+            return;
+        }
+    }
+    std::vector<TuneCand> cands = {{0.0, 0, MF_TC_MIN_ROWS}, {0.1, 256, MF_TC_MIN_ROWS}, {0.25, 256, MF_TC_MIN_ROWS},
+                                   {0.25, 512, MF_TC_MIN_ROWS}};
+    if (mixed) cands.push_back({0.0, 0, 384});
+    const double S = c->solves_per_factor > 0 ? c->solves_per_factor : (mixed ? 256.0 : 45.0);
+    const std::vector<int32_t> amd = c->symC.S.amd;
+    c->tune_rows.clear();
+    int best = -1;
+    for (size_t q = 0; q < cands.size(); q++) {
+        OpSymbolic os;
+        analyze_op(os, um, &cands[q], &amd);
+        TuneRow row = mixed ? tune_trial<zf>(c, os, um, vals_csc, B, true) : tune_trial<zd>(c, os, um, vals_csc, B, false);
+        row.cand = cands[q];
+        row.score_ms = row.factor_ms + S * row.solve_ms;
+        c->tune_rows.push_back(row);
+        if (best < 0 || row.score_ms < c->tune_rows[best].score_ms) best = (int)q;
+        if (std::getenv("TMG_VERBOSE"))
+            std::fprintf(stderr, "[tmg] tune relax %.2f maxw %d tc %d: factor %.1f ms, solve %.2f ms, score %.1f ms, "
+                         "%lld stored, %d supernodes\n", cands[q].relax, cands[q].maxw, cands[q].tc_min,
+                         row.factor_ms, row.solve_ms, row.score_ms, (long long)row.stored, row.supernodes);
+    }
+    const TuneCand w = cands[best];
+    analyze_op(c->symC, um, &w, &amd);
+    c->tune_choice = w;
+    c->tuned_key = c->symC_key;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = w;
 }
 
 // Problems per batch that fit the device-memory budget.
@@ -1856,11 +1971,11 @@ void solve_qep(tmg_context* c, std::vector<Problem>& probs, int num_modes, doubl
     const bool dense = n2 <= 200;
     const int nev = dense ? (int)n2 - 1 : (int)std::min<int64_t>(6 * (int64_t)num_modes, n2 - 1);
     const int ncv = (int)std::min<int64_t>(std::max(4 * nev + 1, 40), n2);
-    if (nev <= 0 || (!dense && ncv > 256)) {
+    if (nev <= 0 || (!dense && ncv > LZ_MAXM)) {
         for (auto& pr : probs) pr.R->status = TMG_ERR_NUMERIC;
         c->err = nev <= 0 ? "Coriolis QEP: system too small for the requested modes"
-                          : "Coriolis QEP: a Lanczos subspace of " + std::to_string(ncv) +
-                                " vectors (num_modes > 10) is not supported";
+                          : "Coriolis QEP: a Lanczos subspace of " + std::to_string(ncv) + " vectors (num_modes > " +
+                                std::to_string((LZ_MAXM - 1) / 24) + ") is not supported";
         return;
     }
     const UnionMaps &WK = c->W0, &WM = c->WM0, &WG = c->WG0;
@@ -2167,7 +2282,7 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
     }
     // complex harmonics: one shared symbolic analysis, batched under the memory budget
     if (!cplx.empty()) {
-        if (!c->symC.valid) analyze_op(c->symC, c->opC);
+        if (!c->symC.valid) { analyze_op(c->symC, c->opC); c->tune_choice = TuneCand{}; }
         UnionMaps& um = c->opC;
         UnionMaps& mu = c->opMC;
         int nev = std::min(cplx[0].nev_target + n_extra, S.n_free - 1);
@@ -2195,6 +2310,7 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
                            mu.U.nnz(), mcsr.p, mu.U.nnz());
             }
             mvals.release();
+            if (c->autotune && c->tuned_key != c->symC_key) tune_complex(c, um, vals.p, B, mixed);
             DevCsr<zd> M;
             M.nrows = S.n_free; M.nnz = mu.U.nnz(); M.rowptr = mu.csr_rowptr.p; M.col = mu.csr_col.p; M.val = mcsr.p;
             M.vstride = mu.U.nnz();
@@ -2288,13 +2404,29 @@ void solve_sweep(tmg_context* c, const std::vector<double>& rpms, const std::vec
     while (g0 < rpms.size()) {
         // the group: speeds after g0 with the pattern of g0 whose problems fit one batch
         prepare(c, rpms[g0], false);
-        if (!c->symC.valid) analyze_op(c->symC, c->opC);
+        if (!c->symC.valid) { analyze_op(c->symC, c->opC); c->tune_choice = TuneCand{}; }
         if (!c->pairSym.valid) analyze_op(c->pairSym, c->pairOp);
         const std::string key = c->symC_key;
         std::vector<int> cks, rks;
         for (int k : ks) {
             const bool is_real = (k == 0) || (N % 2 == 0 && k == max_k);
             (is_real ? rks : cks).push_back(k);
+        }
+        if (c->autotune && c->tuned_key != c->symC_key && !cks.empty()) {
+            // tune on this speed's complex harmonics before the group is sized
+            const int Bt = (int)cks.size();
+            std::vector<double> ph(2 * Bt);
+            for (int p = 0; p < Bt; p++) { ph[2 * p] = std::cos(cks[p] * alpha); ph[2 * p + 1] = std::sin(cks[p] * alpha); }
+            DVec<double> dph;
+            dph.upload(ph);
+            DVec<zd> tv;
+            const int64_t nUt = c->opC.U.nnz();
+            tv.alloc((size_t)Bt * std::max<int64_t>(1, nUt));
+            if (nUt)
+                TMG_LAUNCH(k_form_complex, dim3(nblk(nUt), Bt), 256, 0, st, nUt, c->opC.maps[0].p, c->opC.maps[1].p,
+                           c->opC.maps[2].p, c->opC.maps[3].p, c->opC.maps[4].p, c->opC.maps[5].p, c->Kcf.sv.p,
+                           c->Kpf.sv.p, c->Mcf.sv.p, c->Mpf.sv.p, dph.p, shift, tv.p);
+            tune_complex(c, c->opC, tv.p, Bt, mixed);
         }
         int nev_c = 1, nev_r = 1;
         for (int k : cks) nev_c = std::max(nev_c, std::min((num_modes + 1) / 2 + n_extra, S.n_free - 1));
@@ -2570,6 +2702,9 @@ int tmg_set_option(tmg_context* c, int option, double value) {
         case TMG_OPT_TENSOR_CORES:
             c->tensor_cores = value != 0.0;
             return TMG_OK;
+        case TMG_OPT_AUTOTUNE:
+            c->autotune = value != 0.0;
+            return TMG_OK;
         default:
             return set_err(c, TMG_ERR_ARG, "unknown option " + std::to_string(option));
     }
@@ -2581,6 +2716,7 @@ int tmg_get_option(tmg_context* c, int option, double* value) {
         case TMG_OPT_SHIFT: *value = c->shift; return TMG_OK;
         case TMG_OPT_DEFLATE: *value = c->deflate ? 1.0 : 0.0; return TMG_OK;
         case TMG_OPT_TENSOR_CORES: *value = c->tensor_cores ? 1.0 : 0.0; return TMG_OK;
+        case TMG_OPT_AUTOTUNE: *value = c->autotune ? 1.0 : 0.0; return TMG_OK;
         default: return set_err(c, TMG_ERR_ARG, "unknown option " + std::to_string(option));
     }
 }
@@ -2889,6 +3025,21 @@ int tmg_result_info(tmg_context* c, int idx, tmg_result_meta* info) {
     info->rpm = R.rpm;
     info->max_residual = R.max_residual;
     info->refine_residual = R.refine_residual;
+    return TMG_OK;
+}
+
+int tmg_tuning_report(tmg_context* c, double* out, int max_rows, int* rows) {
+    if (!c || !rows) return TMG_ERR_ARG;
+    *rows = (int)c->tune_rows.size();
+    if (!out) return TMG_OK;
+    for (int r = 0; r < std::min(max_rows, *rows); r++) {
+        const TuneRow& t = c->tune_rows[r];
+        const bool chosen = t.cand.relax == c->tune_choice.relax && t.cand.maxw == c->tune_choice.maxw &&
+                            t.cand.tc_min == c->tune_choice.tc_min;
+        double* o = out + (size_t)r * 9;
+        o[0] = t.cand.relax; o[1] = t.cand.maxw; o[2] = t.cand.tc_min; o[3] = t.factor_ms; o[4] = t.solve_ms;
+        o[5] = t.score_ms; o[6] = (double)t.stored; o[7] = t.supernodes; o[8] = chosen ? 1.0 : 0.0;
+    }
     return TMG_OK;
 }
 

@@ -128,7 +128,7 @@ void lz_three_term(cudaStream_t st, int B, int64_t n, int j, const T* dot, doubl
 template <typename T>
 __global__ void k_gemv_sub(int64_t n, int K, const T* __restrict__ V, int64_t vs, const T* __restrict__ h, int ldh,
                            T* __restrict__ w, int64_t ws) {
-    __shared__ T hs[256];
+    __shared__ T hs[LZ_MAXM];
     const int64_t p = blockIdx.y;
     for (int k = threadIdx.x; k < K; k += blockDim.x) hs[k] = h[p * ldh + k];
     __syncthreads();
@@ -141,7 +141,7 @@ __global__ void k_gemv_sub(int64_t n, int K, const T* __restrict__ V, int64_t vs
 }
 template <typename T>
 void lz_gemv_sub(cudaStream_t st, int B, int64_t n, int K, const T* V, int64_t vs, const T* h, int ldh, T* w, int64_t ws) {
-    if (K > 256) throw std::runtime_error("Lanczos subspace above 256 vectors is not supported");
+    if (K > LZ_MAXM) throw std::runtime_error("Lanczos subspace above " + std::to_string(LZ_MAXM) + " vectors is not supported");
     TMG_LAUNCH(k_gemv_sub<T>, dim3((unsigned)ceil_div(n, 256), B), 256, 0, st, n, K, V, vs, h, ldh, w, ws);
     TMG_CHECK_LAUNCH();
 }
@@ -195,8 +195,8 @@ __global__ void __launch_bounds__(256) k_tridiag(int m, int ldab, int nev, doubl
                                                  double* __restrict__ theta_b, double* __restrict__ S_b,
                                                  double* __restrict__ lam_b, int* __restrict__ order_b,
                                                  int* __restrict__ nconv, double* __restrict__ Z_b) {
-    __shared__ double d[256], e[256], rc[256], rs[256], lamv[256];
-    __shared__ int perm[256], ord[256];
+    __shared__ double d[LZ_MAXM], e[LZ_MAXM], rc[LZ_MAXM], rs[LZ_MAXM], lamv[LZ_MAXM];
+    __shared__ int perm[LZ_MAXM], ord[LZ_MAXM];
     __shared__ int s_m, s_go, s_lo, s_hi;
     const int p = blockIdx.x;
     const double shift = shifts ? shifts[p] : shift0;
@@ -207,10 +207,12 @@ __global__ void __launch_bounds__(256) k_tridiag(int m, int ldab, int nev, doubl
     int* order = order_b + (int64_t)p * ldab;
     double* S = S_b + (int64_t)p * ldab * ldab;
     double* Z = Z_b + (int64_t)p * ldab * ldab;
-    const int k = threadIdx.x;
-    for (int c = 0; c < m; c++)
-        if (k < m) Z[(int64_t)c * m + k] = (c == k) ? 1.0 : 0.0;
-    if (k < m) { d[k] = alpha[k]; e[k] = (k < m - 1) ? beta[k] : 0.0; }
+    const int k = threadIdx.x;   // thread 0 runs the scalar recurrences; rows r = k, k + blockDim, ...
+    for (int r = k; r < m; r += blockDim.x) {
+        for (int c = 0; c < m; c++) Z[(int64_t)c * m + r] = (c == r) ? 1.0 : 0.0;
+        d[r] = alpha[r];
+        e[r] = (r < m - 1) ? beta[r] : 0.0;
+    }
     __syncthreads();
     const double eps = 2.220446049250313e-16;
     double f = 0.0, tst1 = 0.0;   // meaningful in thread 0 only
@@ -267,13 +269,13 @@ __global__ void __launch_bounds__(256) k_tridiag(int m, int ldab, int nev, doubl
                 s_go = (fabs(e[l]) > eps * tst1 && iter < 200) ? 1 : 0;
             }
             __syncthreads();
-            if (k < m) {
+            for (int r = k; r < m; r += blockDim.x) {
                 for (int i = s_hi; i >= s_lo; i--) {
                     const double c = rc[i], s = rs[i];
-                    const double h = Z[(int64_t)(i + 1) * m + k];
-                    const double zi = Z[(int64_t)i * m + k];
-                    Z[(int64_t)(i + 1) * m + k] = s * zi + c * h;
-                    Z[(int64_t)i * m + k] = c * zi - s * h;
+                    const double h = Z[(int64_t)(i + 1) * m + r];
+                    const double zi = Z[(int64_t)i * m + r];
+                    Z[(int64_t)(i + 1) * m + r] = s * zi + c * h;
+                    Z[(int64_t)i * m + r] = c * zi - s * h;
                 }
             }
             __syncthreads();
@@ -303,11 +305,11 @@ __global__ void __launch_bounds__(256) k_tridiag(int m, int ldab, int nev, doubl
         }
     }
     __syncthreads();
-    if (k < m) {
-        theta[k] = d[perm[k]];
-        lam[k] = lamv[k];
-        order[k] = ord[k];
-        for (int c = 0; c < m; c++) S[(int64_t)c * m + k] = Z[(int64_t)perm[c] * m + k];
+    for (int r = k; r < m; r += blockDim.x) {
+        theta[r] = d[perm[r]];
+        lam[r] = lamv[r];
+        order[r] = ord[r];
+        for (int c = 0; c < m; c++) S[(int64_t)c * m + r] = Z[(int64_t)perm[c] * m + r];
     }
     __syncthreads();
     if (k == 0) {
@@ -325,7 +327,7 @@ __global__ void __launch_bounds__(256) k_tridiag(int m, int ldab, int nev, doubl
 void lz_tridiag(cudaStream_t st, int B, int m, int ldab, int nev, double shift, double tol, const double* alpha,
                 const double* beta, double* theta, double* S, double* lam, int* order, int* nconv, double* Z,
                 const double* shifts) {
-    if (m > 256) throw std::runtime_error("Lanczos subspace above 256 vectors is not supported");
+    if (m > LZ_MAXM) throw std::runtime_error("Lanczos subspace above " + std::to_string(LZ_MAXM) + " vectors is not supported");
     TMG_LAUNCH(k_tridiag, B, 256, 0, st, m, ldab, nev, shift, shifts, tol, alpha, beta, theta, S, lam, order, nconv, Z);
     TMG_CHECK_LAUNCH();
 }
@@ -368,20 +370,21 @@ __global__ void __launch_bounds__(256) k_restart_qr(int m, int ldab, int nev, co
         }
     }
     __syncthreads();
-    const int row = threadIdx.x;
-    if (row >= m) return;
-    for (int c = 0; c < m; c++) Q[(int64_t)c * m + row] = (c == row) ? 1.0 : 0.0;
-    for (int s = 0; s < ns; s++)
-        for (int i = 0; i < m - 1; i++) {
-            const double c = rot[2 * ((int64_t)s * (m - 1) + i)], sn = rot[2 * ((int64_t)s * (m - 1) + i) + 1];
-            const double q0 = Q[(int64_t)i * m + row], q1 = Q[(int64_t)(i + 1) * m + row];
-            Q[(int64_t)i * m + row] = c * q0 + sn * q1;
-            Q[(int64_t)(i + 1) * m + row] = -sn * q0 + c * q1;
-        }
+    for (int row = threadIdx.x; row < m; row += blockDim.x) {
+        for (int c = 0; c < m; c++) Q[(int64_t)c * m + row] = (c == row) ? 1.0 : 0.0;
+        for (int s = 0; s < ns; s++)
+            for (int i = 0; i < m - 1; i++) {
+                const double c = rot[2 * ((int64_t)s * (m - 1) + i)], sn = rot[2 * ((int64_t)s * (m - 1) + i) + 1];
+                const double q0 = Q[(int64_t)i * m + row], q1 = Q[(int64_t)(i + 1) * m + row];
+                Q[(int64_t)i * m + row] = c * q0 + sn * q1;
+                Q[(int64_t)(i + 1) * m + row] = -sn * q0 + c * q1;
+            }
+    }
 }
 
 void lz_restart_qr(cudaStream_t st, int B, int m, int ldab, int nev, const double* theta, double* alpha, double* beta,
                    double* Q, double* rot, int64_t rot_stride) {
+    if (m > LZ_MAXM) throw std::runtime_error("Lanczos subspace above " + std::to_string(LZ_MAXM) + " vectors is not supported");
     TMG_LAUNCH(k_restart_qr, B, 256, 0, st, m, ldab, nev, theta, alpha, beta, Q, rot, rot_stride);
     TMG_CHECK_LAUNCH();
 }

@@ -24,6 +24,7 @@ struct DevCsr {
 };
 
 constexpr int LZ_DOT_BLOCKS = 152;
+constexpr int LZ_MAXM = 512;      // largest Lanczos subspace (tridiagonal size) the kernels handle
 
 // y[p](:, v) = A[p] x[p](:, v)   (or y -= A x); vectors of length A.nrows at x + p*xs + v*ld
 template <typename T>

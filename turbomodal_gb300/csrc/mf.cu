@@ -907,7 +907,7 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
                     const int64_t kend = std::min<int64_t>((int64_t)(kb + 1) * MF_NB, w);
                     const bool sb_end = kend == w || kend % MF_SB == 0;   // this pivot block closes a super-block
                     if (!sb_end) continue;
-                    const bool tc = m - kend >= MF_TC_MIN_ROWS;
+                    const bool tc = m - kend >= tc_min_rows;
                     if (tc != (pass == 1)) continue;
                     if (tc) tcf.push_back(s);
                     for (int64_t j0 = kend; j0 < m; j0 += MF_TILE)

@@ -81,6 +81,7 @@ struct DevSymbolic {
     };
     std::vector<Step> steps;
     int64_t tc_rows = 0;       // staging rows (complex) per problem of the largest tc group
+    int32_t tc_min_rows = MF_TC_MIN_ROWS;   // set before upload: tensor-core threshold of the plan
     using SolveLevel = tmg::SolveLevel;
     using SolvePlan = tmg::SolvePlan;
     SolvePlan plan64;          // the solve schedule for 64-wide diagonal blocks

@@ -7,19 +7,24 @@
 // real product of interleaved operands: complex row i of A = L(rows, SB) becomes real rows
 // 2i (Re) and 2i+1 (Im), and likewise for B = L(rows, SB) diag(d), so
 //     P = A_r B_r^T,  Re C(i, j) = P(2i, 2j) + P(2i+1, 2j+1),  Im C(i, j) = P(2i+1, 2j) - P(2i, 2j+1),
-// four real multiply-adds per complex one, none wasted.  FP32 accuracy comes from the 3xTF32
-// split x = hi + lo (hi, lo rounded to TF32): A B^T ~ Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T.
+// four real multiply-adds per complex one, none wasted.  FP32 accuracy comes from a three-way
+// BF16 split x = x1 + x2 + x3 (each x_k = bf16(x - x1 - ... - x_{k-1}); 3 x 8 significand bits
+// hold the 24 of an FP32 value): A B^T ~ sum over the pieces of order below 2^-16,
+//     A1 B1 + A1 B2 + A2 B1 + A1 B3 + A3 B1 + A2 B2,
+// six kind::f16 products with exact BF16 x BF16 terms and FP32 accumulation.  The dropped terms
+// are below 2^-23 of |A||B|, the rounding level of the FP32 SIMT update they replace.
 //
-// k_stage_tc writes, once per super-block and front, the rows [kend, m) of the four operand
-// planes (Ahi, Alo, Bhi, Blo) K-major (256 floats per real row) into a staging tensor.
+// k_stage_tc writes, once per super-block and front, the rows [kend, m) of the six operand
+// planes (A1, A2, A3, B1, B2, B3) K-major (256 BF16 per real row) into a staging tensor.
 // k_update_tc computes one 64x64 complex tile (a 128x128 real accumulator in TMEM) per CTA:
-// warp 0 issues TMA loads of 128x32-float boxes (128-byte swizzle) into a 3-stage ring,
-// warp 1 issues tcgen05.mma kind::tf32 (M = N = 128, K = 8; three per K step), and all four
-// warps read the accumulator back with tcgen05.ld, combine the real parts into complex
-// entries and subtract them from the front.  Every mbarrier wait is bounded (about one
-// second of clock): on expiry the kernel records an error code, stops issuing, waits (again
-// bounded) for what it issued, frees its TMEM and returns without writing.
+// warp 0 issues TMA loads of 128 x 64-BF16 boxes (128-byte swizzle) into a 2-stage ring,
+// warp 1 issues tcgen05.mma kind::f16 (BF16 in, FP32 accumulate; M = N = 128, K = 16; six per
+// K step), and all four warps read the accumulator back with tcgen05.ld, combine the real parts
+// into complex entries and subtract them from the front.  Every mbarrier wait is bounded
+// (about one second of clock): on expiry the kernel records an error code, stops issuing,
+// waits (again bounded) for what it issued, frees its TMEM and returns without writing.
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
 #include <cstring>
@@ -32,18 +37,20 @@ namespace tmg {
 
 namespace {
 
-constexpr int TC_STAGES = 3;
+constexpr int TC_STAGES = 2;
 constexpr int TC_STAGE_ROWS = 16;                  // complex rows per staging item
-constexpr int TC_BOX_K = 32;                       // floats per TMA box row (128 bytes)
+constexpr int TC_PLANES = 6;                       // A1, A2, A3, B1, B2, B3
+constexpr int TC_KS = 256;                         // BF16 per staged real row (one super-block)
+constexpr int TC_BOX_K = 64;                       // BF16 per TMA box row (128 bytes)
 constexpr int TC_ROWS = 128;                       // real rows per operand tile
-constexpr int TC_TILE_BYTES = TC_ROWS * TC_BOX_K * 4;   // 16 KB
-constexpr int TC_STAGE_BYTES = 4 * TC_TILE_BYTES;       // Ahi, Alo, Bhi, Blo
+constexpr int TC_TILE_BYTES = TC_ROWS * TC_BOX_K * 2;   // 16 KB
+constexpr int TC_STAGE_BYTES = TC_PLANES * TC_TILE_BYTES;
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /* alignment slack */ + 256 /* barriers */;
 constexpr int TC_TMEM_COLS = 128;
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;      // ~1 s at 2 GHz
 
-// instruction descriptor of tcgen05.mma kind::tf32: D F32, A/B TF32, both K-major, M = 128, N = 128
-constexpr uint32_t TC_IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+// instruction descriptor of tcgen05.mma kind::f16: D F32, A/B BF16, both K-major, M = 128, N = 128
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -96,11 +103,11 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
         "l"(da), "l"(db), "r"(TC_IDESC), "r"(accumulate)
         : "memory");
 }
@@ -109,20 +116,25 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-__device__ __forceinline__ float tf32_round(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
+// three-way BF16 split: x = p[0] + p[1] + p[2] up to the last bits of an FP32 significand
+__device__ __forceinline__ void split3(float x, __nv_bfloat16 (&p)[3]) {
+    p[0] = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(p[0]);
+    p[1] = __float2bfloat16_rn(r1);
+    const float r2 = r1 - __bfloat162float(p[1]);
+    p[2] = __float2bfloat16_rn(r2);
 }
 
 // ------------------------------------------------------------------------------------
 // Staging.  Item (s, r0, dst0): complex rows r0 .. r0+15 of front s (rows >= m skipped) go to
 // staging rows dst0 .. of every problem's block; columns l in [kl, kl + Kp) of the current
-// super-block, zero beyond kend.  Plane q (0 Ahi, 1 Alo, 2 Bhi, 3 Blo) of problem p, real
-// row t: staging row q * plane_rows + p * prob_rows + t, 256 floats each.
+// super-block, zero beyond kend.  Plane q (0-2: the pieces of A = L, 3-5: those of
+// B = L diag(d)) of problem p, real row t: staging row q * plane_rows + p * prob_rows + t,
+// TC_KS BF16 each.
 __global__ void __launch_bounds__(256) k_stage_tc(const int32_t* __restrict__ items, int kb, SnDev S,
-                                                  const zf* __restrict__ L, int64_t lstride, float* __restrict__ stg,
-                                                  int64_t prob_rows, int64_t plane_rows) {
+                                                  const zf* __restrict__ L, int64_t lstride,
+                                                  __nv_bfloat16* __restrict__ stg, int64_t prob_rows,
+                                                  int64_t plane_rows) {
     __shared__ zf tile[256][TC_STAGE_ROWS + 1];   // [column l][row rr]
     __shared__ float dsh[256];
     const int64_t p = blockIdx.y;
@@ -153,14 +165,15 @@ __global__ void __launch_bounds__(256) k_stage_tc(const int32_t* __restrict__ it
         if (rr >= nrows) continue;
         const zf z = tile[l][rr];
         const float x = c ? z.y : z.x;
-        const float xs = dsh[l] * x;
-        const float ahi = tf32_round(x), bhi = tf32_round(xs);
-        const float alo = tf32_round(x - ahi), blo = tf32_round(xs - bhi);
+        __nv_bfloat16 a[3], b[3];
+        split3(x, a);
+        split3(dsh[l] * x, b);
         const int64_t row = p * prob_rows + 2 * (dst0 + rr) + c;
-        stg[(0 * plane_rows + row) * 256 + l] = ahi;
-        stg[(1 * plane_rows + row) * 256 + l] = alo;
-        stg[(2 * plane_rows + row) * 256 + l] = bhi;
-        stg[(3 * plane_rows + row) * 256 + l] = blo;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            stg[((int64_t)k * plane_rows + row) * TC_KS + l] = a[k];
+            stg[((int64_t)(3 + k) * plane_rows + row) * TC_KS + l] = b[k];
+        }
     }
 }
 
@@ -226,10 +239,9 @@ __global__ void __launch_bounds__(128, 1) k_update_tc(const int32_t* __restrict_
             const uint32_t sb = ring + st * TC_STAGE_BYTES;
             mbar_expect_tx(full(st), TC_STAGE_BYTES);
             const int x = kc * TC_BOX_K;
-            tma_load_2d(sb + 0 * TC_TILE_BYTES, &tmap, x, (int)(0 * plane_rows) + ya, full(st));
-            tma_load_2d(sb + 1 * TC_TILE_BYTES, &tmap, x, (int)(1 * plane_rows) + ya, full(st));
-            tma_load_2d(sb + 2 * TC_TILE_BYTES, &tmap, x, (int)(2 * plane_rows) + yb, full(st));
-            tma_load_2d(sb + 3 * TC_TILE_BYTES, &tmap, x, (int)(3 * plane_rows) + yb, full(st));
+#pragma unroll
+            for (int q = 0; q < TC_PLANES; q++)
+                tma_load_2d(sb + q * TC_TILE_BYTES, &tmap, x, (int)(q * plane_rows) + (q < 3 ? ya : yb), full(st));
             issued++;
         }
     } else if (warp == 1 && lane == 0) {
@@ -245,15 +257,21 @@ __global__ void __launch_bounds__(128, 1) k_update_tc(const int32_t* __restrict_
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t sb = ring + st * TC_STAGE_BYTES;
 #pragma unroll
-            for (int ks = 0; ks < TC_BOX_K / 8; ks++) {
-                const uint32_t off = ks * 32;   // 8 tf32 = 32 bytes along K inside the swizzled row
-                const uint64_t ahi = smem_desc(sb + 0 * TC_TILE_BYTES + off);
-                const uint64_t alo = smem_desc(sb + 1 * TC_TILE_BYTES + off);
-                const uint64_t bhi = smem_desc(sb + 2 * TC_TILE_BYTES + off);
-                const uint64_t blo = smem_desc(sb + 3 * TC_TILE_BYTES + off);
-                mma_tf32(tmem, ahi, bhi, (kc > 0 || ks > 0) ? 1u : 0u);
-                mma_tf32(tmem, ahi, blo, 1u);
-                mma_tf32(tmem, alo, bhi, 1u);
+            for (int ks = 0; ks < TC_BOX_K / 16; ks++) {
+                const uint32_t off = ks * 32;   // 16 BF16 = 32 bytes along K inside the swizzled row
+                const uint64_t a1 = smem_desc(sb + 0 * TC_TILE_BYTES + off);
+                const uint64_t a2 = smem_desc(sb + 1 * TC_TILE_BYTES + off);
+                const uint64_t a3 = smem_desc(sb + 2 * TC_TILE_BYTES + off);
+                const uint64_t b1 = smem_desc(sb + 3 * TC_TILE_BYTES + off);
+                const uint64_t b2 = smem_desc(sb + 4 * TC_TILE_BYTES + off);
+                const uint64_t b3 = smem_desc(sb + 5 * TC_TILE_BYTES + off);
+                // the smaller terms first
+                mma_bf16(tmem, a2, b2, (kc > 0 || ks > 0) ? 1u : 0u);
+                mma_bf16(tmem, a1, b3, 1u);
+                mma_bf16(tmem, a3, b1, 1u);
+                mma_bf16(tmem, a1, b2, 1u);
+                mma_bf16(tmem, a2, b1, 1u);
+                mma_bf16(tmem, a1, b1, 1u);
             }
             mma_commit(empty(st));   // this stage's smem may be refilled once these MMAs are done
         }
@@ -346,21 +364,21 @@ void mf_trail_tc(cudaStream_t st, const DevSymbolic& S, const Batch<zf>& bt, con
     if (stp.tc.empty()) return;
     const int64_t prob_rows = 2 * S.tc_rows;               // real staging rows per problem
     const int64_t plane_rows = prob_rows * bt.B;
-    if (!wk.stg || wk.rows < 4 * plane_rows) {
+    if (!wk.stg || wk.rows < TC_PLANES * plane_rows) {
         wk.release();
-        const size_t bytes = (size_t)4 * plane_rows * 256 * sizeof(float);
+        const size_t bytes = (size_t)TC_PLANES * plane_rows * TC_KS * sizeof(__nv_bfloat16);
         TMG_CUDA(cudaMallocAsync((void**)&wk.stg, bytes, st));
         TMG_CUDA(cudaMemsetAsync(wk.stg, 0, bytes, st));
         TMG_CUDA(cudaMallocAsync((void**)&wk.err, sizeof(int), st));
         TMG_CUDA(cudaMemsetAsync(wk.err, 0, sizeof(int), st));
-        wk.rows = 4 * plane_rows;
+        wk.rows = TC_PLANES * plane_rows;
         wk.stream = st;
         CUtensorMap map;
-        const cuuint64_t dims[2] = {256, (cuuint64_t)wk.rows};
-        const cuuint64_t strides[1] = {256 * sizeof(float)};
+        const cuuint64_t dims[2] = {TC_KS, (cuuint64_t)wk.rows};
+        const cuuint64_t strides[1] = {TC_KS * sizeof(__nv_bfloat16)};
         const cuuint32_t box[2] = {TC_BOX_K, TC_ROWS};
         const cuuint32_t estr[2] = {1, 1};
-        const CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, wk.stg, dims, strides, box, estr,
+        const CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, wk.stg, dims, strides, box, estr,
                                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) throw cuda_error("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
@@ -377,7 +395,7 @@ void mf_trail_tc(cudaStream_t st, const DevSymbolic& S, const Batch<zf>& bt, con
     const unsigned B = bt.B;
     for (const auto& g : stp.tc) {
         TMG_LAUNCH(k_stage_tc, dim3(g.stage_cnt, B), 256, 0, st, S.items + g.stage_off, stp.kb, sn, bt.L, bt.lstride,
-                   wk.stg, prob_rows, plane_rows);
+                   static_cast<__nv_bfloat16*>(wk.stg), prob_rows, plane_rows);
         TMG_LAUNCH(k_update_tc, dim3(g.upd_cnt, B), 128, TC_SMEM, st, S.items + g.upd_off, stp.kb, sn, bt.L, bt.U,
                    bt.lstride, bt.ustride, map, prob_rows, plane_rows, wk.err);
     }

@@ -11,7 +11,7 @@ namespace tmg {
 // Staging buffer and tensor map of the tensor-core updates of one factorisation (allocated on
 // first use, in the stream's order).
 struct TcWork {
-    float* stg = nullptr;        // 4 planes x B problems x 2 tc_rows real rows x 256 floats
+    void* stg = nullptr;         // 6 BF16 planes x B problems x 2 tc_rows real rows x 256 entries
     int* err = nullptr;          // nonzero: a bounded wait of k_update_tc expired
     int64_t rows = 0;
     cudaStream_t stream = nullptr;

@@ -416,14 +416,18 @@ Product product(const Pattern& A, const Pattern& B) {
 // ---------------------------------------------------------------------------------
 // Supernodal symbolic factorisation
 // ---------------------------------------------------------------------------------
-Symbolic analyze(const Pattern& lower, double relax, int32_t relax_max_width) {
+Symbolic analyze(const Pattern& lower, double relax, int32_t relax_max_width, const std::vector<int32_t>* amd) {
     Symbolic S;
     const int32_t n = lower.ncols;
     S.n = n;
-    // full symmetric pattern with diagonal, rows sorted
-    Pattern up = transpose(lower);
-    Pattern full = pattern_union({&lower, &up});
-    S.amd = amd_order(n, full.p, full.i);
+    if (amd && (int32_t)amd->size() == n) {   // the order of an earlier analysis of this pattern
+        S.amd = *amd;
+    } else {
+        // full symmetric pattern with diagonal, rows sorted
+        Pattern up = transpose(lower);
+        Pattern full = pattern_union({&lower, &up});
+        S.amd = amd_order(n, full.p, full.i);
+    }
     std::vector<int32_t> P(n);
     for (int32_t k = 0; k < n; k++) P[S.amd[k]] = k;
     // permuted upper pattern (AMD numbering): column max(pi,pj) holds row min(pi,pj)

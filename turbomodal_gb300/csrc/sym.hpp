@@ -57,7 +57,8 @@ struct Symbolic {
 // lower: lower-triangle pattern (orig numbering) of the operator.  relax: merge a child
 // supernode into its parent when the combined front adds at most this fraction of
 // explicit zeros (0 = fundamental supernodes only).
-Symbolic analyze(const Pattern& lower, double relax = 0.0, int32_t relax_max_width = 0);
+Symbolic analyze(const Pattern& lower, double relax = 0.0, int32_t relax_max_width = 0,
+                 const std::vector<int32_t>* amd = nullptr);
 
 // Triangular-solve schedule for diagonal blocks of width nb, per tree level (host side; the
 // device kernels read the item lists).  Forward: gather (the level's supernodes), triangle

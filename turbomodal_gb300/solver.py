@@ -122,6 +122,17 @@ class CyclicSymmetrySolver:
         complex FP32 factorisation, the default)."""
         self.ctx.check(self.ctx.L.tmg_set_option(self.ctx.h, _lib.OPT[name], float(value)), "tmg_set_option")
 
+    def tuning_report(self) -> list[dict]:
+        """Trials of the last supernode-shape tuning (set_option("autotune", 1))."""
+        rows = C.c_int()
+        self.ctx.check(self.ctx.L.tmg_tuning_report(self.ctx.h, None, 0, C.byref(rows)), "tmg_tuning_report")
+        out = np.zeros(9 * max(rows.value, 1))
+        self.ctx.check(self.ctx.L.tmg_tuning_report(self.ctx.h, _lib.ptr(out, C.c_double), rows.value, C.byref(rows)),
+                       "tmg_tuning_report")
+        keys = ("relax", "max_width", "tc_min_rows", "factor_ms", "solve_ms", "score_ms", "l_entries", "supernodes",
+                "chosen")
+        return [dict(zip(keys, out[9 * r:9 * r + 9].tolist())) for r in range(rows.value)]
+
     def get_option(self, name: str) -> float:
         v = C.c_double()
         self.ctx.check(self.ctx.L.tmg_get_option(self.ctx.h, _lib.OPT[name], C.byref(v)), "tmg_get_option")
