@@ -59,9 +59,11 @@ def parse():
                     help="speeds per solve_rpm_sweep call (their harmonics are factorised and iterated as one batch)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the served request-stream sample")
-    ap.add_argument("--serve-requests", type=int, default=12)
-    ap.add_argument("--serve-max-nodes", type=int, default=30000,
-                    help="largest sector of the request-stream sample (the full stream goes to 200000)")
+    ap.add_argument("--serve-requests", type=int, default=16)
+    ap.add_argument("--serve-max-nodes", type=int, default=200000,
+                    help="largest sector of the request-stream sample")
+    ap.add_argument("--serve-designs", type=int, default=4,
+                    help="distinct sector designs the requests draw from (repeats are batched and reuse contexts)")
     return ap.parse_args()
 
 
@@ -492,14 +494,17 @@ def main():
             from turbomodal_gb300.serve import ModalServer, latency_summary, request_stream
 
             reqs = request_stream(args.serve_requests, seed=2024, rate_hz=20.0, min_nodes=2000,
-                                  max_nodes=args.serve_max_nodes)
+                                  max_nodes=args.serve_max_nodes, distinct_sectors=args.serve_designs)
             srv = ModalServer(device=local, budget_bytes=150 << 30, max_inflight=4)
             done = srv.serve(reqs)
             srv.close()
             serving = latency_summary(done)
-            serving["sample"] = (f"{len(reqs)} requests, Poisson 20 req/s, config-0/1-style sectors of 2000-"
-                                 f"{args.serve_max_nodes} nodes (log-uniform), 24/36/48 sectors, rpm U(0,15000), "
-                                 "5-20 modes, 1-19 random harmonics, mixed precision, 150 GB budget, 4 in flight")
+            sizes = sorted({r.mesh.num_nodes() for r in reqs})
+            serving["sample"] = (f"{len(reqs)} requests, Poisson 20 req/s, drawn from {args.serve_designs} config-0/1-"
+                                 f"style sector designs ({', '.join(str(n) for n in sizes)} nodes; log-uniform in "
+                                 f"2000-{args.serve_max_nodes}), 24/36/48 sectors, rpm U(0,15000), 5-20 modes, 1-19 "
+                                 "random harmonics, mixed precision, 150 GB budget, 4 in flight, same-sector "
+                                 "requests batched")
             log(f"serving sample: p50 {serving.get('p50_s')} s, p99 {serving.get('p99_s')} s")
     if rank == 0:
         cpu = None

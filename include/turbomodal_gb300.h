@@ -183,6 +183,13 @@ int tmg_solve_sweep(tmg_context* ctx, const double* rpms, int nrpm, int num_mode
 int tmg_result_info(tmg_context* ctx, int idx, tmg_result_meta* info);
 int tmg_result_copy(tmg_context* ctx, int idx, double* freqs, double* shapes, int32_t* whirl);
 
+/* Device memory this context holds now (*current: sector data, operators, symbolic
+ * analyses, results of the last solve kept for copying) and the most it held since creation or
+ * tmg_reset_peak_bytes (*peak), in bytes; either pointer may be NULL.  For admission control
+ * of concurrent contexts; no counterpart in the reference, which runs on the CPU. */
+int tmg_device_bytes(tmg_context* ctx, int64_t* current, int64_t* peak);
+int tmg_reset_peak_bytes(tmg_context* ctx);
+
 /* Trials of the last supernode-shape tuning (TMG_OPT_AUTOTUNE); no counterpart in the reference,
  * whose simplicial factorisation has no tile shapes.  *rows = number of trials; out (may be NULL)
  * receives min(max_rows, *rows) rows of 9 doubles: relax, front width cap, tensor-core row

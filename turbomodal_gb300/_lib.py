@@ -28,7 +28,8 @@ EXPORTED = ["tmg_create", "tmg_destroy", "tmg_last_error", "tmg_upload_sector", 
             "tmg_prepare", "tmg_projection", "tmg_symbolic", "tmg_solve_at_rpm", "tmg_result_info",
             "tmg_result_copy", "tmg_last_timing", "tmg_symbolic_stats",
             "tmg_set_profiling", "tmg_profile_solve", "tmg_projection_harmonic_static", "tmg_set_memory_budget",
-            "tmg_set_option", "tmg_get_option", "tmg_result_modal_mass", "tmg_solve_sweep", "tmg_tuning_report"]
+            "tmg_set_option", "tmg_get_option", "tmg_result_modal_mass", "tmg_solve_sweep", "tmg_tuning_report",
+            "tmg_device_bytes", "tmg_reset_peak_bytes"]
 OPT = {"shift": 0, "deflate": 1, "tensor_cores": 2, "autotune": 3}
 
 
@@ -88,6 +89,8 @@ def load(build_if_missing: bool = True):
     L.tmg_set_option.argtypes = [P, C.c_int, C.c_double]
     L.tmg_result_modal_mass.argtypes = [P, C.c_int, DP]
     L.tmg_tuning_report.argtypes = [P, DP, C.c_int, C.POINTER(C.c_int)]
+    L.tmg_device_bytes.argtypes = [P, I64P, I64P]
+    L.tmg_reset_peak_bytes.argtypes = [P]
     L.tmg_solve_sweep.argtypes = [P, DP, C.c_int, C.c_int, I32P, C.c_int, C.c_int, C.c_double, C.c_int, I32P]
     L.tmg_get_option.argtypes = [P, C.c_int, DP]
     _lib = L

@@ -30,6 +30,13 @@ extern thread_local int64_t g_kernel_launches;
 // Stream of the context the calling thread is working for (set on entry to every C-ABI call
 // that touches the device); device buffers are allocated, copied and freed in its order.
 extern thread_local cudaStream_t g_stream;
+// Device bytes held by the context the calling thread is working for (its stream-ordered
+// buffers; null outside a C-ABI call).
+struct ByteCount {
+    int64_t cur = 0, peak = 0;
+    void add(int64_t b) { cur += b; if (cur > peak) peak = cur; }
+};
+extern thread_local ByteCount* g_bytes;
 #define TMG_LAUNCH(kernel, grid, block, smem, stream, ...)                                    \
     do {                                                                                      \
         kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);                            \

@@ -431,6 +431,9 @@ struct ResultHost {
 };
 
 struct tmg_context {
+    // device bytes this context holds (current, peak); first member, so it outlives every
+    // buffer that counts itself in it during destruction
+    ByteCount bytes;
     int device = 0;
     cudaStream_t st = nullptr;
     size_t budget = 0;
@@ -541,6 +544,8 @@ int guarded(tmg_context* c, F&& fn) {
     try {
         cudaSetDevice(c->device);
         g_stream = c->st;
+        g_bytes = &c->bytes;
+        struct Reset { ~Reset() { g_bytes = nullptr; } } reset;
         return fn();
     } catch (const cuda_error& e) {
         return set_err(c, TMG_ERR_CUDA, e.what());
@@ -3025,6 +3030,19 @@ int tmg_result_info(tmg_context* c, int idx, tmg_result_meta* info) {
     info->rpm = R.rpm;
     info->max_residual = R.max_residual;
     info->refine_residual = R.refine_residual;
+    return TMG_OK;
+}
+
+int tmg_device_bytes(tmg_context* c, int64_t* current, int64_t* peak) {
+    if (!c) return TMG_ERR_ARG;
+    if (current) *current = c->bytes.cur;
+    if (peak) *peak = c->bytes.peak;
+    return TMG_OK;
+}
+
+int tmg_reset_peak_bytes(tmg_context* c) {
+    if (!c) return TMG_ERR_ARG;
+    c->bytes.peak = c->bytes.cur;
     return TMG_OK;
 }
 

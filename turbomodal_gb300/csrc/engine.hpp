@@ -23,14 +23,15 @@ struct DVec {
     T* p = nullptr;
     size_t n = 0;
     cudaStream_t s_ = nullptr;       // stream the buffer was allocated on (freed in its order)
+    ByteCount* cnt_ = nullptr;       // the owning context's byte count
     DVec() = default;
     DVec(const DVec&) = delete;
     DVec& operator=(const DVec&) = delete;
-    DVec(DVec&& o) noexcept : p(o.p), n(o.n), s_(o.s_) { o.p = nullptr; o.n = 0; }
+    DVec(DVec&& o) noexcept : p(o.p), n(o.n), s_(o.s_), cnt_(o.cnt_) { o.p = nullptr; o.n = 0; o.cnt_ = nullptr; }
     DVec& operator=(DVec&& o) noexcept {
         release();
-        p = o.p; n = o.n; s_ = o.s_;
-        o.p = nullptr; o.n = 0;
+        p = o.p; n = o.n; s_ = o.s_; cnt_ = o.cnt_;
+        o.p = nullptr; o.n = 0; o.cnt_ = nullptr;
         return *this;
     }
     ~DVec() { release(); }
@@ -40,7 +41,11 @@ struct DVec {
         release();
         n = count;
         s_ = g_stream;
-        if (count) TMG_CUDA(cudaMallocAsync((void**)&p, count * sizeof(T), s_));
+        if (count) {
+            TMG_CUDA(cudaMallocAsync((void**)&p, count * sizeof(T), s_));
+            cnt_ = g_bytes;
+            if (cnt_) cnt_->add((int64_t)(count * sizeof(T)));
+        }
     }
     void zero(cudaStream_t st) { if (n) TMG_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), st)); }
     void upload(const std::vector<T>& h) {
@@ -60,9 +65,13 @@ struct DVec {
         return h;
     }
     void release() {
-        if (p) cudaFreeAsync(p, s_);
+        if (p) {
+            cudaFreeAsync(p, s_);
+            if (cnt_) cnt_->cur -= (int64_t)(n * sizeof(T));
+        }
         p = nullptr;
         n = 0;
+        cnt_ = nullptr;
     }
     size_t bytes() const { return n * sizeof(T); }
 };

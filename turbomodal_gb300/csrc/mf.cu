@@ -25,6 +25,7 @@ namespace tmg {
 
 thread_local int64_t g_kernel_launches = 0;
 thread_local cudaStream_t g_stream = nullptr;
+thread_local ByteCount* g_bytes = nullptr;
 
 template <typename T>
 __device__ __forceinline__ T dev_div(T a, typename real_of<T>::type d) { return a / d; }
@@ -805,10 +806,12 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
     }
     u_entries = std::max<int64_t>(ff.peak, 1);
     alloc_stream = g_stream;
+    cnt = g_bytes;
     auto put = [&](auto*& dptr, const auto& vec) {
         using E = typename std::decay<decltype(vec[0])>::type;
         const size_t b = std::max<size_t>(1, vec.size()) * sizeof(E);
         TMG_CUDA(cudaMallocAsync((void**)&dptr, b, alloc_stream));
+        if (cnt) cnt->add((int64_t)b);
         if (!vec.empty())
             TMG_CUDA(cudaMemcpyAsync(dptr, vec.data(), vec.size() * sizeof(E), cudaMemcpyHostToDevice, alloc_stream));
         TMG_CUDA(cudaStreamSynchronize(alloc_stream));   // the host vectors are temporaries
@@ -978,6 +981,7 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
 }
 
 void DevSymbolic::release() {
+    if (bytes && cnt) cnt->cur -= (int64_t)bytes;
     for (void* p : {(void*)sn_first, (void*)sn_rows, (void*)rel, (void*)child_ptr, (void*)child_list,
                     (void*)sn_row_ptr, (void*)loff, (void*)uoff, (void*)rel_ptr, (void*)perm, (void*)level_sn,
                     (void*)items, (void*)sitems, (void*)dest, (void*)conj})

@@ -60,6 +60,7 @@ struct DevSymbolic {
     double flops = 0.0;        // real flops of one complex factorisation (4 sum c_j^2)
     size_t bytes = 0;
     cudaStream_t alloc_stream = nullptr;   // stream the device arrays were allocated on
+    ByteCount* cnt = nullptr;              // the owning context's byte count
     struct Step {
         int32_t level = 0, kb = 0;
         int64_t uzero_off = 0;                 // (s) items whose update blocks are zeroed

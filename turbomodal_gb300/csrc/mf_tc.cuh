@@ -13,7 +13,8 @@ namespace tmg {
 struct TcWork {
     void* stg = nullptr;         // 6 BF16 planes x B problems x 2 tc_rows real rows x 256 entries
     int* err = nullptr;          // nonzero: a bounded wait of k_update_tc expired
-    int64_t rows = 0;
+    int64_t rows = 0, bytes = 0;
+    ByteCount* cnt = nullptr;
     cudaStream_t stream = nullptr;
     alignas(64) unsigned char map[128];
     void release();

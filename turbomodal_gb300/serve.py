@@ -1,27 +1,34 @@
 """Served request stream: concurrent cyclic modal solves on one GPU, admitted by a
-device-memory budget.
+device-memory budget, with requests on the same sector batched together.
 
-Every request (sector mesh, material, speed, modes, harmonic subset, precision) runs in its
-own device context, which owns a non-blocking CUDA stream, its factors and its Lanczos bases
-for the life of the request.  Worker threads take requests in arrival order; a request first
-builds its operators (assembly, prestress, projections, symbolic analysis), then asks the
-server for the device memory its factorisation batch needs and waits until that much of the
-budget is free, so requests that arrive while others are on the GPU are admitted as memory
-frees up and their kernels overlap on the device.
+Every request (sector mesh, material, speed, modes, harmonic subset, precision) runs on a
+device context, which owns a non-blocking CUDA stream, its factors and its Lanczos bases.
+Worker threads take requests in arrival order.  A worker that takes a request also takes every
+queued request on the same sector and precision (continuous batching: requests that arrived
+while the GPU was busy join the next batch) and solves them as one batched sweep
+(solve_rpm_sweep: the harmonics of all their speeds factorised and iterated together), with the
+union of their harmonic subsets and the largest mode count; each request then gets its own
+harmonics and its own number of modes from the batch.
+
+Admission by budget covers every device byte a request holds: before its context builds
+anything, the request reserves an estimate of the sector set-up (assembly, prestress,
+projections, symbolic analyses; bytes per node learnt from earlier contexts), trued up to the
+context's own count (tmg_device_bytes) once the set-up is done; then it reserves its
+factorisation batch.  Requests wait until that much of the budget is free.
 
 Contexts outlive their requests: an idle context is kept per sector (mesh, boundary data and
 material, by content), and a later request on the same sector takes it over with its
-assembled sector matrices, structural operator patterns and symbolic analyses, so only the
-speed-dependent work runs again.  At most `max_cached` idle contexts are kept (least recently
-used evicted).  The reference solves one request at a time on the CPU
-(python/turbomodal/solver.py:237-375); this layer has no counterpart there.
+assembled sector matrices, structural operator patterns and symbolic analyses.  Idle contexts
+stay counted against the budget; when a request cannot be admitted, idle contexts are closed,
+least recently used first, before it waits.  The reference solves one request at a time on the
+CPU (python/turbomodal/solver.py:237-375); this layer has no counterpart there.
 """
 
 from __future__ import annotations
 
+import copy
 import hashlib
 import math
-import queue
 import threading
 import time
 from collections import OrderedDict
@@ -56,6 +63,7 @@ class Completed:
     grant_bytes: int = 0
     error: str = ""
     reused: bool = False           # ran on a context kept from an earlier request
+    batched: int = 1               # requests solved in the same batched sweep
 
     @property
     def latency(self) -> float:
@@ -95,124 +103,195 @@ def sector_key(mesh, material, apply_hub_constraint: bool = True) -> str:
 
 
 class ModalServer:
-    """Concurrent request loop with admission by device-memory budget and reuse of a sector's
-    context across requests."""
+    """Concurrent request loop with admission by device-memory budget, batching of queued
+    requests on the same sector, and reuse of a sector's context across requests."""
 
     def __init__(self, device: int = 0, budget_bytes: int = 150 << 30, max_inflight: int = 4,
-                 max_cached: int = 8, solver_factory=None):
+                 max_cached: int = 8, solver_factory=None, max_batch: int = 8):
         self.device = device
         self.budget = int(budget_bytes)
         self.max_inflight = max_inflight
         self.max_cached = max_cached
+        self.max_batch = max_batch
         self._factory = solver_factory or (lambda mesh, material, precision: CyclicSymmetrySolver(
             mesh, material, device=device, precision=precision, mem_budget_bytes=self.budget))
-        self._used = 0
+        self._used = 0                      # active grants + bytes of idle contexts
         self._cv = threading.Condition()
-        self._idle: OrderedDict = OrderedDict()   # sector key -> idle contexts, least recently used first
-        self._pool_lock = threading.Lock()
+        self._idle: OrderedDict = OrderedDict()   # sector key -> [(solver, bytes)], least recently used first
+        self.bytes_per_node = 60 << 10      # set-up estimate, raised to what contexts report
 
     # -- context reuse ------------------------------------------------------------------
-    def _checkout(self, key: str, mesh, material, precision: str):
-        """An idle context of this sector (reused = True) or a new one."""
-        with self._pool_lock:
+    def _checkout(self, key: str):
+        """An idle context of this sector and the bytes it holds (still counted), or None."""
+        with self._cv:
             lst = self._idle.get(key)
             if lst:
-                solver = lst.pop()
+                solver, held = lst.pop()
                 if not lst:
                     del self._idle[key]
-                return solver, True
-        return self._factory(mesh, material, precision), False
+                return solver, held
+        return None, 0
 
-    def _checkin(self, key: str, solver) -> None:
-        """Keep an idle context; the least recently used ones beyond max_cached are closed."""
+    def _checkin(self, key: str, solver, held: int) -> None:
+        """Keep an idle context (its bytes stay counted); beyond max_cached the least recently
+        used ones are closed."""
         evicted = []
-        with self._pool_lock:
-            self._idle.setdefault(key, []).append(solver)
+        with self._cv:
+            self._idle.setdefault(key, []).append((solver, held))
             self._idle.move_to_end(key)
             while sum(len(v) for v in self._idle.values()) > self.max_cached:
-                k0, lst = next(iter(self._idle.items()))
-                evicted.append(lst.pop(0))
-                if not lst:
-                    del self._idle[k0]
-        for s in evicted:
-            s.close()
+                evicted.append(self._pop_lru())
+        self._close(evicted)
+
+    def _pop_lru(self):
+        k0, lst = next(iter(self._idle.items()))
+        item = lst.pop(0)
+        if not lst:
+            del self._idle[k0]
+        return item
+
+    def _close(self, items) -> None:
+        for solver, held in items:
+            solver.close()
+            with self._cv:
+                self._used -= held
+                self._cv.notify_all()
 
     def cached_contexts(self) -> int:
-        with self._pool_lock:
+        with self._cv:
             return sum(len(v) for v in self._idle.values())
 
     def close(self) -> None:
         """Release every idle context."""
-        with self._pool_lock:
-            items = [s for lst in self._idle.values() for s in lst]
+        with self._cv:
+            items = [it for lst in self._idle.values() for it in lst]
             self._idle.clear()
-        for s in items:
-            s.close()
+        self._close(items)
 
     # -- memory admission ------------------------------------------------------------
     def _acquire(self, need: int) -> int:
-        need = min(need, self.budget)
-        with self._cv:
-            while self._used + need > self.budget:
-                self._cv.wait()
-            self._used += need
-        return need
+        """Reserve `need` bytes (at most the budget); idle contexts are closed, least recently
+        used first, while the reservation does not fit; then wait for active ones."""
+        need = max(0, min(int(need), self.budget))
+        while True:
+            victim = None
+            with self._cv:
+                if self._used + need <= self.budget:
+                    self._used += need
+                    return need
+                if self._idle:
+                    victim = self._pop_lru()
+                else:
+                    self._cv.wait()
+                    continue
+            self._close([victim])
 
     def _release(self, grant: int) -> None:
         with self._cv:
             self._used -= grant
             self._cv.notify_all()
 
-    # -- one request ------------------------------------------------------------------
-    def _run(self, req: Request, t0: float) -> Completed:
-        out = Completed(req.rid, arrival=req.arrival, start=time.perf_counter() - t0)
+    def _resize(self, grant: int, need: int) -> int:
+        """Adjust a reservation to `need` bytes (waits if it grows)."""
+        if need > grant:
+            return grant + self._acquire(need - grant)
+        self._release(grant - need)
+        return need
+
+    # -- one batch of requests on the same sector ---------------------------------------
+    def _run(self, group: list, t0: float) -> list:
+        outs = [Completed(r.rid, arrival=r.arrival, start=time.perf_counter() - t0) for r in group]
+        req = group[0]
         solver = None
-        grant = 0
+        setup = grant = 0
         key = sector_key(req.mesh, req.material)
         ok = False
         try:
-            solver, out.reused = self._checkout(key, req.mesh, req.material, req.precision)
+            solver, setup = self._checkout(key)
+            reused = solver is not None
+            if not reused:   # reserve the set-up before the context allocates anything
+                setup = self._acquire(self.bytes_per_node * req.mesh.num_nodes())
+                solver = self._factory(req.mesh, req.material, req.precision)
+            for o in outs:
+                o.reused = reused
             solver.set_memory_budget(self.budget)
             solver.prepare(req.rpm)
-            ks = list(req.harmonics) or list(range(req.mesh.num_sectors // 2 + 1))
+            cur, _ = solver.device_bytes()
+            self.bytes_per_node = max(self.bytes_per_node, int(1.1 * cur / max(1, req.mesh.num_nodes())))
+            setup = self._resize(setup, cur)
+            full = list(range(req.mesh.num_sectors // 2 + 1))
+            ks = sorted({k for r in group for k in (r.harmonics or full)})
+            nm = max(r.num_modes for r in group)
             n_cplx = sum(1 for k in ks if 0 < k and 2 * k != req.mesh.num_sectors)
-            need = batch_bytes(solver.symbolic_stats(0), req.num_modes, max(n_cplx, 2), req.precision)
+            need = batch_bytes(solver.symbolic_stats(0), nm, max(n_cplx, 2) * len(group), req.precision)
             grant = self._acquire(need)
-            out.admitted = time.perf_counter() - t0
-            out.grant_bytes = grant
+            adm = time.perf_counter() - t0
+            for o in outs:
+                o.admitted = adm
+                o.grant_bytes = grant
             solver.set_memory_budget(grant)
-            out.results = solver.solve_at_rpm(req.rpm, req.num_modes, ks, precision=req.precision)
+            sweep = solver.solve_rpm_sweep([r.rpm for r in group], nm, ks, precision=req.precision)
+            for r, o, res in zip(group, outs, sweep):
+                mine = set(r.harmonics or full)
+                o.results = [_first_modes(x, r.num_modes) for x in res if x.harmonic_index in mine]
+                o.batched = len(group)
             ok = True
-        except Exception as e:  # a failed request is reported, the stream goes on
-            out.error = f"{type(e).__name__}: {e}"
+        except Exception as e:  # a failed batch is reported, the stream goes on
+            for o in outs:
+                o.error = f"{type(e).__name__}: {e}"
         finally:
             if grant:
                 self._release(grant)
             if solver is not None:
                 if ok:
-                    self._checkin(key, solver)
+                    cur, _ = solver.device_bytes()
+                    setup = self._resize(setup, cur)   # the idle context's bytes stay counted
+                    self._checkin(key, solver, setup)
                 else:   # a context that failed mid-request is not kept
-                    solver.close()
-            out.done = time.perf_counter() - t0
-        return out
+                    self._close([(solver, setup)])
+            elif setup:
+                self._release(setup)
+            done = time.perf_counter() - t0
+            for o in outs:
+                o.done = done
+        return outs
 
     # -- the stream -------------------------------------------------------------------
     def serve(self, requests: list) -> list:
         """Replay `requests` at their arrival times; return one Completed per request."""
         reqs = sorted(requests, key=lambda r: r.arrival)
-        q: queue.Queue = queue.Queue()
+        pending: list = []
+        cv = threading.Condition()
+        finished = [False]
         done: list = []
-        lock = threading.Lock()
         t0 = time.perf_counter()
+
+        def take():
+            """The oldest queued request and the queued requests on its sector and precision."""
+            with cv:
+                while not pending and not finished[0]:
+                    cv.wait()
+                if not pending:
+                    return None
+                first = pending.pop(0)
+                key = (sector_key(first.mesh, first.material), first.precision)
+                group, rest = [first], []
+                for r in pending:
+                    if len(group) < self.max_batch and (sector_key(r.mesh, r.material), r.precision) == key:
+                        group.append(r)
+                    else:
+                        rest.append(r)
+                pending[:] = rest
+                return group
 
         def worker():
             while True:
-                r = q.get()
-                if r is None:
+                g = take()
+                if g is None:
                     return
-                c = self._run(r, t0)
-                with lock:
-                    done.append(c)
+                outs = self._run(g, t0)
+                with cv:
+                    done.extend(outs)
 
         ws = [threading.Thread(target=worker, daemon=True) for _ in range(self.max_inflight)]
         for w in ws:
@@ -221,12 +300,29 @@ class ModalServer:
             dt = r.arrival - (time.perf_counter() - t0)
             if dt > 0:
                 time.sleep(dt)
-            q.put(r)
-        for _ in ws:
-            q.put(None)
+            with cv:
+                pending.append(r)
+                cv.notify()
+        with cv:
+            finished[0] = True
+            cv.notify_all()
         for w in ws:
             w.join()
         return sorted(done, key=lambda c: c.rid)
+
+
+def _first_modes(r, m: int):
+    """The result with its first m modes (a batch ran with the largest mode count of its
+    requests; the reference truncates to the requested count the same way,
+    src/cyclic_solver.cpp:1058-1211)."""
+    if len(r.frequencies) <= m:
+        return r
+    out = copy.copy(r)
+    out.frequencies = r.frequencies[:m]
+    out.mode_shapes = r.mode_shapes[:, :m]
+    out.whirl_direction = r.whirl_direction[:m]
+    out.modal_mass_kg = r.modal_mass_kg[:m]
+    return out
 
 
 def request_stream(n: int, seed: int, rate_hz: float = 20.0, min_nodes: int = 2000, max_nodes: int = 200000,
@@ -272,4 +368,5 @@ def latency_summary(done: list) -> dict:
     return {"requests": len(done), "failed": len(done) - len(ok), "p50_s": float(np.percentile(lat, 50)),
             "p99_s": float(np.percentile(lat, 99)), "eigenpairs": pairs,
             "eigenpairs_per_s": pairs / span if span > 0 else 0.0, "makespan_s": span,
-            "reused_contexts": sum(1 for c in done if c.reused)}
+            "reused_contexts": sum(1 for c in done if c.reused),
+            "batched_requests": sum(1 for c in done if c.batched > 1)}

@@ -122,6 +122,15 @@ class CyclicSymmetrySolver:
         complex FP32 factorisation, the default)."""
         self.ctx.check(self.ctx.L.tmg_set_option(self.ctx.h, _lib.OPT[name], float(value)), "tmg_set_option")
 
+    def device_bytes(self) -> tuple[int, int]:
+        """(current, peak) device bytes of this solver's context (tmg_device_bytes)."""
+        cur, peak = C.c_int64(), C.c_int64()
+        self.ctx.check(self.ctx.L.tmg_device_bytes(self.ctx.h, C.byref(cur), C.byref(peak)), "tmg_device_bytes")
+        return cur.value, peak.value
+
+    def reset_peak_bytes(self) -> None:
+        self.ctx.check(self.ctx.L.tmg_reset_peak_bytes(self.ctx.h), "tmg_reset_peak_bytes")
+
     def tuning_report(self) -> list[dict]:
         """Trials of the last supernode-shape tuning (set_option("autotune", 1))."""
         rows = C.c_int()
