@@ -12,7 +12,11 @@
 // hold the 24 of an FP32 value): A B^T ~ sum over the pieces of order below 2^-16,
 //     A1 B1 + A1 B2 + A2 B1 + A1 B3 + A3 B1 + A2 B2,
 // six kind::f16 products with exact BF16 x BF16 terms and FP32 accumulation.  The dropped terms
-// are below 2^-23 of |A||B|, the rounding level of the FP32 SIMT update they replace.
+// are below 2^-23 of |A||B|, the rounding level of the FP32 SIMT update they replace.  The
+// tensor core's accumulation rounds every partial sum, so the terms go to three TMEM
+// accumulators summed in FP32 by the epilogue: the leading product A1 B1 of even and of odd
+// 64-wide K chunks in two of them (each sees half the K steps), the five smaller products in
+// the third (their rounding then scales with their own size, 2^-8 of the leading one).
 //
 // k_stage_tc writes, once per super-block and front, the rows [kend, m) of the six operand
 // planes (A1, A2, A3, B1, B2, B3) K-major (256 BF16 per real row) into a staging tensor.
@@ -46,7 +50,8 @@ constexpr int TC_ROWS = 128;                       // real rows per operand tile
 constexpr int TC_TILE_BYTES = TC_ROWS * TC_BOX_K * 2;   // 16 KB
 constexpr int TC_STAGE_BYTES = TC_PLANES * TC_TILE_BYTES;
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /* alignment slack */ + 256 /* barriers */;
-constexpr int TC_TMEM_COLS = 128;
+constexpr int TC_ACC_COLS = 128;                   // f32 columns of one 128x128 accumulator
+constexpr int TC_TMEM_COLS = 512;                  // three accumulators (power of two)
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;      // ~1 s at 2 GHz
 
 // instruction descriptor of tcgen05.mma kind::f16: D F32, A/B BF16, both K-major, M = 128, N = 128
@@ -265,13 +270,14 @@ __global__ void __launch_bounds__(128, 1) k_update_tc(const int32_t* __restrict_
                 const uint64_t b1 = smem_desc(sb + 3 * TC_TILE_BYTES + off);
                 const uint64_t b2 = smem_desc(sb + 4 * TC_TILE_BYTES + off);
                 const uint64_t b3 = smem_desc(sb + 5 * TC_TILE_BYTES + off);
-                // the smaller terms first
-                mma_bf16(tmem, a2, b2, (kc > 0 || ks > 0) ? 1u : 0u);
-                mma_bf16(tmem, a1, b3, 1u);
-                mma_bf16(tmem, a3, b1, 1u);
-                mma_bf16(tmem, a1, b2, 1u);
-                mma_bf16(tmem, a2, b1, 1u);
-                mma_bf16(tmem, a1, b1, 1u);
+                const uint32_t big = tmem + (uint32_t)((kc & 1) * TC_ACC_COLS);   // A1 B1, by K chunk parity
+                const uint32_t small = tmem + 2u * TC_ACC_COLS;                   // the five smaller terms
+                mma_bf16(small, a2, b2, (kc > 0 || ks > 0) ? 1u : 0u);
+                mma_bf16(small, a1, b3, 1u);
+                mma_bf16(small, a3, b1, 1u);
+                mma_bf16(small, a1, b2, 1u);
+                mma_bf16(small, a2, b1, 1u);
+                mma_bf16(big, a1, b1, (kc > 1 || ks > 0) ? 1u : 0u);
             }
             mma_commit(empty(st));   // this stage's smem may be refilled once these MMAs are done
         }
@@ -290,24 +296,30 @@ __global__ void __launch_bounds__(128, 1) k_update_tc(const int32_t* __restrict_
     const int64_t i = i0 + (r >> 1);
     const bool odd = lane & 1;
 #pragma unroll 1
-    for (int c0 = 0; c0 < 128; c0 += 32) {
-        uint32_t v[32];
-        const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-            "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-              "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-              "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    for (int c0 = 0; c0 < TC_ACC_COLS; c0 += 32) {
         float own[32], other[32];
 #pragma unroll
-        for (int q = 0; q < 32; q++) {
-            own[q] = __uint_as_float(v[q]);
-            other[q] = __shfl_xor_sync(0xffffffffu, own[q], 1);
+        for (int q = 0; q < 32; q++) own[q] = 0.f;
+        // accumulator 2 (smaller terms), then 0 and 1 (leading product; 1 only with a second K chunk)
+        for (int a = 2; a >= 0; a--) {
+            if (a == 1 && nK < 2) continue;
+            uint32_t v[32];
+            const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(a * TC_ACC_COLS + c0);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 32; q++) own[q] += __uint_as_float(v[q]);
         }
+#pragma unroll
+        for (int q = 0; q < 32; q++) other[q] = __shfl_xor_sync(0xffffffffu, own[q], 1);
         if (!write) continue;
         // the even lane of a pair takes complex columns 0..7 of this chunk, the odd lane 8..15
 #pragma unroll
