@@ -107,8 +107,10 @@ int tmg_set_memory_budget(tmg_context* ctx, size_t mem_budget_bytes);
  *   pattern (default 0).  Method change only: results equal the undeflated ones to the
  *   refinement tolerance.
  * TMG_OPT_TENSOR_CORES: 1 = the complex FP32 factorisation of the mixed path runs its large
- *   trailing Schur updates on the tensor cores (3xTF32, tcgen05); 0 = on the FP32 SIMT pipe
- *   (default 1).  Method change only, as above.
+ *   trailing Schur updates on the tensor cores (tcgen05, three-way BF16 split with FP32
+ *   accumulation); 0 = on the FP32 SIMT pipe (default 0: on the config-1 sector the tensor-core
+ *   factor took as long and its refined solves needed about a quarter more FP32 solves).
+ *   Method change only, as above.
  * TMG_OPT_AUTOTUNE: 1 = the first solve on a new complex operator pattern times candidate
  *   supernode shapes (relaxed amalgamation, front width cap, tensor-core row threshold) on its
  *   own operator values and keeps the fastest, cached per pattern for the process (default 0).

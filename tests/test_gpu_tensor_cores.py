@@ -1,4 +1,4 @@
-"""Tensor-core (tcgen05, 3xTF32) trailing Schur updates of the mixed path's complex FP32
+"""Tensor-core (tcgen05, three-way BF16 split) trailing Schur updates of the mixed path's complex FP32
 factorisation against the same factorisation on the FP32 SIMT pipe.
 
 Both factors only precondition the FP64-refined shift-invert solves, which stop at a 1e-10
@@ -30,9 +30,9 @@ def test_tensor_core_factor_matches_simt_factor(mesh_args):
 
     m = config_mesh(0) if "cfg" in mesh_args else scaled_mesh(mesh_args["nodes"], 36, seed=5)
     simt = CyclicSymmetrySolver(m, TITANIUM, precision="mixed")
-    simt.set_option("tensor_cores", 0)
-    tc = CyclicSymmetrySolver(m, TITANIUM, precision="mixed")
-    assert tc.get_option("tensor_cores") == 1.0
+        tc = CyclicSymmetrySolver(m, TITANIUM, precision="mixed")
+    assert tc.get_option("tensor_cores") == 0.0   # the SIMT updates are the default
+    tc.set_option("tensor_cores", 1)
     ks = [1, 2, 9, 17]
     a = {r.harmonic_index: r for r in simt.solve_at_rpm(9000.0, 10, harmonic_indices=ks)}
     ta = simt.last_timing()

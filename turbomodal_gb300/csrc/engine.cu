@@ -493,7 +493,7 @@ struct tmg_context {
     double solves_per_factor = 0.0;   // FP32 solves per factorisation seen in the last mixed batch
     std::string tuned_key;        // pattern the current complex analysis was tuned for
     double shift = 1.0;           // sigma of the standard path (cyclic_solver.cpp:1017)
-    bool tensor_cores = true;     // tcgen05 trailing updates in the complex FP32 factorisation
+    bool tensor_cores = false;    // tcgen05 trailing updates in the complex FP32 factorisation
     std::string recycle_key;
     std::map<int, DVec<zd>> recycle;
     struct Qep {

@@ -1,7 +1,9 @@
 """Fixed workloads for profiler captures of the GPU path.
 
-``python -m turbomodal_gb300.profiling <case> [reps]`` solves the complex harmonics of one
-sector at 10000 rpm in mixed precision ``reps`` times and prints the per-call timing.  Cases:
+``python -m turbomodal_gb300.profiling <case> [reps] [tensor_cores]`` solves the complex
+harmonics of one sector at 10000 rpm in mixed precision ``reps`` times and prints the per-call
+timing; ``tensor_cores`` (0 or 1) sets the factorisation's trailing-update path (default: the
+library's).  Cases:
 
 * ``medium``  — 11,305-node bladed sector (20x12x4 hub + 16x6x2 blade, 36 sectors, n = 32,160
   free DOF per harmonic, 17 complex harmonics in one batch): small enough for multi-pass
@@ -32,6 +34,8 @@ def main(argv: list[str]) -> None:
     reps = int(argv[1]) if len(argv) > 1 else 1
     mesh = case_mesh(name)
     solver = CyclicSymmetrySolver(mesh, TITANIUM)
+    if len(argv) > 2:
+        solver.set_option("tensor_cores", float(argv[2]))
     ks = list(range(1, mesh.num_sectors // 2))
     for r in range(reps):
         t = time.time()

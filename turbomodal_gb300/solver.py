@@ -119,7 +119,7 @@ class CyclicSymmetrySolver:
         """tmg_set_option: "shift" (sigma of the standard path, default 1.0 as the reference's
         src/cyclic_solver.cpp:1017), "deflate" (1 = deflate the mixed refinement CG with the
         previous speed's eigenvectors) or "tensor_cores" (1 = tcgen05 trailing updates in the
-        complex FP32 factorisation, the default)."""
+        complex FP32 factorisation; default 0, the SIMT updates)."""
         self.ctx.check(self.ctx.L.tmg_set_option(self.ctx.h, _lib.OPT[name], float(value)), "tmg_set_option")
 
     def device_bytes(self) -> tuple[int, int]:
