@@ -30,7 +30,7 @@ def test_tensor_core_factor_matches_simt_factor(mesh_args):
 
     m = config_mesh(0) if "cfg" in mesh_args else scaled_mesh(mesh_args["nodes"], 36, seed=5)
     simt = CyclicSymmetrySolver(m, TITANIUM, precision="mixed")
-        tc = CyclicSymmetrySolver(m, TITANIUM, precision="mixed")
+    tc = CyclicSymmetrySolver(m, TITANIUM, precision="mixed")
     assert tc.get_option("tensor_cores") == 0.0   # the SIMT updates are the default
     tc.set_option("tensor_cores", 1)
     ks = [1, 2, 9, 17]
