@@ -114,11 +114,15 @@ int tmg_set_memory_budget(tmg_context* ctx, size_t mem_budget_bytes);
  * TMG_OPT_AUTOTUNE: 1 = the first solve on a new complex operator pattern times candidate
  *   supernode shapes (relaxed amalgamation, front width cap, tensor-core row threshold) on its
  *   own operator values and keeps the fastest, cached per pattern for the process (default 0).
- *   tmg_tuning_report lists the trials. */
+ *   tmg_tuning_report lists the trials.
+ * TMG_OPT_REFINE_TOL: relative residual ||b - A x|| / ||b|| at which the FP64 refinement of a
+ *   mixed-precision shift-invert solve stops (default 1e-10, accepted range [1e-14, 1e-6]); a
+ *   problem whose refinement stalls above 100x the target is solved again in FP64. */
 #define TMG_OPT_SHIFT 0
 #define TMG_OPT_DEFLATE 1
 #define TMG_OPT_TENSOR_CORES 2
 #define TMG_OPT_AUTOTUNE 3
+#define TMG_OPT_REFINE_TOL 4
 int tmg_set_option(tmg_context* ctx, int option, double value);
 int tmg_get_option(tmg_context* ctx, int option, double* value);
 int tmg_destroy(tmg_context* ctx);

@@ -30,7 +30,7 @@ EXPORTED = ["tmg_create", "tmg_destroy", "tmg_last_error", "tmg_upload_sector", 
             "tmg_set_profiling", "tmg_profile_solve", "tmg_projection_harmonic_static", "tmg_set_memory_budget",
             "tmg_set_option", "tmg_get_option", "tmg_result_modal_mass", "tmg_solve_sweep", "tmg_tuning_report",
             "tmg_device_bytes", "tmg_reset_peak_bytes"]
-OPT = {"shift": 0, "deflate": 1, "tensor_cores": 2, "autotune": 3}
+OPT = {"shift": 0, "deflate": 1, "tensor_cores": 2, "autotune": 3, "refine_tol": 4}
 
 
 class SectorDesc(C.Structure):

@@ -494,6 +494,7 @@ struct tmg_context {
     std::string tuned_key;        // pattern the current complex analysis was tuned for
     double shift = 1.0;           // sigma of the standard path (cyclic_solver.cpp:1017)
     bool tensor_cores = false;    // tcgen05 trailing updates in the complex FP32 factorisation
+    double refine_tol = 1e-10;    // relative residual target of a refined (mixed) solve
     std::string recycle_key;
     std::map<int, DVec<zd>> recycle;
     struct Qep {
@@ -1794,6 +1795,7 @@ void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os
     A.nrows = um.U.ncols; A.nnz = nU; A.rowptr = um.csr_rowptr.p; A.col = um.csr_col.p; A.val = acsr.p; A.vstride = nU;
     ShiftInvertB<Tv, Tf> op;
     op.c = c; op.D = &os.D; op.um = &um; op.n = um.U.ncols; op.B = B; op.mixed = mixed; op.A = A;
+    op.rtol = c->refine_tol;
     auto t0 = std::chrono::steady_clock::now();
     op.factor(lower.p);
     lower.release();
@@ -2096,7 +2098,7 @@ std::vector<Problem> mixed_failures(tmg_context* c, const std::vector<Problem>& 
     std::vector<Problem> out;
     for (const Problem& pr : grp) {
         ResultHost& R = *pr.R;
-        if (R.status == TMG_ERR_NUMERIC || (R.status == TMG_OK && R.refine_residual > 1e-8)) {
+        if (R.status == TMG_ERR_NUMERIC || (R.status == TMG_OK && R.refine_residual > 100.0 * c->refine_tol)) {
             ResultHost fresh;
             fresh.k = R.k;
             fresh.rpm = R.rpm;
@@ -2710,6 +2712,10 @@ int tmg_set_option(tmg_context* c, int option, double value) {
         case TMG_OPT_AUTOTUNE:
             c->autotune = value != 0.0;
             return TMG_OK;
+        case TMG_OPT_REFINE_TOL:
+            if (!(value >= 1e-14 && value <= 1e-6)) return set_err(c, TMG_ERR_ARG, "refinement target outside [1e-14, 1e-6]");
+            c->refine_tol = value;
+            return TMG_OK;
         default:
             return set_err(c, TMG_ERR_ARG, "unknown option " + std::to_string(option));
     }
@@ -2722,6 +2728,7 @@ int tmg_get_option(tmg_context* c, int option, double* value) {
         case TMG_OPT_DEFLATE: *value = c->deflate ? 1.0 : 0.0; return TMG_OK;
         case TMG_OPT_TENSOR_CORES: *value = c->tensor_cores ? 1.0 : 0.0; return TMG_OK;
         case TMG_OPT_AUTOTUNE: *value = c->autotune ? 1.0 : 0.0; return TMG_OK;
+        case TMG_OPT_REFINE_TOL: *value = c->refine_tol; return TMG_OK;
         default: return set_err(c, TMG_ERR_ARG, "unknown option " + std::to_string(option));
     }
 }
