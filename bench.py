@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=16)
     ap.add_argument("--serve-max-nodes", type=int, default=200000,
                     help="largest sector of the request-stream sample")
+    ap.add_argument("--serve-deadline", type=float, default=180.0,
+                    help="no served batch starts later than this many seconds into the stream")
     ap.add_argument("--serve-designs", type=int, default=4,
                     help="distinct sector designs the requests draw from (repeats are batched and reuse contexts)")
     return ap.parse_args()
@@ -497,9 +499,10 @@ def main():
             reqs = request_stream(args.serve_requests, seed=2024, rate_hz=20.0, min_nodes=2000,
                                   max_nodes=args.serve_max_nodes, distinct_sectors=args.serve_designs)
             srv = ModalServer(device=local, budget_bytes=150 << 30, max_inflight=4)
-            done = srv.serve(reqs)
+            done = srv.serve(reqs, deadline_s=args.serve_deadline)
             srv.close()
             serving = latency_summary(done)
+            serving["deadline_s"] = args.serve_deadline
             sizes = sorted({r.mesh.num_nodes() for r in reqs})
             serving["sample"] = (f"{len(reqs)} requests, Poisson 20 req/s, drawn from {args.serve_designs} config-0/1-"
                                  f"style sector designs ({', '.join(str(n) for n in sizes)} nodes; log-uniform in "

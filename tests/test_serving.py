@@ -233,3 +233,44 @@ def test_same_sector_requests_are_batched():
         np.testing.assert_array_equal(c.results[0].frequencies,
                                       np.arange(1.0, r.num_modes + 1.0) * (c.results[0].harmonic_index + 1))
     assert done[0].batched == 3 and done[1].batched == 1
+
+
+def test_batch_grants_cannot_deadlock():
+    """Two requests that hold set-up reservations and then ask for their factorisation batches
+    (each wanting the whole rest of the budget) both proceed: a batch grant takes what is free
+    once one problem's worth is, and the engine sizes its batches to the grant."""
+    from turbomodal_gb300.serve import ModalServer
+
+    srv = ModalServer(budget_bytes=100)
+    a_setup, b_setup = srv._acquire(20), srv._acquire(20)
+    got = {}
+
+    def batch(name, setup):
+        g = srv._acquire_flexible(100 - setup, 10)
+        got[name] = g
+        time.sleep(0.02)
+        srv._release(g)
+
+    ts = [threading.Thread(target=batch, args=(n, 20)) for n in ("a", "b")]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join(timeout=5)
+    assert not any(t.is_alive() for t in ts)
+    assert sorted(got) == ["a", "b"] and all(10 <= g <= 60 for g in got.values())
+    srv._release(a_setup + b_setup)
+    assert srv._used == 0
+
+
+def test_serving_deadline_reports_unstarted_requests():
+    from turbomodal_gb300.meshgen import TITANIUM, sector_mesh
+    from turbomodal_gb300.serve import ModalServer, Request
+
+    _FakeSolver.made, _FakeSolver.closed = [], []
+    a = sector_mesh(4, 3, 1, num_sectors=24, seed=1)
+    b = sector_mesh(5, 3, 1, num_sectors=24, seed=2)
+    reqs = [Request(0, a, TITANIUM, 1000.0, 4, [1]), Request(1, b, TITANIUM, 1500.0, 5, [2], arrival=0.3)]
+    srv = ModalServer(budget_bytes=1 << 40, max_inflight=1, solver_factory=lambda m, mat, p: _FakeSolver())
+    done = srv.serve(reqs, deadline_s=0.1)
+    srv.close()
+    assert not done[0].error and done[1].error.startswith("not started")

@@ -186,6 +186,29 @@ class ModalServer:
                     continue
             self._close([victim])
 
+    def _acquire_flexible(self, want: int, minimum: int) -> int:
+        """Reserve up to `want` bytes, taking what is free once at least `minimum` is (idle contexts
+        are closed first, least recently used first).  A batch reservation is flexible because
+        the engine sizes its factorisation batches to the grant: two requests that each hold a
+        set-up reservation and wait for their batch can therefore never block each other while
+        the set-ups and one problem fit the budget."""
+        want = max(0, min(int(want), self.budget))
+        minimum = max(0, min(int(minimum), want))
+        while True:
+            victim = None
+            with self._cv:
+                free = self.budget - self._used
+                if free >= want or (free >= minimum and not self._idle):
+                    g = max(minimum, min(want, free))
+                    self._used += g
+                    return g
+                if self._idle:
+                    victim = self._pop_lru()
+                else:
+                    self._cv.wait()
+                    continue
+            self._close([victim])
+
     def _release(self, grant: int) -> None:
         with self._cv:
             self._used -= grant
@@ -223,8 +246,9 @@ class ModalServer:
             ks = sorted({k for r in group for k in (r.harmonics or full)})
             nm = max(r.num_modes for r in group)
             n_cplx = sum(1 for k in ks if 0 < k and 2 * k != req.mesh.num_sectors)
-            need = batch_bytes(solver.symbolic_stats(0), nm, max(n_cplx, 2) * len(group), req.precision)
-            grant = self._acquire(need)
+            stats = solver.symbolic_stats(0)
+            need = batch_bytes(stats, nm, max(n_cplx, 2) * len(group), req.precision)
+            grant = self._acquire_flexible(min(need, self.budget - setup), batch_bytes(stats, nm, 1, req.precision))
             adm = time.perf_counter() - t0
             for o in outs:
                 o.admitted = adm
@@ -257,8 +281,10 @@ class ModalServer:
         return outs
 
     # -- the stream -------------------------------------------------------------------
-    def serve(self, requests: list) -> list:
-        """Replay `requests` at their arrival times; return one Completed per request."""
+    def serve(self, requests: list, deadline_s: float | None = None) -> list:
+        """Replay `requests` at their arrival times; return one Completed per request.  With
+        `deadline_s`, no batch starts later than that many seconds after the start: requests
+        still queued then are returned with an error ("not started") and count as failed."""
         reqs = sorted(requests, key=lambda r: r.arrival)
         pending: list = []
         cv = threading.Condition()
@@ -272,6 +298,13 @@ class ModalServer:
                 while not pending and not finished[0]:
                     cv.wait()
                 if not pending:
+                    return None
+                if deadline_s is not None and time.perf_counter() - t0 > deadline_s:
+                    late = list(pending)
+                    pending.clear()
+                    now = time.perf_counter() - t0
+                    done.extend(Completed(r.rid, arrival=r.arrival, start=now, done=now,
+                                          error="not started: serving deadline passed") for r in late)
                     return None
                 first = pending.pop(0)
                 key = (sector_key(first.mesh, first.material), first.precision)
@@ -308,6 +341,9 @@ class ModalServer:
             cv.notify_all()
         for w in ws:
             w.join()
+        now = time.perf_counter() - t0
+        done.extend(Completed(r.rid, arrival=r.arrival, start=now, done=now, error="not started: serving deadline passed")
+                    for r in pending)
         return sorted(done, key=lambda c: c.rid)
 
 
