@@ -99,3 +99,25 @@ def test_device_modal_mass_matches_host_formula(cfg0_mesh, oracle):
         np.testing.assert_allclose(r.modal_mass_kg, host, rtol=1e-12)
     enriched = solve(cfg0_mesh, TITANIUM, 7000.0, 6, harmonic_indices=[2], verbose=0, precision="mixed", solver=s)
     np.testing.assert_allclose(enriched[0].modal_mass_kg, res[1].modal_mass_kg, rtol=1e-9)
+
+
+def test_interior_shift_mixed_refinement_converges(cfg0_mesh):
+    """A shift inside the spectrum (sigma = (2 pi 600 Hz)^2, several modes below it) makes K - sigma M
+    indefinite: the mixed path refines with restarted GMRES preconditioned by the FP32 factor.
+    Its frequencies equal the FP64 path's within 1e-6, every refined solve reaches its target and
+    no problem falls back to FP64."""
+    from turbomodal_gb300.meshgen import TITANIUM
+    from turbomodal_gb300.solver import CyclicSymmetrySolver
+
+    sigma = (2 * np.pi * 600.0) ** 2
+    mixed = CyclicSymmetrySolver(cfg0_mesh, TITANIUM, precision="mixed")
+    a = {r.harmonic_index: r for r in mixed.solve_at_rpm(8000.0, 6, [0, 1, 7, 18], shift=sigma)}
+    t = mixed.last_timing()
+    assert t["retried_fp64"] == 0, t
+    fp = CyclicSymmetrySolver(cfg0_mesh, TITANIUM, precision="fp64")
+    b = {r.harmonic_index: r for r in fp.solve_at_rpm(8000.0, 6, [0, 1, 7, 18], shift=sigma)}
+    assert sorted(a) == sorted(b) == [0, 1, 7, 18]
+    for k in a:
+        assert a[k].refine_residual <= 1e-10
+        assert len(a[k].frequencies) == len(b[k].frequencies)
+        assert np.max(np.abs(a[k].frequencies - b[k].frequencies) / b[k].frequencies) <= FREQ_TOL

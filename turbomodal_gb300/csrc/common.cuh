@@ -123,4 +123,22 @@ template <> HD zd conv<zd, zf>(zf a) { return zd{(double)a.x, (double)a.y}; }
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// Stream-ordered allocation from the device's default pool.  The pool keeps freed blocks (its
+// release threshold is unlimited), so a large request can fail while the pool holds enough
+// memory in smaller free blocks: on an out-of-memory error the stream is synchronised, the pool
+// returns its unused memory to the device, and the allocation is tried once more.
+inline cudaError_t pool_malloc(void** p, size_t bytes, cudaStream_t st) {
+    cudaError_t e = cudaMallocAsync(p, bytes, st);
+    if (e != cudaErrorMemoryAllocation) return e;
+    (void)cudaGetLastError();
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess || cudaMemPoolTrimTo(pool, 0) != cudaSuccess)
+        return e;
+    e = cudaMallocAsync(p, bytes, st);
+    if (e != cudaSuccess) (void)cudaGetLastError();
+    return e;
+}
+
 }  // namespace tmg

@@ -1205,6 +1205,16 @@ __global__ void k_ir_update(int64_t n, T* __restrict__ x, const T* __restrict__ 
 }
 
 // y[p] = sgn * Einv[p] h[p] for the m x m (column-major) matrix of every problem (deflation)
+// dst[p] = inv[p] * src[p] (per-problem scalar)
+template <typename T>
+__global__ void k_scale_into(int64_t n, const double* __restrict__ inv, const T* __restrict__ src, int64_t ss,
+                             T* __restrict__ dst, int64_t ds) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t p = blockIdx.y;
+    if (i >= n) return;
+    dst[p * ds + i] = inv[p] * src[p * ss + i];
+}
+
 template <typename T>
 __global__ void k_small_mv(int m, const T* __restrict__ Einv, const T* __restrict__ h, T* __restrict__ y, double sgn) {
     const int64_t p = blockIdx.x;
@@ -1250,6 +1260,12 @@ struct ShiftInvertB {
     // (mdef x mdef, column-major).
     int mdef = 0;
     DVec<Tv> W, AW, Einv, hdef, ydef, pdef;
+    // restarted GMRES of the indefinite case: GM Krylov vectors per cycle, V ((GM+1) x n per
+    // problem), preconditioned directions Z (GM x n per problem)
+    static constexpr int GM = 16;
+    int gmres_cycles = 4;
+    DVec<Tv> GV, GZ, gh, gpart, gy;
+    DVec<double> ginv;
     cudaGraphExec_t gexec = nullptr;
     int64_t launches_per_solve = 0;
     ~ShiftInvertB() { if (gexec) cudaGraphExecDestroy(gexec); }
@@ -1415,6 +1431,132 @@ struct ShiftInvertB {
         TMG_CUDA(cudaStreamSynchronize(c->st));
         return h;
     }
+    // Restarted GMRES on A x = b, right-preconditioned by the FP32 factor (z = F^-1 v), FP64
+    // Arnoldi with two classical Gram-Schmidt passes and complex Givens rotations on the host, per
+    // problem.  Used when some pivot is negative (indefinite or strongly shifted operators), where
+    // plain refinement x += F^-1 (b - A x) stalls as soon as the factor's error is not a
+    // contraction; GMRES converges whenever the preconditioned operator's spectrum clusters with a
+    // few outliers.  Each cycle ends with the true FP64 residual.  Returns the inner iterations.
+    int gmres(const Tv* b, Tv* x, const std::vector<double>& bn, std::vector<int>& done, std::vector<double>& rn) {
+        using cplx = std::complex<double>;
+        cudaStream_t st = c->st;
+        const int64_t vs = (int64_t)(GM + 1) * n, zs = (int64_t)GM * n;
+        if (!GV.p) {
+            GV.alloc((size_t)B * vs);
+            GZ.alloc((size_t)B * zs);
+            gh.alloc((size_t)B * (GM + 1));
+            gpart.alloc((size_t)B * (GM + 1) * LZ_DOT_BLOCKS);
+            gy.alloc((size_t)B * GM);
+            ginv.alloc(B);
+        }
+        TMG_CUDA(cudaMemsetAsync(x, 0, (size_t)B * n * sizeof(Tv), st));
+        lz_copy<Tv>(st, (int64_t)B * n, b, r.p);
+        std::vector<cplx> H((size_t)B * (GM + 1) * GM), cs((size_t)B * GM), sn((size_t)B * GM), g((size_t)B * (GM + 1));
+        std::vector<double> inv(B), est(B);
+        std::vector<Tv> hv((size_t)B * (GM + 1)), yv((size_t)B * GM);
+        auto Hat = [&](int p, int i, int j) -> cplx& { return H[((size_t)p * GM + j) * (GM + 1) + i]; };
+        auto scale_into = [&](const Tv* src, int64_t ss, Tv* dst, int64_t ds) {
+            TMG_CUDA(cudaMemcpyAsync(ginv.p, inv.data(), B * sizeof(double), cudaMemcpyHostToDevice, st));
+            TMG_LAUNCH(k_scale_into<Tv>, dim3(nblk(n), B), 256, 0, st, (int64_t)n, ginv.p, src, ss, dst, ds);
+            TMG_CUDA(cudaStreamSynchronize(st));   // inv is a host vector reused by the next call
+        };
+        int total = 0;
+        for (int cycle = 0; cycle < gmres_cycles; cycle++) {
+            rn = norms(r.p);
+            bool all = true;
+            for (int p = 0; p < B; p++) {
+                if (!done[p] && rn[p] <= rtol * rtol * bn[p]) done[p] = 1;
+                all = all && done[p];
+            }
+            TMG_CUDA(cudaMemcpyAsync(ddone.p, done.data(), B * sizeof(int), cudaMemcpyHostToDevice, st));
+            if (all) break;
+            std::fill(H.begin(), H.end(), cplx(0.0));
+            std::fill(g.begin(), g.end(), cplx(0.0));
+            for (int p = 0; p < B; p++) {
+                const double beta = std::sqrt(rn[p]);
+                inv[p] = (!done[p] && beta > 0.0) ? 1.0 / beta : 0.0;
+                g[(size_t)p * (GM + 1)] = beta;
+            }
+            scale_into(r.p, n, GV.p, vs);                      // v_0 = r / ||r||
+            int jj = 0;
+            for (int j = 0; j < GM; j++) {
+                // z_j = F^-1 v_j, w = A z_j (w in z)
+                TMG_CUDA(cudaMemcpy2DAsync(d.p, n * sizeof(Tv), GV.p + (int64_t)j * n, vs * sizeof(Tv), n * sizeof(Tv), B,
+                                           cudaMemcpyDeviceToDevice, st));
+                solve1(d.p, q.p);
+                TMG_CUDA(cudaMemcpy2DAsync(GZ.p + (int64_t)j * n, zs * sizeof(Tv), q.p, n * sizeof(Tv), n * sizeof(Tv), B,
+                                           cudaMemcpyDeviceToDevice, st));
+                lz_spmv<Tv>(st, B, A, q.p, n, z.p, n, 1, n);
+                for (int pass = 0; pass < 2; pass++) {
+                    lz_multidot<Tv>(st, B, n, GV.p, vs, n, j + 1, z.p, n, gpart.p, gh.p);
+                    lz_gemv_sub<Tv>(st, B, n, j + 1, GV.p, vs, gh.p, j + 1, z.p, n);
+                    TMG_CUDA(cudaMemcpyAsync(hv.data(), gh.p, (size_t)B * (j + 1) * sizeof(Tv), cudaMemcpyDeviceToHost, st));
+                    TMG_CUDA(cudaStreamSynchronize(st));
+                    for (int p = 0; p < B; p++)
+                        for (int k = 0; k <= j; k++) Hat(p, k, j) += to_std(hv[(size_t)p * (j + 1) + k]);
+                }
+                const std::vector<double> hn = norms(z.p);
+                for (int p = 0; p < B; p++) {
+                    const double h = std::sqrt(hn[p]);
+                    Hat(p, j + 1, j) = h;
+                    inv[p] = (!done[p] && h > 0.0) ? 1.0 / h : 0.0;
+                }
+                scale_into(z.p, n, GV.p + (int64_t)(j + 1) * n, vs);   // v_{j+1}
+                bool conv = true;
+                for (int p = 0; p < B; p++) {
+                    if (done[p]) continue;
+                    cplx* gp = g.data() + (size_t)p * (GM + 1);
+                    for (int i = 0; i < j; i++) {   // earlier rotations on the new column
+                        const cplx ci = cs[(size_t)p * GM + i], si = sn[(size_t)p * GM + i];
+                        const cplx t = ci * Hat(p, i, j) + si * Hat(p, i + 1, j);
+                        Hat(p, i + 1, j) = -std::conj(si) * Hat(p, i, j) + ci * Hat(p, i + 1, j);
+                        Hat(p, i, j) = t;
+                    }
+                    const cplx a = Hat(p, j, j), bb = Hat(p, j + 1, j);
+                    const double rho = std::hypot(std::abs(a), std::abs(bb));
+                    cplx ci, si;
+                    if (rho == 0.0) { ci = 1.0; si = 0.0; }
+                    else if (std::abs(a) == 0.0) { ci = 0.0; si = std::conj(bb) / std::abs(bb); }
+                    else { ci = std::abs(a) / rho; si = (a / std::abs(a)) * std::conj(bb) / rho; }
+                    cs[(size_t)p * GM + j] = ci;
+                    sn[(size_t)p * GM + j] = si;
+                    Hat(p, j, j) = ci * a + si * bb;
+                    Hat(p, j + 1, j) = 0.0;
+                    gp[j + 1] = -std::conj(si) * gp[j];
+                    gp[j] = ci * gp[j];
+                    est[p] = std::abs(gp[j + 1]);
+                    if (est[p] > 0.5 * rtol * std::sqrt(bn[p])) conv = false;
+                }
+                jj = j + 1;
+                total++;
+                if (conv) break;
+            }
+            // x += Z y with H y = g (back substitution per problem; converged problems add nothing)
+            std::fill(yv.begin(), yv.end(), from_std<Tv>(cplx(0.0)));
+            for (int p = 0; p < B; p++) {
+                if (done[p]) continue;
+                std::vector<cplx> y(jj);
+                const cplx* gp = g.data() + (size_t)p * (GM + 1);
+                for (int i = jj - 1; i >= 0; i--) {
+                    cplx acc = gp[i];
+                    for (int k = i + 1; k < jj; k++) acc -= Hat(p, i, k) * y[k];
+                    const cplx dgl = Hat(p, i, i);
+                    y[i] = std::abs(dgl) > 0.0 ? acc / dgl : cplx(0.0);
+                }
+                for (int i = 0; i < jj; i++) yv[(size_t)p * jj + i] = from_std<Tv>(-y[i]);
+            }
+            TMG_CUDA(cudaMemcpyAsync(gy.p, yv.data(), (size_t)B * jj * sizeof(Tv), cudaMemcpyHostToDevice, st));
+            lz_gemv_sub<Tv>(st, B, n, jj, GZ.p, zs, gy.p, jj, x, n);
+            TMG_CUDA(cudaStreamSynchronize(st));
+            lz_copy<Tv>(st, (int64_t)B * n, b, r.p);
+            lz_spmv<Tv>(st, B, A, x, n, r.p, n, 1, n, true);
+        }
+        rn = norms(r.p);
+        for (int p = 0; p < B; p++)
+            if (!done[p] && rn[p] <= rtol * rtol * bn[p]) done[p] = 1;
+        return total;
+    }
+
     // x = (K - sigma M)^-1 b for every problem of the batch; problem p's right-hand side
     // starts at b + p * bs, its solution at x + p * n
     void apply(const Tv* b, int64_t bs, Tv* x) {
@@ -1472,15 +1614,7 @@ struct ShiftInvertB {
                 TMG_CUDA(cudaMemcpyAsync(sc.p, sc.p + 2 * B, B * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
             }
         } else {
-            // plain iterative refinement with the FP64 residual
-            solve1(b, x);
-            for (it = 1; it <= max_iter; it++) {
-                lz_copy<Tv>(c->st, (int64_t)B * n, b, r.p);
-                lz_spmv<Tv>(c->st, B, A, x, n, r.p, n, 1, n, true);
-                if (check()) break;
-                solve1(r.p, d.p);
-                TMG_LAUNCH(k_ir_update<Tv>, dim3(nblk(n), B), 256, 0, c->st, n, x, d.p, ddone.p);
-            }
+            it = gmres(b, x, bn, done, rn);
         }
         max_its = std::max<int64_t>(max_its, it);
         for (int p = 0; p < B; p++)
@@ -2282,6 +2416,10 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
                     } catch (const numeric_error& e) {
                         for (auto& pr : again) pr.R->status = TMG_ERR_NUMERIC;
                         c->err = e.what();
+                    } catch (const cuda_error& e) {   // the FP64 factor does not fit: these problems fail alone
+                        if (!std::strstr(e.what(), "out of memory")) throw;
+                        for (auto& pr : again) pr.R->status = TMG_ERR_NOMEM;
+                        c->err = std::string("FP64 retry of a mixed-path failure: ") + e.what();
                     }
                 }
             }
@@ -2371,6 +2509,10 @@ void solve_set(tmg_context* c, const std::vector<int>& ks, int num_modes, double
                     } catch (const numeric_error& e) {
                         for (auto& pr : again) pr.R->status = TMG_ERR_NUMERIC;
                         c->err = e.what();
+                    } catch (const cuda_error& e) {   // the FP64 factor does not fit: these problems fail alone
+                        if (!std::strstr(e.what(), "out of memory")) throw;
+                        for (auto& pr : again) pr.R->status = TMG_ERR_NOMEM;
+                        c->err = std::string("FP64 retry of a mixed-path failure: ") + e.what();
                     }
                 }
             }
@@ -2554,6 +2696,10 @@ void solve_sweep(tmg_context* c, const std::vector<double>& rpms, const std::vec
                     } catch (const numeric_error& e) {
                         for (auto& pr : again) pr.R->status = TMG_ERR_NUMERIC;
                         c->err = e.what();
+                    } catch (const cuda_error& e) {   // the FP64 factor does not fit: these problems fail alone
+                        if (!std::strstr(e.what(), "out of memory")) throw;
+                        for (auto& pr : again) pr.R->status = TMG_ERR_NOMEM;
+                        c->err = std::string("FP64 retry of a mixed-path failure: ") + e.what();
                     }
                 }
             }
@@ -2618,6 +2764,10 @@ void solve_sweep(tmg_context* c, const std::vector<double>& rpms, const std::vec
                     } catch (const numeric_error& e) {
                         for (auto& pr : again) pr.R->status = TMG_ERR_NUMERIC;
                         c->err = e.what();
+                    } catch (const cuda_error& e) {   // the FP64 factor does not fit: these problems fail alone
+                        if (!std::strstr(e.what(), "out of memory")) throw;
+                        for (auto& pr : again) pr.R->status = TMG_ERR_NOMEM;
+                        c->err = std::string("FP64 retry of a mixed-path failure: ") + e.what();
                     }
                 }
             }

@@ -42,7 +42,7 @@ struct DVec {
         n = count;
         s_ = g_stream;
         if (count) {
-            TMG_CUDA(cudaMallocAsync((void**)&p, count * sizeof(T), s_));
+            TMG_CUDA(pool_malloc((void**)&p, count * sizeof(T), s_));
             cnt_ = g_bytes;
             if (cnt_) cnt_->add((int64_t)(count * sizeof(T)));
         }

@@ -810,7 +810,7 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
     auto put = [&](auto*& dptr, const auto& vec) {
         using E = typename std::decay<decltype(vec[0])>::type;
         const size_t b = std::max<size_t>(1, vec.size()) * sizeof(E);
-        TMG_CUDA(cudaMallocAsync((void**)&dptr, b, alloc_stream));
+        TMG_CUDA(pool_malloc((void**)&dptr, b, alloc_stream));
         if (cnt) cnt->add((int64_t)b);
         if (!vec.empty())
             TMG_CUDA(cudaMemcpyAsync(dptr, vec.data(), vec.size() * sizeof(E), cudaMemcpyHostToDevice, alloc_stream));

@@ -379,12 +379,12 @@ void mf_trail_tc(cudaStream_t st, const DevSymbolic& S, const Batch<zf>& bt, con
     if (!wk.stg || wk.rows < TC_PLANES * plane_rows) {
         wk.release();
         const size_t bytes = (size_t)TC_PLANES * plane_rows * TC_KS * sizeof(__nv_bfloat16);
-        TMG_CUDA(cudaMallocAsync((void**)&wk.stg, bytes, st));
+        TMG_CUDA(pool_malloc((void**)&wk.stg, bytes, st));
         wk.bytes = (int64_t)bytes;
         wk.cnt = g_bytes;
         if (wk.cnt) wk.cnt->add(wk.bytes);
         TMG_CUDA(cudaMemsetAsync(wk.stg, 0, bytes, st));
-        TMG_CUDA(cudaMallocAsync((void**)&wk.err, sizeof(int), st));
+        TMG_CUDA(pool_malloc((void**)&wk.err, sizeof(int), st));
         TMG_CUDA(cudaMemsetAsync(wk.err, 0, sizeof(int), st));
         wk.rows = TC_PLANES * plane_rows;
         wk.stream = st;
