@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--wall-budget", type=float, default=1200.0,
                     help="seconds after start beyond which the optional legs (serving sample, CPU baseline) "
                          "are skipped")
+    ap.add_argument("--refine-tol", type=float, default=1e-8,
+                    help="relative residual target of the FP64 refinement of every mixed solve (frequencies are "
+                         "still verified against the FP64 path at 1e-6)")
     ap.add_argument("--sweep-group", type=int, default=2,
                     help="speeds per solve_rpm_sweep call (their harmonics are factorised and iterated as one batch)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -398,6 +401,7 @@ def main():
     my_rpms = shard_speeds(RPMS, rank, ws)
     # deflated refinement (previous speed's eigenvectors); SIMT trailing updates (the library default)
     solver = CyclicSymmetrySolver(mesh, TITANIUM, device=local, precision="mixed", deflate=True)
+    solver.set_option("refine_tol", args.refine_tol)
     order = list(my_rpms) * (1 + (args.warmup + args.steps) // max(1, len(my_rpms)))
     warm, timed = order[: args.warmup], order[args.warmup: args.warmup + args.steps]
     grp = max(1, args.sweep_group)
@@ -527,6 +531,7 @@ def main():
                        "harmonics": args.harmonics, "num_modes": args.num_modes,
                        "speeds": [float(r) for r in timed], "speeds_per_call": grp,
                        "deflated_refinement": True, "tensor_core_updates": bool(solver.get_option("tensor_cores")),
+                       "refine_tol": args.refine_tol,
                        "verified_speeds": [float(timed[i]) for i in vidx],
                        "parallelism": f"replicas x{ws} (speeds sharded)",
                        "l2": "inputs larger than L2 (no flush needed)"},
