@@ -3,8 +3,8 @@
 * the reference's free-hub diagnostic case (tests/test_validation.cpp:830-1022): the blade_sector
   fixture without the hub constraint, titanium, min_frequency 1 Hz, at 0 and 20000 rpm, both
   precisions, against the oracle: frequencies within 1e-6 relative, MAC >= 0.999.  Without the
-  hub constraint K - M is indefinite, so the mixed path refines with plain iterative refinement,
-  and solves that stall there are solved again in FP64 (the count is reported);
+  hub constraint K - M is indefinite, so the mixed path refines with restarted GMRES
+  preconditioned by the FP32 factor (a problem whose refinement stalls is solved again in FP64);
 * solve_parametric on the device equals solve_at_rpm per condition (src/cyclic_solver.cpp:1375-1485);
 * the shift option: sigma = 0 gives the frequencies of the reference's sigma = 1 within 1e-8.
 """
