@@ -59,3 +59,21 @@ def test_rpm_sweep_module_function_uses_the_batched_sweep(cfg0_mesh):
         for a, b in zip(res, ref):
             np.testing.assert_allclose(a.frequencies, b.frequencies, rtol=FREQ_TOL)
             assert np.all(a.modal_mass_kg > 0)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_returning_to_rest_reuses_the_kept_pattern_state(cfg0_mesh, precision):
+    """Rest and speed have different operator patterns; the context keeps the other regime's
+    unions and symbolic analyses, so a sweep that goes rest -> speed -> rest -> speed reuses them.
+    Every speed's result equals a fresh solver's within 1e-9."""
+    from turbomodal_gb300.meshgen import TITANIUM
+    from turbomodal_gb300.solver import CyclicSymmetrySolver
+
+    rpms = [0.0, 5000.0, 0.0, 9000.0]
+    s = CyclicSymmetrySolver(cfg0_mesh, TITANIUM, precision=precision)
+    seq = [s.solve_rpm_sweep([r], 5, [0, 2, 18])[0] for r in rpms]
+    for rpm, res in zip(rpms, seq):
+        fresh = CyclicSymmetrySolver(cfg0_mesh, TITANIUM, precision=precision).solve_at_rpm(rpm, 5, [0, 2, 18])
+        assert [r.harmonic_index for r in res] == [r.harmonic_index for r in fresh]
+        for a, b in zip(res, fresh):
+            np.testing.assert_allclose(a.frequencies, b.frequencies, rtol=FREQ_TOL)

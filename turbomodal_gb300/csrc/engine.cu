@@ -478,6 +478,15 @@ struct tmg_context {
     UnionMaps pairOp, pairM;
     OpSymbolic pairSym;
     std::string pair_key;
+    // the operator-pattern state of the other regime (rest vs speed) last seen, kept so that a
+    // sweep that returns to it reuses its unions, maps and symbolic analyses
+    struct PatternState {
+        std::string key;
+        UnionMaps opC, opMC, W0, WM0, pairOp, pairM;
+        OpSymbolic symC, pairSym;
+        TuneCand tune_choice;
+        std::string tuned_key;
+    } stash;
     // Coriolis QEP: gyroscopic sum domain W_G = Gc u Gp u Gp^H and the Lancaster block maps
     // of the shifted operator L1 - sigma L2 and of L2 over (W, W_M, W_G)
     std::vector<int64_t> gpT;
@@ -741,6 +750,7 @@ void setup_sector(tmg_context* c, const tmg_sector_desc* d) {
     c->kw_omega = -1.0;
     c->symC.valid = false;
     c->symC_key.clear();
+    c->stash.key.clear();
     c->real[0].valid = c->real[1].valid = false;
     c->results.clear();
 }
@@ -914,6 +924,12 @@ void project(tmg_context* c, const CandMat& A, ProjChain* ch, Flagged& fl, FreeM
 
 bool same_pattern(const Pattern& a, const Pattern& b) { return a.p == b.p && a.i == b.i && a.nrows == b.nrows; }
 
+void swap_op(OpSymbolic& a, OpSymbolic& b) {
+    std::swap(a.S, b.S);
+    a.D.swap(b.D);
+    std::swap(a.valid, b.valid);
+}
+
 void prepare(tmg_context* c, double rpm, bool coriolis) {
     Sector& S = *c->sec;
     const double omega = rpm * 2.0 * PI / 60.0;
@@ -958,7 +974,27 @@ void prepare(tmg_context* c, double rpm, bool coriolis) {
     c->MpfH = transpose_map(c->Mpf.spat, c->mpT);
     const std::string key = pattern_key(c->Kcf.spat) + pattern_key(c->Kpf.spat) + pattern_key(c->Mcf.spat) +
                             pattern_key(c->Mpf.spat);
-    if (key != c->symC_key) {
+    if (key != c->symC_key && c->stash.key == key) {
+        // back to the pattern of the other regime: exchange the current state with the kept one
+        auto& o = c->stash;
+        std::swap(c->opC, o.opC); std::swap(c->opMC, o.opMC); std::swap(c->W0, o.W0); std::swap(c->WM0, o.WM0);
+        std::swap(c->pairOp, o.pairOp); std::swap(c->pairM, o.pairM);
+        swap_op(c->symC, o.symC);
+        swap_op(c->pairSym, o.pairSym);
+        std::swap(c->tune_choice, o.tune_choice); std::swap(c->tuned_key, o.tuned_key);
+        o.key = c->symC_key;
+        c->symC_key = key;
+        c->pair_key = key;
+    } else if (key != c->symC_key) {
+        if (c->symC.valid && c->pairSym.valid) {   // keep the current regime's state for a later return
+            auto& o = c->stash;
+            std::swap(c->opC, o.opC); std::swap(c->opMC, o.opMC); std::swap(c->W0, o.W0); std::swap(c->WM0, o.WM0);
+            std::swap(c->pairOp, o.pairOp); std::swap(c->pairM, o.pairM);
+            swap_op(c->symC, o.symC);
+            swap_op(c->pairSym, o.pairSym);
+            std::swap(c->tune_choice, o.tune_choice); std::swap(c->tuned_key, o.tuned_key);
+            o.key = c->symC_key;
+        }
         // complex harmonic operator: union of Kc, Kp, Kp^H, Mc, Mp, Mp^H
         build_union(c->opC, {&c->Kcf.spat, &c->Kpf.spat, &c->KpfH, &c->Mcf.spat, &c->Mpf.spat, &c->MpfH});
         build_union(c->opMC, {&c->Mcf.spat, &c->Mpf.spat, &c->MpfH});

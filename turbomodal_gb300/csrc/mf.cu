@@ -980,6 +980,19 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
     put(sitems, si);
 }
 
+void DevSymbolic::swap(DevSymbolic& o) noexcept {
+    using std::swap;
+    swap(n, o.n); swap(ns, o.ns); swap(max_front, o.max_front);
+    swap(l_entries, o.l_entries); swap(u_entries, o.u_entries); swap(t_entries, o.t_entries);
+    swap(l_stored, o.l_stored);
+    swap(sn_first, o.sn_first); swap(sn_rows, o.sn_rows); swap(rel, o.rel); swap(child_ptr, o.child_ptr);
+    swap(child_list, o.child_list); swap(sn_row_ptr, o.sn_row_ptr); swap(loff, o.loff); swap(uoff, o.uoff);
+    swap(rel_ptr, o.rel_ptr); swap(perm, o.perm); swap(level_sn, o.level_sn); swap(items, o.items);
+    swap(sitems, o.sitems); swap(dest, o.dest); swap(conj, o.conj); swap(nlower, o.nlower); swap(flops, o.flops);
+    swap(bytes, o.bytes); swap(alloc_stream, o.alloc_stream); swap(cnt, o.cnt); swap(steps, o.steps);
+    swap(tc_rows, o.tc_rows); swap(tc_min_rows, o.tc_min_rows); swap(plan64, o.plan64); swap(level_ptr, o.level_ptr);
+}
+
 void DevSymbolic::release() {
     if (bytes && cnt) cnt->cur -= (int64_t)bytes;
     for (void* p : {(void*)sn_first, (void*)sn_rows, (void*)rel, (void*)child_ptr, (void*)child_list,

@@ -92,6 +92,7 @@ struct DevSymbolic {
     }
     void upload(const Symbolic& S, const std::vector<int64_t>& dest_h, const std::vector<uint8_t>& conj_h);
     void release();
+    void swap(DevSymbolic& o) noexcept;   // exchanges every field (device arrays change owner)
     DevSymbolic() = default;
     DevSymbolic(const DevSymbolic&) = delete;
     DevSymbolic& operator=(const DevSymbolic&) = delete;
