@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -33,8 +34,12 @@ extern thread_local cudaStream_t g_stream;
 // Device bytes held by the context the calling thread is working for (its stream-ordered
 // buffers; null outside a C-ABI call).
 struct ByteCount {
-    int64_t cur = 0, peak = 0;
-    void add(int64_t b) { cur += b; if (cur > peak) peak = cur; }
+    std::atomic<int64_t> cur{0}, peak{0};
+    void add(int64_t b) {
+        const int64_t v = cur.fetch_add(b) + b;
+        int64_t pk = peak.load();
+        while (v > pk && !peak.compare_exchange_weak(pk, v)) {}
+    }
 };
 extern thread_local ByteCount* g_bytes;
 #define TMG_LAUNCH(kernel, grid, block, smem, stream, ...)                                    \

@@ -21,6 +21,7 @@
 #include <numeric>
 #include <random>
 #include <set>
+#include <thread>
 
 #include "../../include/turbomodal_gb300.h"
 #include "engine.hpp"
@@ -434,6 +435,8 @@ struct tmg_context {
     // device bytes this context holds (current, peak); first member, so it outlives every
     // buffer that counts itself in it during destruction
     ByteCount bytes;
+    std::mutex mu;                // phase timings and the error text, written by a batch's helper thread too
+    cudaStream_t st2 = nullptr;   // stream of the real-harmonic batch run beside the complex one
     int device = 0;
     cudaStream_t st = nullptr;
     size_t budget = 0;
@@ -542,6 +545,12 @@ size_t device_free_bytes(int device) {
         if (reserved > used) fr += (size_t)(reserved - used);
     }
     return fr;
+}
+
+// error text written while a batch's helper thread may also write it
+void note_err(tmg_context* c, const std::string& m) {
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->err = m;
 }
 
 int set_err(tmg_context* c, int code, const std::string& m) {
@@ -1310,28 +1319,28 @@ struct ShiftInvertB {
         const int64_t nl = D->nlower;
         L.alloc((size_t)B * D->l_entries);
         U.alloc((size_t)B * std::max<int64_t>(D->u_entries, 1));
-        L.zero(c->st);
+        L.zero(g_stream);
         const Batch<Tf> bt{B, L.p, U.p, D->l_entries, D->u_entries};
         if constexpr (std::is_same<Tv, Tf>::value) {
-            mf_scatter<Tf>(c->st, *D, bt, lower_vals);
+            mf_scatter<Tf>(g_stream, *D, bt, lower_vals);
         } else {
             scale.alloc((size_t)B * n);
-            TMG_LAUNCH(k_diag_scale<Tv>, dim3(nblk(n), B), 256, 0, c->st, n, A.rowptr, A.col, A.val, A.vstride, scale.p);
+            TMG_LAUNCH(k_diag_scale<Tv>, dim3(nblk(n), B), 256, 0, g_stream, n, A.rowptr, A.col, A.val, A.vstride, scale.p);
             DVec<Tf> lv;
             lv.alloc((size_t)B * nl);
-            TMG_LAUNCH((k_scale_lower<Tf, Tv>), dim3(nblk(nl), B), 256, 0, c->st, nl, n, um->low_row.p, um->low_col.p,
+            TMG_LAUNCH((k_scale_lower<Tf, Tv>), dim3(nblk(nl), B), 256, 0, g_stream, nl, n, um->low_row.p, um->low_col.p,
                        scale.p, lower_vals, lv.p);
-            mf_scatter<Tf>(c->st, *D, bt, lv.p);
-            TMG_CUDA(cudaStreamSynchronize(c->st));
+            mf_scatter<Tf>(g_stream, *D, bt, lv.p);
+            TMG_CUDA(cudaStreamSynchronize(g_stream));
         }
         DVec<int> status;
         status.alloc(2 * B);
-        status.zero(c->st);
-        mf_factor<Tf>(c->st, *D, bt, status.p, c->tensor_cores);
-        mf_count_nonpos<Tf>(c->st, *D, bt, status.p + B);
+        status.zero(g_stream);
+        mf_factor<Tf>(g_stream, *D, bt, status.p, c->tensor_cores);
+        mf_count_nonpos<Tf>(g_stream, *D, bt, status.p + B);
         std::vector<int> hs(2 * B);
-        TMG_CUDA(cudaMemcpyAsync(hs.data(), status.p, 2 * B * sizeof(int), cudaMemcpyDeviceToHost, c->st));
-        TMG_CUDA(cudaStreamSynchronize(c->st));
+        TMG_CUDA(cudaMemcpyAsync(hs.data(), status.p, 2 * B * sizeof(int), cudaMemcpyDeviceToHost, g_stream));
+        TMG_CUDA(cudaStreamSynchronize(g_stream));
         spd = true;
         skip.assign(B, 0);
         failed.assign(B, std::string());
@@ -1354,7 +1363,7 @@ struct ShiftInvertB {
         np.alloc((size_t)B * LZ_DOT_BLOCKS);
         nrm.alloc(B);
         ddone.alloc(B);
-        ddone.zero(c->st);
+        ddone.zero(g_stream);
         worst.assign(B, 0.0);
     }
     Batch<Tf> batch() const { return Batch<Tf>{B, L.p, nullptr, D->l_entries, 0}; }
@@ -1368,8 +1377,8 @@ struct ShiftInvertB {
         const int64_t nm = (int64_t)n * m;
         W.alloc((size_t)B * nm);
         AW.alloc((size_t)B * nm);
-        TMG_CUDA(cudaMemcpyAsync(W.p, Wsrc, (size_t)B * nm * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
-        lz_spmv<Tv>(c->st, B, A, W.p, nm, AW.p, nm, m, n);
+        TMG_CUDA(cudaMemcpyAsync(W.p, Wsrc, (size_t)B * nm * sizeof(Tv), cudaMemcpyDeviceToDevice, g_stream));
+        lz_spmv<Tv>(g_stream, B, A, W.p, nm, AW.p, nm, m, n);
         pdef.alloc((size_t)B * m * LZ_DOT_BLOCKS);
         hdef.alloc((size_t)B * m);
         ydef.alloc((size_t)B * m);
@@ -1377,9 +1386,9 @@ struct ShiftInvertB {
         std::vector<std::complex<double>> E((size_t)B * m * m);
         std::vector<Tv> col((size_t)B * m);
         for (int v = 0; v < m; v++) {
-            lz_multidot<Tv>(c->st, B, n, W.p, nm, n, m, AW.p + (int64_t)v * n, nm, pdef.p, hdef.p);
-            TMG_CUDA(cudaMemcpyAsync(col.data(), hdef.p, col.size() * sizeof(Tv), cudaMemcpyDeviceToHost, c->st));
-            TMG_CUDA(cudaStreamSynchronize(c->st));
+            lz_multidot<Tv>(g_stream, B, n, W.p, nm, n, m, AW.p + (int64_t)v * n, nm, pdef.p, hdef.p);
+            TMG_CUDA(cudaMemcpyAsync(col.data(), hdef.p, col.size() * sizeof(Tv), cudaMemcpyDeviceToHost, g_stream));
+            TMG_CUDA(cudaStreamSynchronize(g_stream));
             for (int p = 0; p < B; p++)
                 for (int k = 0; k < m; k++) E[((size_t)p * m + v) * m + k] = to_std(col[(size_t)p * m + k]);
         }
@@ -1417,9 +1426,9 @@ struct ShiftInvertB {
     // z -= W Einv (AW^H z) for every problem
     void deflate(Tv* z) {
         const int64_t nm = (int64_t)n * mdef;
-        lz_multidot<Tv>(c->st, B, n, AW.p, nm, n, mdef, z, n, pdef.p, hdef.p);
-        TMG_LAUNCH(k_small_mv<Tv>, B, 32, 0, c->st, mdef, Einv.p, hdef.p, ydef.p, 1.0);
-        lz_gemv_sub<Tv>(c->st, B, n, mdef, W.p, nm, ydef.p, mdef, z, n);
+        lz_multidot<Tv>(g_stream, B, n, AW.p, nm, n, mdef, z, n, pdef.p, hdef.p);
+        TMG_LAUNCH(k_small_mv<Tv>, B, 32, 0, g_stream, mdef, Einv.p, hdef.p, ydef.p, 1.0);
+        lz_gemv_sub<Tv>(g_stream, B, n, mdef, W.p, nm, ydef.p, mdef, z, n);
     }
 
     // the permute / supernodal sweeps / permute sequence of one batched solve is captured
@@ -1429,24 +1438,24 @@ struct ShiftInvertB {
         if (!gexec) {
             const int64_t l0 = g_kernel_launches;
             cudaGraph_t g;
-            TMG_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-            mf_permute_in<Tf, Tv>(c->st, *D, B, gin.p, n, xw.p, s);
-            mf_solve<Tf>(c->st, *D, batch(), xw.p, tb.p, ddone.p);
-            mf_permute_out<Tf, Tv>(c->st, *D, B, xw.p, gout.p, n, s);
-            TMG_CUDA(cudaStreamEndCapture(c->st, &g));
+            TMG_CUDA(cudaStreamBeginCapture(g_stream, cudaStreamCaptureModeThreadLocal));
+            mf_permute_in<Tf, Tv>(g_stream, *D, B, gin.p, n, xw.p, s);
+            mf_solve<Tf>(g_stream, *D, batch(), xw.p, tb.p, ddone.p);
+            mf_permute_out<Tf, Tv>(g_stream, *D, B, xw.p, gout.p, n, s);
+            TMG_CUDA(cudaStreamEndCapture(g_stream, &g));
             TMG_CUDA(cudaGraphInstantiate(&gexec, g, 0));
             TMG_CUDA(cudaGraphDestroy(g));
             launches_per_solve = g_kernel_launches - l0;
             g_kernel_launches = l0;
         }
-        TMG_CUDA(cudaMemcpyAsync(gin.p, b, (size_t)B * n * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
+        TMG_CUDA(cudaMemcpyAsync(gin.p, b, (size_t)B * n * sizeof(Tv), cudaMemcpyDeviceToDevice, g_stream));
         if (c->profile) {
             if (!c->pev0) { TMG_CUDA(cudaEventCreate(&c->pev0)); TMG_CUDA(cudaEventCreate(&c->pev1)); }
-            TMG_CUDA(cudaEventRecord(c->pev0, c->st));
+            TMG_CUDA(cudaEventRecord(c->pev0, g_stream));
         }
-        TMG_CUDA(cudaGraphLaunch(gexec, c->st));
+        TMG_CUDA(cudaGraphLaunch(gexec, g_stream));
         if (c->profile) {
-            TMG_CUDA(cudaEventRecord(c->pev1, c->st));
+            TMG_CUDA(cudaEventRecord(c->pev1, g_stream));
             TMG_CUDA(cudaEventSynchronize(c->pev1));
             float ms = 0.f;
             TMG_CUDA(cudaEventElapsedTime(&ms, c->pev0, c->pev1));
@@ -1457,14 +1466,14 @@ struct ShiftInvertB {
             c->solve_bytes += (double)B * (2.0 * (double)D->l_stored * sizeof(Tf) + 4.0 * (double)n * sizeof(Tf));
         }
         g_kernel_launches += launches_per_solve;
-        TMG_CUDA(cudaMemcpyAsync(x, gout.p, (size_t)B * n * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
+        TMG_CUDA(cudaMemcpyAsync(x, gout.p, (size_t)B * n * sizeof(Tv), cudaMemcpyDeviceToDevice, g_stream));
         solves++;
     }
     std::vector<double> norms(const Tv* v) {
         std::vector<double> h(B);
-        lz_norm2<Tv>(c->st, B, n, v, n, np.p, nrm.p);
-        TMG_CUDA(cudaMemcpyAsync(h.data(), nrm.p, B * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-        TMG_CUDA(cudaStreamSynchronize(c->st));
+        lz_norm2<Tv>(g_stream, B, n, v, n, np.p, nrm.p);
+        TMG_CUDA(cudaMemcpyAsync(h.data(), nrm.p, B * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
+        TMG_CUDA(cudaStreamSynchronize(g_stream));
         return h;
     }
     // Restarted GMRES on A x = b, right-preconditioned by the FP32 factor (z = F^-1 v), FP64
@@ -1475,7 +1484,7 @@ struct ShiftInvertB {
     // few outliers.  Each cycle ends with the true FP64 residual.  Returns the inner iterations.
     int gmres(const Tv* b, Tv* x, const std::vector<double>& bn, std::vector<int>& done, std::vector<double>& rn) {
         using cplx = std::complex<double>;
-        cudaStream_t st = c->st;
+        cudaStream_t st = g_stream;
         const int64_t vs = (int64_t)(GM + 1) * n, zs = (int64_t)GM * n;
         if (!GV.p) {
             GV.alloc((size_t)B * vs);
@@ -1600,18 +1609,18 @@ struct ShiftInvertB {
         if (bs != n) {
             if (!bin.p) bin.alloc((size_t)B * n);
             TMG_CUDA(cudaMemcpy2DAsync(bin.p, n * sizeof(Tv), b, bs * sizeof(Tv), n * sizeof(Tv), B,
-                                       cudaMemcpyDeviceToDevice, c->st));
+                                       cudaMemcpyDeviceToDevice, g_stream));
             b = bin.p;
         }
         if (!mixed) {   // finished problems are skipped by the solve kernels
-            TMG_CUDA(cudaMemcpyAsync(ddone.p, skip.data(), B * sizeof(int), cudaMemcpyHostToDevice, c->st));
+            TMG_CUDA(cudaMemcpyAsync(ddone.p, skip.data(), B * sizeof(int), cudaMemcpyHostToDevice, g_stream));
             solve1(b, x);
             return;
         }
         const std::vector<double> bn = norms(b);
         std::vector<int> done(skip);
         std::vector<double> rn;
-        TMG_CUDA(cudaMemcpyAsync(ddone.p, done.data(), B * sizeof(int), cudaMemcpyHostToDevice, c->st));
+        TMG_CUDA(cudaMemcpyAsync(ddone.p, done.data(), B * sizeof(int), cudaMemcpyHostToDevice, g_stream));
         int it = 0;
         auto check = [&]() {
             rn = norms(r.p);
@@ -1620,34 +1629,34 @@ struct ShiftInvertB {
                 if (!done[p] && rn[p] <= rtol * rtol * bn[p]) { done[p] = 1; changed = true; }
                 all = all && done[p];
             }
-            if (changed) TMG_CUDA(cudaMemcpyAsync(ddone.p, done.data(), B * sizeof(int), cudaMemcpyHostToDevice, c->st));
+            if (changed) TMG_CUDA(cudaMemcpyAsync(ddone.p, done.data(), B * sizeof(int), cudaMemcpyHostToDevice, g_stream));
             return all;
         };
         if (spd) {
             // CG on A x = b preconditioned by the FP32 factor; FP64 operator and vectors
-            TMG_CUDA(cudaMemsetAsync(x, 0, (size_t)B * n * sizeof(Tv), c->st));
-            lz_copy<Tv>(c->st, (int64_t)B * n, b, r.p);
+            TMG_CUDA(cudaMemsetAsync(x, 0, (size_t)B * n * sizeof(Tv), g_stream));
+            lz_copy<Tv>(g_stream, (int64_t)B * n, b, r.p);
             if (mdef > 0) {   // deflated start x0 = W Einv W^H b, r0 = b - A x0
                 const int64_t nm = (int64_t)n * mdef;
-                lz_multidot<Tv>(c->st, B, n, W.p, nm, n, mdef, b, n, pdef.p, hdef.p);
-                TMG_LAUNCH(k_small_mv<Tv>, B, 32, 0, c->st, mdef, Einv.p, hdef.p, ydef.p, -1.0);
-                lz_gemv_sub<Tv>(c->st, B, n, mdef, W.p, nm, ydef.p, mdef, x, n);
-                lz_spmv<Tv>(c->st, B, A, x, n, r.p, n, 1, n, true);
+                lz_multidot<Tv>(g_stream, B, n, W.p, nm, n, mdef, b, n, pdef.p, hdef.p);
+                TMG_LAUNCH(k_small_mv<Tv>, B, 32, 0, g_stream, mdef, Einv.p, hdef.p, ydef.p, -1.0);
+                lz_gemv_sub<Tv>(g_stream, B, n, mdef, W.p, nm, ydef.p, mdef, x, n);
+                lz_spmv<Tv>(g_stream, B, A, x, n, r.p, n, 1, n, true);
             }
             solve1(r.p, z.p);
             if (mdef > 0) deflate(z.p);
-            lz_copy<Tv>(c->st, (int64_t)B * n, z.p, pp.p);
-            lz_multidot<Tv>(c->st, B, n, r.p, n, n, 1, z.p, n, d.p, sc.p);           // rz
+            lz_copy<Tv>(g_stream, (int64_t)B * n, z.p, pp.p);
+            lz_multidot<Tv>(g_stream, B, n, r.p, n, n, 1, z.p, n, d.p, sc.p);           // rz
             for (it = 1; it <= max_iter; it++) {
-                lz_spmv<Tv>(c->st, B, A, pp.p, n, q.p, n, 1, n);
-                lz_multidot<Tv>(c->st, B, n, pp.p, n, n, 1, q.p, n, d.p, sc.p + B);   // pq
-                TMG_LAUNCH(k_pcg_xr<Tv>, dim3(nblk(n), B), 256, 0, c->st, n, x, r.p, pp.p, q.p, sc.p, sc.p + B, ddone.p);
+                lz_spmv<Tv>(g_stream, B, A, pp.p, n, q.p, n, 1, n);
+                lz_multidot<Tv>(g_stream, B, n, pp.p, n, n, 1, q.p, n, d.p, sc.p + B);   // pq
+                TMG_LAUNCH(k_pcg_xr<Tv>, dim3(nblk(n), B), 256, 0, g_stream, n, x, r.p, pp.p, q.p, sc.p, sc.p + B, ddone.p);
                 if (check()) break;
                 solve1(r.p, z.p);
                 if (mdef > 0) deflate(z.p);
-                lz_multidot<Tv>(c->st, B, n, r.p, n, n, 1, z.p, n, d.p, sc.p + 2 * B);  // rz_new
-                TMG_LAUNCH(k_pcg_p<Tv>, dim3(nblk(n), B), 256, 0, c->st, n, pp.p, z.p, sc.p + 2 * B, sc.p, ddone.p);
-                TMG_CUDA(cudaMemcpyAsync(sc.p, sc.p + 2 * B, B * sizeof(Tv), cudaMemcpyDeviceToDevice, c->st));
+                lz_multidot<Tv>(g_stream, B, n, r.p, n, n, 1, z.p, n, d.p, sc.p + 2 * B);  // rz_new
+                TMG_LAUNCH(k_pcg_p<Tv>, dim3(nblk(n), B), 256, 0, g_stream, n, pp.p, z.p, sc.p + 2 * B, sc.p, ddone.p);
+                TMG_CUDA(cudaMemcpyAsync(sc.p, sc.p + 2 * B, B * sizeof(Tv), cudaMemcpyDeviceToDevice, g_stream));
             }
         } else {
             it = gmres(b, x, bn, done, rn);
@@ -1683,7 +1692,7 @@ std::vector<EigOut<Tv>> lanczos(tmg_context* c, ShiftInvertB<Tv, Tf>& op, const 
                                 double shift, double tol, int max_restarts, const double* dshifts = nullptr) {
     const int64_t n = op.n;
     const int B = op.B;
-    cudaStream_t st = c->st;
+    cudaStream_t st = g_stream;
     const int64_t vs = (int64_t)(ncv + 1) * n;
     DVec<Tv> V, MV, w, Mw, h, dot, part;
     V.alloc((size_t)B * vs); MV.alloc((size_t)B * vs);
@@ -1802,7 +1811,7 @@ struct Problem {
 // (src/cyclic_solver.cpp:1185-1211); X holds nm free-space columns of n_free entries.
 void expand_to_sector(tmg_context* c, const Problem& pr, const zd* X, int nm, ResultHost& R) {
     Sector& S = *c->sec;
-    cudaStream_t st = c->st;
+    cudaStream_t st = g_stream;
     const int32_t ndof = 3 * S.nn;
     DVec<zd> full;
     full.alloc((size_t)ndof * std::max(nm, 1));
@@ -1836,7 +1845,7 @@ void finish_result(tmg_context* c, const Problem& pr, EigOut<Tv>& eo, const DevC
                    double shift, int num_modes, double min_frequency, const double* residuals = nullptr) {
     Sector& S = *c->sec;
     ResultHost& R = *pr.R;
-    cudaStream_t st = c->st;
+    cudaStream_t st = g_stream;
     const int64_t n = S.n_free;
     std::vector<int> keep;
     for (int t = 0; t < eo.ne; t++) {
@@ -1942,7 +1951,7 @@ void finish_qep(tmg_context* c, const Problem& pr, const EigOut<zd>& eo, int num
     for (int t = 0; t < nm; t++) {
         R.freqs.push_back(std::fabs(keep[t].om) / (2.0 * PI));
         R.whirl.push_back(keep[t].wh);
-        lz_copy<zd>(c->st, n, eo.X.p + (int64_t)keep[t].idx * n2, Xq.p + (int64_t)t * n);
+        lz_copy<zd>(g_stream, n, eo.X.p + (int64_t)keep[t].idx * n2, Xq.p + (int64_t)t * n);
     }
     expand_to_sector(c, pr, Xq.p, nm, R);
 }
@@ -1953,7 +1962,7 @@ void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os
                const Tv* vals_csc, const DevCsr<Tv>& M, int nev, int ncv, double shift, int max_restarts, bool mixed,
                int num_modes, double min_frequency, const std::vector<double>* shifts = nullptr, bool qep = false,
                const Tv* Wdef = nullptr, int mdef = 0) {
-    cudaStream_t st = c->st;
+    cudaStream_t st = g_stream;
     const int B = (int)probs.size();
     const int64_t nl = (int64_t)um.lower2csc.n, nU = um.U.nnz();
     DVec<Tv> lower, acsr;
@@ -1975,8 +1984,11 @@ void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os
     if (shifts) dsh.upload(*shifts);
     std::vector<EigOut<Tv>> eo = lanczos<Tv, Tf>(c, op, M, nev, ncv, shift, 1e-8, max_restarts, shifts ? dsh.p : nullptr);
     auto t2 = std::chrono::steady_clock::now();
-    c->phase_ms[1] += std::chrono::duration<double, std::milli>(t1 - t0).count();
-    c->phase_ms[2] += std::chrono::duration<double, std::milli>(t2 - t1).count();
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        c->phase_ms[1] += std::chrono::duration<double, std::milli>(t1 - t0).count();
+        c->phase_ms[2] += std::chrono::duration<double, std::milli>(t2 - t1).count();
+    }
     if constexpr (std::is_same<Tv, zd>::value) {
         if (c->deflate && !qep) {   // keep the lowest eigenvectors for the next speed
             if (c->recycle_key != c->symC_key) {
@@ -1991,10 +2003,13 @@ void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os
                 }
         }
     }
-    c->phase_ms[5] += (double)op.solves;
-    if (mixed && !qep && std::is_same<Tv, zd>::value) c->solves_per_factor = (double)op.solves;
-    c->phase_ms[6] += (double)op.applies;
-    c->phase_ms[7] = std::max(c->phase_ms[7], (double)op.max_its);
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        c->phase_ms[5] += (double)op.solves;
+        if (mixed && !qep && std::is_same<Tv, zd>::value) c->solves_per_factor = (double)op.solves;
+        c->phase_ms[6] += (double)op.applies;
+        c->phase_ms[7] = std::max(c->phase_ms[7], (double)op.max_its);
+    }
     if (std::getenv("TMG_VERBOSE"))
         std::fprintf(stderr, "[tmg] batch B=%d n=%d %s: factor %.1f ms, lanczos %.1f ms, %lld solves (%lld launches each), "
                      "%lld applies, <=%lld refinement iterations\n", B, op.n, mixed ? "mixed" : "fp64",
@@ -2008,7 +2023,7 @@ void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os
         R.refine_residual = op.worst[p];
         R.solves = op.solves;
         R.applies = op.applies;
-        if (!eo[p].failed.empty()) { R.status = TMG_ERR_NUMERIC; c->err = eo[p].failed; continue; }
+        if (!eo[p].failed.empty()) { R.status = TMG_ERR_NUMERIC; note_err(c, eo[p].failed); continue; }
         if (!eo[p].converged && eo[p].ne == 0) { R.status = TMG_ERR_NUMERIC; continue; }
         if constexpr (std::is_same<Tv, zd>::value) {
             if (qep) { finish_qep(c, probs[p], eo[p], num_modes, min_frequency); continue; }
@@ -2019,6 +2034,7 @@ void run_batch(tmg_context* c, std::vector<Problem>& probs, const OpSymbolic& os
         finish_result<Tv>(c, probs[p], eo[p], Ap, Mp, shift, num_modes, min_frequency);
     }
     auto t3 = std::chrono::steady_clock::now();
+    std::lock_guard<std::mutex> lk(c->mu);
     c->phase_ms[3] += std::chrono::duration<double, std::milli>(t3 - t2).count();
 }
 
@@ -2276,7 +2292,10 @@ std::vector<Problem> mixed_failures(tmg_context* c, const std::vector<Problem>& 
             out.push_back(pr);
         }
     }
-    c->phase_ms[8] += (double)out.size();
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        c->phase_ms[8] += (double)out.size();
+    }
     if (!out.empty() && std::getenv("TMG_VERBOSE"))
         std::fprintf(stderr, "[tmg] %zu problem(s) of a mixed batch solved again in FP64\n", out.size());
     return out;
@@ -2694,8 +2713,10 @@ void solve_sweep(tmg_context* c, const std::vector<double>& rpms, const std::vec
                 }
             }
         }
-        // real harmonics of the group: one batch (problem stride rnU / rnM)
-        if (!real.empty()) {
+        // real harmonics of the group: one batch (problem stride rnU / rnM), run by a helper
+        // thread on the context's second stream while this thread runs the complex batches
+        // (both are latency-bound at these batch sizes, so their launches overlap on the device)
+        auto real_batch = [&]() {
             const int nev = std::min(real[0].nev_target + n_extra, S.n_free - 1);
             const int ncv = std::min(std::max(4 * nev + 1, 40), S.n_free);
             DevCsr<double> M;
@@ -2710,7 +2731,7 @@ void solve_sweep(tmg_context* c, const std::vector<double>& rpms, const std::vec
                                               num_modes, min_frequency);
             } catch (const numeric_error& e) {
                 for (auto& pr : real) pr.R->status = TMG_ERR_NUMERIC;
-                c->err = e.what();
+                note_err(c, e.what());
             }
             if (mixed) {
                 std::vector<Problem> again = mixed_failures(c, real);
@@ -2721,8 +2742,8 @@ void solve_sweep(tmg_context* c, const std::vector<double>& rpms, const std::vec
                     for (size_t q = 0; q < again.size(); q++) {
                         size_t src = 0;
                         while (real[src].R != again[q].R) src++;
-                        if (rnU) lz_copy<double>(st, rnU, rvals.p + src * rnU, v2.p + q * rnU);
-                        if (rnM) lz_copy<double>(st, rnM, rm.p + src * rnM, m2.p + q * rnM);
+                        if (rnU) lz_copy<double>(g_stream, rnU, rvals.p + src * rnU, v2.p + q * rnU);
+                        if (rnM) lz_copy<double>(g_stream, rnM, rm.p + src * rnM, m2.p + q * rnM);
                     }
                     DevCsr<double> M2 = M;
                     M2.val = m2.p;
@@ -2731,17 +2752,52 @@ void solve_sweep(tmg_context* c, const std::vector<double>& rpms, const std::vec
                                                   false, num_modes, min_frequency);
                     } catch (const numeric_error& e) {
                         for (auto& pr : again) pr.R->status = TMG_ERR_NUMERIC;
-                        c->err = e.what();
+                        note_err(c, e.what());
                     } catch (const cuda_error& e) {   // the FP64 factor does not fit: these problems fail alone
                         if (!std::strstr(e.what(), "out of memory")) throw;
                         for (auto& pr : again) pr.R->status = TMG_ERR_NOMEM;
-                        c->err = std::string("FP64 retry of a mixed-path failure: ") + e.what();
+                        note_err(c, std::string("FP64 retry of a mixed-path failure: ") + e.what());
                     }
                 }
             }
+        };
+        std::thread helper;
+        std::exception_ptr helper_err;
+        int64_t helper_launches = 0;
+        if (!real.empty()) {
+            if (c->profile) {
+                real_batch();
+            } else {
+                if (!c->st2) TMG_CUDA(cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking));
+                if (!S.dcand_i.p) S.dcand_i.upload(S.cand.i);   // shared, read-only from here on
+                cudaEvent_t formed;
+                TMG_CUDA(cudaEventCreateWithFlags(&formed, cudaEventDisableTiming));
+                TMG_CUDA(cudaEventRecord(formed, st));
+                const int dev = c->device;
+                helper = std::thread([&, formed, dev]() {
+                    try {
+                        TMG_CUDA(cudaSetDevice(dev));
+                        g_stream = c->st2;
+                        g_bytes = &c->bytes;
+                        TMG_CUDA(cudaStreamWaitEvent(c->st2, formed, 0));
+                        const int64_t l0 = g_kernel_launches;
+                        real_batch();
+                        helper_launches = g_kernel_launches - l0;
+                        TMG_CUDA(cudaStreamSynchronize(c->st2));
+                    } catch (...) {
+                        helper_err = std::current_exception();
+                    }
+                    g_stream = nullptr;
+                    g_bytes = nullptr;
+                });
+                TMG_CUDA(cudaEventDestroy(formed));
+            }
         }
-        rvals.release();
-        rm.release();
+        struct Join {   // the helper thread ends before anything it reads goes out of scope
+            std::thread& t;
+            ~Join() { if (t.joinable()) t.join(); }
+        } join_helper{helper};
+
         // complex harmonics of the group, in batches of at most bmax problems
         for (size_t b0 = 0; b0 < cplx.size(); b0 += bmax) {
             std::vector<Problem> grp(cplx.begin() + b0, cplx.begin() + std::min(cplx.size(), b0 + (size_t)bmax));
@@ -2778,7 +2834,7 @@ void solve_sweep(tmg_context* c, const std::vector<double>& rpms, const std::vec
                                       min_frequency);
             } catch (const numeric_error& e) {
                 for (auto& pr : grp) pr.R->status = TMG_ERR_NUMERIC;
-                c->err = e.what();
+                note_err(c, e.what());
             }
             if (mixed) {
                 std::vector<Problem> again = mixed_failures(c, grp);
@@ -2799,15 +2855,18 @@ void solve_sweep(tmg_context* c, const std::vector<double>& rpms, const std::vec
                                           min_frequency);
                     } catch (const numeric_error& e) {
                         for (auto& pr : again) pr.R->status = TMG_ERR_NUMERIC;
-                        c->err = e.what();
+                        note_err(c, e.what());
                     } catch (const cuda_error& e) {   // the FP64 factor does not fit: these problems fail alone
                         if (!std::strstr(e.what(), "out of memory")) throw;
                         for (auto& pr : again) pr.R->status = TMG_ERR_NOMEM;
-                        c->err = std::string("FP64 retry of a mixed-path failure: ") + e.what();
+                        note_err(c, std::string("FP64 retry of a mixed-path failure: ") + e.what());
                     }
                 }
             }
         }
+        if (helper.joinable()) helper.join();
+        g_kernel_launches += helper_launches;
+        if (helper_err) std::rethrow_exception(helper_err);
         g0 = group.back() + 1;
     }
     TMG_CUDA(cudaStreamSynchronize(st));
@@ -2922,10 +2981,14 @@ int tmg_get_option(tmg_context* c, int option, double* value) {
 int tmg_destroy(tmg_context* c) {
     if (!c) return TMG_ERR_ARG;
     cudaSetDevice(c->device);
-    cudaStream_t st = c->st;
+    cudaStream_t st = c->st, st2 = c->st2;
     g_stream = st;                     // the context's buffers are freed in its stream's order
     delete c;
     g_stream = nullptr;
+    if (st2) {
+        cudaStreamSynchronize(st2);
+        cudaStreamDestroy(st2);
+    }
     if (st) {
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);
@@ -3228,14 +3291,14 @@ int tmg_result_info(tmg_context* c, int idx, tmg_result_meta* info) {
 
 int tmg_device_bytes(tmg_context* c, int64_t* current, int64_t* peak) {
     if (!c) return TMG_ERR_ARG;
-    if (current) *current = c->bytes.cur;
-    if (peak) *peak = c->bytes.peak;
+    if (current) *current = c->bytes.cur.load();
+    if (peak) *peak = c->bytes.peak.load();
     return TMG_OK;
 }
 
 int tmg_reset_peak_bytes(tmg_context* c) {
     if (!c) return TMG_ERR_ARG;
-    c->bytes.peak = c->bytes.cur;
+    c->bytes.peak.store(c->bytes.cur.load());
     return TMG_OK;
 }
 
