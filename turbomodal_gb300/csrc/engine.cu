@@ -1307,7 +1307,7 @@ struct ShiftInvertB {
     DVec<Tv> W, AW, Einv, hdef, ydef, pdef;
     // restarted GMRES of the indefinite case: GM Krylov vectors per cycle, V ((GM+1) x n per
     // problem), preconditioned directions Z (GM x n per problem)
-    static constexpr int GM = 16;
+    static constexpr int GM = 32;
     int gmres_cycles = 4;
     DVec<Tv> GV, GZ, gh, gpart, gy;
     DVec<double> ginv;
