@@ -460,10 +460,11 @@ def main():
     v_dev_s = sum(dev_ms[i] for i in vidx) / 1e3
     v_wall_s = sum(wall_s[i] for i in vidx)
     # roofline of the dominant kernel: the shift-invert triangular-solve graph of the batch of
-    # complex harmonics (HBM bound), timed live with CUDA events in one extra profiled solve
+    # complex harmonics (HBM bound), timed live with CUDA events in one extra profiled sweep call
+    # of the timed batch shape (the complex harmonics of --sweep-group speeds)
     mesh_k = [k for k in (hi or range(mesh.num_sectors // 2 + 1)) if 0 < k < mesh.num_sectors / 2]
     solver.set_profiling(True)
-    solver.solve_at_rpm(timed[0], args.num_modes, mesh_k, precision="mixed")
+    solver.solve_rpm_sweep(timed[:grp], args.num_modes, mesh_k, precision="mixed")
     prof = solver.profile_solve()
     solver.set_profiling(False)
     log(f"profiled solve: {prof['count']} batched triangular solves, {prof['ms']:.1f} ms")
@@ -477,13 +478,13 @@ def main():
     per_launch_bytes = prof["bytes"] / max(prof["count"], 1)
     per_launch_s = prof["ms"] / max(prof["count"], 1) / 1e3
     achieved = per_launch_bytes / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
-    traffic = None   # DRAM bytes of one batched solve from an ncu capture of this workload
+    traffic = None   # DRAM bytes of one batched solve: the ncu-measured DRAM / algorithmic ratio
     tr_path = os.path.join(ROOT, "profiles", "trisolve_cfg1_traffic.txt")
     if os.path.exists(tr_path):
         with open(tr_path) as fh:
             for line in fh:
-                if line.startswith("dram_bytes_per_solve"):
-                    traffic = float(line.split("=")[1])
+                if line.startswith("dram_over_algorithmic"):
+                    traffic = float(line.split("=")[1]) * per_launch_bytes
     t_dev_all = max_over_ranks(pg, sum(dev_ms) / 1e3)
     t_dev = max_over_ranks(pg, v_dev_s)
     t_wall = max_over_ranks(pg, v_wall_s)
@@ -545,8 +546,8 @@ def main():
                     "h2d_bytes_per_step": 8 + 4 * max(len(hi), 19) // grp,
                     "d2h_bytes_per_step": int(np.mean(d2h)) if d2h else 0},
             "gpu_launches": launches,
-            "roofline": {"kernel": f"shift-invert triangular solve of the {len(mesh_k)} complex harmonics "
-                                   "(supernodal sweeps, one CUDA graph per batched solve)",
+            "roofline": {"kernel": f"shift-invert triangular solve of the {len(mesh_k)} complex harmonics of "
+                                   f"{min(grp, len(timed))} speeds (supernodal sweeps, one CUDA graph per batched solve)",
                          "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak if hbm_peak else None, "traffic": traffic,
                          "per_launch_bytes": per_launch_bytes, "launches": prof["count"],
