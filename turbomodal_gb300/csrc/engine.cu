@@ -2764,39 +2764,45 @@ void solve_sweep(tmg_context* c, const std::vector<double>& rpms, const std::vec
         std::thread helper;
         std::exception_ptr helper_err;
         int64_t helper_launches = 0;
+        cudaEvent_t formed = nullptr;
+        struct Join {   // the helper thread ends before anything it reads goes out of scope
+            std::thread& t;
+            cudaEvent_t& ev;
+            ~Join() {
+                if (t.joinable()) t.join();
+                if (ev) cudaEventDestroy(ev);   // only after the helper waited on it
+                ev = nullptr;
+            }
+        } join_helper{helper, formed};
         if (!real.empty()) {
             if (c->profile) {
                 real_batch();
             } else {
                 if (!c->st2) TMG_CUDA(cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking));
                 if (!S.dcand_i.p) S.dcand_i.upload(S.cand.i);   // shared, read-only from here on
-                cudaEvent_t formed;
                 TMG_CUDA(cudaEventCreateWithFlags(&formed, cudaEventDisableTiming));
                 TMG_CUDA(cudaEventRecord(formed, st));
                 const int dev = c->device;
-                helper = std::thread([&, formed, dev]() {
+                cudaStream_t st2 = c->st2;
+                cudaEvent_t ready = formed;
+                helper = std::thread([&, ready, dev, st2]() {
                     try {
                         TMG_CUDA(cudaSetDevice(dev));
-                        g_stream = c->st2;
+                        g_stream = st2;
                         g_bytes = &c->bytes;
-                        TMG_CUDA(cudaStreamWaitEvent(c->st2, formed, 0));
+                        TMG_CUDA(cudaStreamWaitEvent(st2, ready, 0));
                         const int64_t l0 = g_kernel_launches;
                         real_batch();
                         helper_launches = g_kernel_launches - l0;
-                        TMG_CUDA(cudaStreamSynchronize(c->st2));
+                        TMG_CUDA(cudaStreamSynchronize(st2));
                     } catch (...) {
                         helper_err = std::current_exception();
                     }
                     g_stream = nullptr;
                     g_bytes = nullptr;
                 });
-                TMG_CUDA(cudaEventDestroy(formed));
             }
         }
-        struct Join {   // the helper thread ends before anything it reads goes out of scope
-            std::thread& t;
-            ~Join() { if (t.joinable()) t.join(); }
-        } join_helper{helper};
 
         // complex harmonics of the group, in batches of at most bmax problems
         for (size_t b0 = 0; b0 < cplx.size(); b0 += bmax) {
@@ -2865,6 +2871,7 @@ void solve_sweep(tmg_context* c, const std::vector<double>& rpms, const std::vec
             }
         }
         if (helper.joinable()) helper.join();
+        if (formed) { cudaEventDestroy(formed); formed = nullptr; }
         g_kernel_launches += helper_launches;
         if (helper_err) std::rethrow_exception(helper_err);
         g0 = group.back() + 1;
