@@ -399,9 +399,12 @@ def main():
     mesh = config_mesh(1)
     hi = harmonics_arg(args.harmonics)
     my_rpms = shard_speeds(RPMS, rank, ws)
-    # deflated refinement (previous speed's eigenvectors); SIMT trailing updates (the library default)
+    # deflated refinement (previous speed's eigenvectors); SIMT trailing updates (the library
+    # default); supernode shapes tuned on the first batch of each operator pattern (at rest and
+    # at speed, both in the warm-up speeds)
     solver = CyclicSymmetrySolver(mesh, TITANIUM, device=local, precision="mixed", deflate=True)
     solver.set_option("refine_tol", args.refine_tol)
+    solver.set_option("autotune", 1)
     order = list(my_rpms) * (1 + (args.warmup + args.steps) // max(1, len(my_rpms)))
     warm, timed = order[: args.warmup], order[args.warmup: args.warmup + args.steps]
     grp = max(1, args.sweep_group)
@@ -486,6 +489,7 @@ def main():
                 if line.startswith("dram_over_algorithmic"):
                     traffic = float(line.split("=")[1]) * per_launch_bytes
     t_dev_all = max_over_ranks(pg, sum(dev_ms) / 1e3)
+    tune_rows = solver.tuning_report()
     t_dev = max_over_ranks(pg, v_dev_s)
     t_wall = max_over_ranks(pg, v_wall_s)
     tot_ok = sum_over_ranks(pg, n_ok)
@@ -532,6 +536,10 @@ def main():
                        "harmonics": args.harmonics, "num_modes": args.num_modes,
                        "speeds": [float(r) for r in timed], "speeds_per_call": grp,
                        "deflated_refinement": True, "tensor_core_updates": bool(solver.get_option("tensor_cores")),
+                       "supernode_autotune": True,
+                       "supernode_shape": next(({"relax": r["relax"], "max_width": int(r["max_width"]),
+                                                 "solve_ms": round(r["solve_ms"], 2), "factor_ms": round(r["factor_ms"], 1)}
+                                                for r in tune_rows if r["chosen"]), None),
                        "refine_tol": args.refine_tol,
                        "verified_speeds": [float(timed[i]) for i in vidx],
                        "parallelism": f"replicas x{ws} (speeds sharded)",

@@ -710,6 +710,173 @@ __global__ void __launch_bounds__(256) k_bwd_tri(const int32_t* __restrict__ ite
     }
 }
 
+// Subtree solves.  One warp carries a whole subtree of narrow fronts (w <= 64: one diagonal
+// block) through the forward solve in postorder and back through the backward solve in
+// reverse postorder, with no grid-wide step between its fronts.  Lane i holds the pivot rows
+// i and i + 32 of the current front in registers; the update rows stay in tbuf, where the
+// parent's assembly (same warp, after __syncwarp) reads them.
+constexpr int SUB_WARPS = 4;                     // subtrees (warps) per CTA
+
+// task = (first, root): forward over the supernodes first..root
+template <typename T>
+__global__ void __launch_bounds__(32 * SUB_WARPS) k_sub_fwd(const int32_t* __restrict__ tasks, int ntasks, SnDev S,
+                                                           SolveArgs A, const T* __restrict__ L, T* __restrict__ x,
+                                                           T* __restrict__ tbuf) {
+    pdl_trigger();
+    const int task = blockIdx.x * SUB_WARPS + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    const int64_t p = blockIdx.y;
+    pdl_wait();
+    if (task >= ntasks || (A.skip && A.skip[p])) return;
+    x += p * A.xstride;
+    tbuf += p * A.tstride;
+    L += p * A.lstride;
+    const int s0 = tasks[2 * task], s1 = tasks[2 * task + 1];
+    for (int s = s0; s <= s1; s++) {
+        const int f = S.first[s];
+        const int w = S.first[s + 1] - f;
+        const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
+        const T* Fs = L + S.loff[s];
+        T* t = tbuf + S.row_ptr[s];
+        // assemble t: pivot rows from x, update rows zero, plus every child's update rows
+        for (int64_t r = lane; r < m; r += 32) t[r] = r < w ? x[f + r] : zero_of<T>();
+        __syncwarp();
+        for (int c = S.child_ptr[s]; c < S.child_ptr[s + 1]; c++) {
+            const int ch = S.child_list[c];
+            const int64_t nu = (S.row_ptr[ch + 1] - S.row_ptr[ch]) - (S.first[ch + 1] - S.first[ch]);
+            const T* tc = tbuf + S.row_ptr[ch + 1] - nu;
+            const int32_t* rl = S.rel + S.rel_ptr[ch];
+            for (int64_t a = lane; a < nu; a += 32) t[rl[a]] += tc[a];
+            __syncwarp();
+        }
+        const T d0 = lane < w ? Fs[(int64_t)lane * m + lane] : one_of<T>();
+        const T d1 = lane + 32 < w ? Fs[(int64_t)(lane + 32) * m + lane + 32] : one_of<T>();
+        const T t0 = lane < w ? t[lane] : zero_of<T>();
+        const T t1 = lane + 32 < w ? t[lane + 32] : zero_of<T>();
+        // y = X t (X: the block's unit-lower inverse, stored below the diagonal), eight columns
+        // of X per step; y_i = 0 for i >= w
+        T y0 = t0, y1 = t1;
+        for (int k0 = 0; k0 + 1 < w; k0 += 8) {
+            T xa[8], xb[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int k = k0 + u;
+                xa[u] = lane > k && lane < w ? Fs[(int64_t)k * m + lane] : zero_of<T>();
+                xb[u] = lane + 32 > k && lane + 32 < w ? Fs[(int64_t)k * m + lane + 32] : zero_of<T>();
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int k = k0 + u;
+                const T tk = shfl_t(k < 32 ? t0 : t1, k & 31);
+                y0 += xa[u] * tk;
+                y1 += xb[u] * tk;
+            }
+        }
+        if (lane < w) x[f + lane] = dev_div(y0, re(d0));
+        if (lane + 32 < w) x[f + lane + 32] = dev_div(y1, re(d1));
+        // update rows: t[r] -= sum_j L(r, j) y_j, two rows per lane, eight columns per step
+        for (int64_t r0 = w; r0 < m; r0 += 64) {
+            const int64_t ra = r0 + lane, rb = ra + 32;
+            const bool ha = ra < m, hb = rb < m;
+            T aa = zero_of<T>(), ab = zero_of<T>();
+            for (int j0 = 0; j0 < w; j0 += 8) {
+                T la[8], lb[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int j = j0 + u;
+                    la[u] = ha && j < w ? Fs[(int64_t)j * m + ra] : zero_of<T>();
+                    lb[u] = hb && j < w ? Fs[(int64_t)j * m + rb] : zero_of<T>();
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int j = j0 + u;
+                    const T yj = shfl_t(j < 32 ? y0 : y1, j & 31);
+                    aa += la[u] * yj;
+                    ab += lb[u] * yj;
+                }
+            }
+            if (ha) t[ra] -= aa;
+            if (hb) t[rb] -= ab;
+        }
+        __syncwarp();
+    }
+}
+
+// task = (first, root): backward over the supernodes root..first
+template <typename T>
+__global__ void __launch_bounds__(32 * SUB_WARPS) k_sub_bwd(const int32_t* __restrict__ tasks, int ntasks, SnDev S,
+                                                           SolveArgs A, const T* __restrict__ L, T* __restrict__ x) {
+    pdl_trigger();
+    const int task = blockIdx.x * SUB_WARPS + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    const int64_t p = blockIdx.y;
+    pdl_wait();
+    if (task >= ntasks || (A.skip && A.skip[p])) return;
+    x += p * A.xstride;
+    L += p * A.lstride;
+    const int s0 = tasks[2 * task], s1 = tasks[2 * task + 1];
+    for (int s = s1; s >= s0; s--) {
+        const int f = S.first[s];
+        const int w = S.first[s + 1] - f;
+        const int64_t m = S.row_ptr[s + 1] - S.row_ptr[s];
+        const T* Fs = L + S.loff[s];
+        const int32_t* rows = S.rows + S.row_ptr[s];
+        // z_j = x_j - sum_{r >= w} conj(L(r, j)) x(rows[r]), eight columns per pass
+        T z0 = lane < w ? x[f + lane] : zero_of<T>();
+        T z1 = lane + 32 < w ? x[f + lane + 32] : zero_of<T>();
+        for (int j0 = 0; j0 < w; j0 += 8) {
+            T acc[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) acc[u] = zero_of<T>();
+            for (int64_t r = w + lane; r < m; r += 64) {
+                const bool h1 = r + 32 < m;
+                const T xa = x[rows[r]];
+                const T xb = h1 ? x[rows[r + 32]] : zero_of<T>();
+                T la[8], lb[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const bool hj = j0 + u < w;
+                    la[u] = hj ? Fs[(int64_t)(j0 + u) * m + r] : zero_of<T>();
+                    lb[u] = hj && h1 ? Fs[(int64_t)(j0 + u) * m + r + 32] : zero_of<T>();
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    acc[u] += conj(la[u]) * xa;
+                    acc[u] += conj(lb[u]) * xb;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const T v = warp_sum(acc[u]);
+                if (j0 + u == lane) z0 -= v;
+                if (j0 + u == lane + 32) z1 -= v;
+            }
+        }
+        // x = X^H z: x_i = z_i + sum_{k > i} conj(X(k, i)) z_k, X(k, i) = Fs[i m + k]
+        T o0 = z0, o1 = z1;
+        for (int i0 = 0; i0 + 1 < w; i0 += 8) {
+            T v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = i0 + u;
+                T a = zero_of<T>();
+                if (lane > i && lane < w) a = conj(Fs[(int64_t)i * m + lane]) * z0;
+                if (lane + 32 > i && lane + 32 < w) a += conj(Fs[(int64_t)i * m + lane + 32]) * z1;
+                v[u] = a;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const T sum = warp_sum(v[u]);
+                if (i0 + u == lane) o0 += sum;
+                if (i0 + u == lane + 32) o1 += sum;
+            }
+        }
+        if (lane < w) x[f + lane] = o0;
+        if (lane + 32 < w) x[f + lane + 32] = o1;
+        __syncwarp();
+    }
+}
+
 template <typename T, typename U>
 __global__ void k_perm_in(int n, const int32_t* __restrict__ perm, const U* __restrict__ b, int64_t ldb,
                           T* __restrict__ x, const double* __restrict__ scale) {
@@ -978,6 +1145,16 @@ void DevSymbolic::upload(const Symbolic& S, const std::vector<int64_t>& dest_h, 
     std::vector<int32_t> si;
     plan64 = build_solve_plan(S, 64, SV_RR, si);
     put(sitems, si);
+    if (std::getenv("TMG_VERBOSE")) {
+        int64_t launches = 0;
+        for (const auto& L : plan64.levels) {
+            if (!L.gath_cnt) continue;
+            launches += 3;
+            for (size_t b = 0; b < L.ftri_cnt.size(); b++) launches += (L.ftri_cnt[b] > 0) + (L.btri_cnt[b] > 0);
+        }
+        std::fprintf(stderr, "[tmg] solve plan n=%d: %d subtrees hold %d of %d fronts; %lld launches per solve\n", n,
+                     plan64.sub_cnt, plan64.sub_fronts, ns, (long long)(launches + 2 * (plan64.sub_cnt > 0)));
+    }
 }
 
 void DevSymbolic::swap(DevSymbolic& o) noexcept {
@@ -1114,16 +1291,19 @@ void mf_solve(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, T* x, T
     auto chunk_of = [&](const DevSymbolic::SolveLevel& L) {
         return (int)std::max<int64_t>(1, std::min<int64_t>(SV_CH, L.maxu));
     };
+    const unsigned sub_grid = (unsigned)ceil_div(P.sub_cnt, SUB_WARPS);
+    if (P.sub_cnt)
+        TMG_LAUNCH_PDL(k_sub_fwd<T>, dim3(sub_grid, B), 32 * SUB_WARPS, 0, st, S.sitems + P.sub_off, P.sub_cnt, sn, A,
+                       bt.L, x, tbuf);
     for (int l = 0; l < nlev; l++) {
-        const int cnt = S.level_ptr[l + 1] - S.level_ptr[l];
-        if (!cnt) continue;
         const auto& L = P.levels[l];
-        TMG_LAUNCH_PDL(k_fwd_gather<T>, dim3(cnt, B), 256, xs_of(L), st, S.level_sn + S.level_ptr[l], sn, A, bt.L, x,
+        if (!L.gath_cnt) continue;
+        TMG_LAUNCH_PDL(k_fwd_gather<T>, dim3(L.gath_cnt, B), 256, xs_of(L), st, S.sitems + L.gath_off, sn, A, bt.L, x,
                        tbuf);
         for (size_t b = 0; b < L.ftri_cnt.size(); b++)
             if (L.ftri_cnt[b])
                 TMG_LAUNCH_PDL(k_fwd_tri<T>, dim3(L.ftri_cnt[b], B), 256, xs, st, S.sitems + L.ftri_off[b], (int)b, sn, A,
-                           bt.L, x, tbuf);
+                               bt.L, x, tbuf);
         if (L.frect_cnt)
             TMG_LAUNCH_PDL(k_fwd_rect<T>, dim3(L.frect_cnt, B), 256, 0, st, S.sitems + L.frect_off, sn, A, bt.L, tbuf);
     }
@@ -1135,8 +1315,11 @@ void mf_solve(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, T* x, T
         for (int b = (int)L.btri_cnt.size() - 1; b >= 1; b--)
             if (L.btri_cnt[b])
                 TMG_LAUNCH_PDL(k_bwd_tri<T>, dim3(L.btri_cnt[b], B), 256, xs, st, S.sitems + L.btri_off[b], b, sn, A, bt.L,
-                           x, tbuf);
+                               x, tbuf);
     }
+    if (P.sub_cnt)
+        TMG_LAUNCH_PDL(k_sub_bwd<T>, dim3(sub_grid, B), 32 * SUB_WARPS, 0, st, S.sitems + P.sub_off, P.sub_cnt, sn, A,
+                       bt.L, x);
     TMG_CHECK_LAUNCH();
 }
 

@@ -693,52 +693,81 @@ void scatter_map(const Symbolic& S, const Pattern& lower, std::vector<int64_t>& 
         }
 }
 
-SolvePlan build_solve_plan(const Symbolic& S, int nb, int rows_per_rect, std::vector<int32_t>& si) {
+SolvePlan build_solve_plan(const Symbolic& S, int nb, int rows_per_rect, std::vector<int32_t>& si,
+                           int64_t subtree_entries) {
     SolvePlan P;
     P.nb = nb;
     const int nlev = (int)S.level_ptr.size() - 1;
     P.levels.assign(std::max(nlev, 0), SolveLevel{});
     auto width = [&](int s) { return S.sn_first[s + 1] - S.sn_first[s]; };
     auto height = [&](int s) { return S.sn_row_ptr[s + 1] - S.sn_row_ptr[s]; };
+    // subtrees solved whole by one warp: every front at most nb wide, at most subtree_entries
+    // panel entries in all, and the subtree a contiguous range of supernodes (postorder)
+    std::vector<int64_t> ent(S.ns, 0);
+    std::vector<int32_t> lo(S.ns), cnt(S.ns, 1);
+    std::vector<char> small(S.ns, 0);
+    for (int s = 0; s < S.ns; s++) {
+        bool ok = width(s) <= nb;
+        int64_t e = (int64_t)width(s) * height(s);
+        lo[s] = s;
+        for (int c = S.child_ptr[s]; c < S.child_ptr[s + 1]; c++) {
+            const int ch = S.child_list[c];
+            if (ch >= s) { ok = false; continue; }   // not a postorder: never merged
+            ok = ok && small[ch];
+            e += ent[ch];
+            cnt[s] += cnt[ch];
+            lo[s] = std::min(lo[s], lo[ch]);
+        }
+        ent[s] = e;
+        small[s] = ok && e <= subtree_entries && s - lo[s] + 1 == cnt[s];
+    }
+    std::vector<std::pair<int64_t, int>> roots;
+    for (int s = 0; s < S.ns; s++) {
+        const int par = S.sn_parent[s];
+        if (small[s] && (par < 0 || !small[par])) roots.push_back({ent[s], s});
+    }
+    std::stable_sort(roots.begin(), roots.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+    P.sub_off = (int64_t)si.size();
+    for (auto [e, s] : roots) {
+        si.push_back(lo[s]); si.push_back(s); P.sub_cnt++;
+        P.sub_fronts += cnt[s];
+    }
     for (int l = 0; l < nlev; l++) {
         SolveLevel& L = P.levels[l];
-        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-            const int s = S.level_sn[q];
+        std::vector<int32_t> up;                   // the level's upper fronts
+        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++)
+            if (!small[S.level_sn[q]]) up.push_back(S.level_sn[q]);
+        L.gath_off = (int64_t)si.size();
+        for (int s : up) {
+            si.push_back(s); L.gath_cnt++;
             L.maxw = std::max(L.maxw, width(s));
             L.maxu = std::max<int64_t>(L.maxu, height(s) - width(s));
         }
-        const int nbk = (L.maxw + nb - 1) / nb;
+        const int nbk = (L.maxw + nb - 1) / nb;   // diagonal blocks of the widest upper front
         L.ftri_off.assign(std::max(nbk, 1), 0);
         L.ftri_cnt.assign(std::max(nbk, 1), 0);
         L.btri_off.assign(std::max(nbk, 1), 0);
         L.btri_cnt.assign(std::max(nbk, 1), 0);
         for (int b = 0; b + 1 < nbk; b++) {              // forward triangle launches
             L.ftri_off[b] = (int64_t)si.size();
-            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-                const int s = S.level_sn[q];
+            for (int s : up)
                 for (int r0 = (b + 1) * nb; r0 < width(s); r0 += nb) { si.push_back(s); si.push_back(r0); L.ftri_cnt[b]++; }
-            }
-        }
-        L.frect_off = (int64_t)si.size();
-        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-            const int s = S.level_sn[q];
-            for (int64_t r0 = width(s); r0 < height(s); r0 += rows_per_rect) {
-                si.push_back(s); si.push_back((int32_t)r0); L.frect_cnt++;
-            }
-        }
-        L.brect_off = (int64_t)si.size();
-        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-            const int s = S.level_sn[q];
-            for (int c0 = 0; c0 < width(s); c0 += nb) { si.push_back(s); si.push_back(c0); L.brect_cnt++; }
         }
         for (int b = 1; b < nbk; b++) {                  // backward triangle launches
             L.btri_off[b] = (int64_t)si.size();
-            for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
-                const int s = S.level_sn[q];
+            for (int s : up) {
                 if (width(s) <= b * nb) continue;
                 for (int c0 = 0; c0 < b * nb; c0 += nb) { si.push_back(s); si.push_back(c0); L.btri_cnt[b]++; }
             }
         }
+        L.frect_off = (int64_t)si.size();
+        for (int s : up)
+            for (int64_t r0 = width(s); r0 < height(s); r0 += rows_per_rect) {
+                si.push_back(s); si.push_back((int32_t)r0); L.frect_cnt++;
+            }
+        L.brect_off = (int64_t)si.size();
+        for (int s : up)
+            for (int c0 = 0; c0 < width(s); c0 += nb) { si.push_back(s); si.push_back(c0); L.brect_cnt++; }
     }
     // diagonal blocks to invert after the factorisation
     P.inv_small_off = (int64_t)si.size();

@@ -60,29 +60,44 @@ struct Symbolic {
 Symbolic analyze(const Pattern& lower, double relax = 0.0, int32_t relax_max_width = 0,
                  const std::vector<int32_t>* amd = nullptr);
 
-// Triangular-solve schedule for diagonal blocks of width nb, per tree level (host side; the
-// device kernels read the item lists).  Forward: gather (the level's supernodes), triangle
-// launches b = 0.. (items (s, r0): rows [r0, r0 + nb) of the triangle below block b), one
-// rectangle launch (items (s, r0): rows [r0, r0 + rows_per_rect) below the triangle).
-// Backward: one rectangle launch (items (s, c0): columns [c0, c0 + nb)), triangle launches
-// b = last .. 1 (items (s, c0): columns [c0, c0 + nb) left of block b).  Inverse lists: items
-// (s, b) of the diagonal blocks to invert after a factorisation (small: width <= 32).
+// Triangular-solve schedule for diagonal blocks of width nb (host side; the device kernels
+// read the item lists).
+//
+// Subtrees: the largest subtrees whose fronts are all at most nb columns wide and that hold
+// at most `subtree_entries` panel entries in all are solved whole, one warp per subtree (in
+// postorder forward, in reverse postorder backward), in one launch per direction.  Supernodes
+// are numbered in postorder, so a subtree is the contiguous range (first, root); the tasks
+// are listed heaviest first.
+//
+// The other ("upper") fronts go level by level.  Forward: gather (the level's upper fronts;
+// it also solves each front's first diagonal block), triangle launches b = 0.. (items
+// (s, r0): rows [r0, r0 + nb) of the triangle below block b), one rectangle launch (items
+// (s, r0): rows [r0, r0 + rows_per_rect) below the triangle).  Backward: one rectangle launch
+// (items (s, c0): columns [c0, c0 + nb); it also solves each front's last diagonal block),
+// triangle launches b = last .. 1 (items (s, c0): columns [c0, c0 + nb) left of block b).
+// The forward subtree launch runs before the levels and the backward one after them.  Inverse
+// lists: items (s, b) of the diagonal blocks to invert after a factorisation (small: width
+// <= 32).
 struct SolveLevel {
     std::vector<int64_t> ftri_off, btri_off;   // index b
     std::vector<int32_t> ftri_cnt, btri_cnt;
-    int64_t frect_off = 0, brect_off = 0;
-    int32_t frect_cnt = 0, brect_cnt = 0;
-    int32_t maxw = 0;                          // widest front of the level
+    int64_t gath_off = 0, frect_off = 0, brect_off = 0;
+    int32_t gath_cnt = 0, frect_cnt = 0, brect_cnt = 0;
+    int32_t maxw = 0;                          // widest upper front of the level
     int64_t maxu = 0;                          // most rows below a triangle (m - w)
 };
 struct SolvePlan {
     int nb = 0;
+    int64_t sub_off = 0;                       // subtree tasks (first, root), heaviest first
+    int32_t sub_cnt = 0;
+    int32_t sub_fronts = 0;                    // fronts inside the subtrees
     std::vector<SolveLevel> levels;
     int64_t inv_small_off = 0, inv_large_off = 0;
     int32_t inv_small_cnt = 0, inv_large_cnt = 0;
 };
 // Builds the schedule of S; its items are appended to `items` (offsets index that array).
-SolvePlan build_solve_plan(const Symbolic& S, int nb, int rows_per_rect, std::vector<int32_t>& items);
+SolvePlan build_solve_plan(const Symbolic& S, int nb, int rows_per_rect, std::vector<int32_t>& items,
+                           int64_t subtree_entries = 65536);
 
 // Destination of every lower-triangle entry of `lower` (in its CSC order) inside the
 // front storage of `S`; conj flag set when the entry lands transposed.
