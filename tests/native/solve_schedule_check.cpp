@@ -1,11 +1,14 @@
 // Host check of the triangular-solve schedule (tests/test_solve_schedule.py): builds the
 // supernodal analysis and the solve plan with the library's own host code (sym.cpp), replays
-// every launch item with the index arithmetic of the device kernels (mf.cu: k_inv_*,
-// k_fwd_gather, k_fwd_tri, k_fwd_rect, k_bwd_rect, k_bwd_tri) with bounds checks, and compares
+// every launch item with the index arithmetic of the device kernels (mf.cu: k_inv_*, k_sub_fwd,
+// k_fwd_gather, k_fwd_tri, k_fwd_rect, k_bwd_rect, k_bwd_tri, k_sub_bwd) with bounds checks, and
+// checks that every supernode is solved exactly once per direction, by one subtree task (whose
+// fronts are at most 64 wide and whose children lie inside the task) or by its level; compares
 // the result with a plain column-by-column supernodal solve on the same random unit-lower L and
 // positive D, and checks every column's fill against the rows its front stores.  Optional
 // arguments: supernode relaxation and its width limit (analyze()).  Prints
-// "max_rel_err=<e> bounds_errors=<k> launches=<n> supernodes=<s> struct_errors=<f>".
+// "max_rel_err=<e> bounds_errors=<k> launches=<n> supernodes=<s> struct_errors=<f> subtrees=<t>
+// subtree_fronts=<u>".
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -122,12 +125,44 @@ int main(int argc, char** argv) {
             v[i] = a;
         }
     };
-    // forward sweep
+    std::vector<int> solved_fwd(ns, 0), solved_bwd(ns, 0);
+    // forward sweep: k_sub_fwd (one warp per task, supernodes first..root in order)
+    if (plan.sub_cnt) launches++;
+    for (int it = 0; it < plan.sub_cnt; it++) {
+        const int s0 = item(plan.sub_off, it, 0), s1 = item(plan.sub_off, it, 1);
+        if (s0 > s1 || s0 < 0 || s1 >= ns) { nerr++; continue; }
+        for (int s = s0; s <= s1; s++) {
+            solved_fwd[s]++;
+            const int fs = S.sn_first[s], w = W(s);
+            if (w > 64) nerr++;
+            for (int64_t r = 0; r < H(s); r++) Tat(s, r) = r < w ? Xat(fs + r) : 0.0;
+            for (int c = S.child_ptr[s]; c < S.child_ptr[s + 1]; c++) {
+                const int ch = S.child_list[c];
+                if (ch < s0 || ch >= s) nerr++;                            // solved earlier by this warp
+                const int64_t nu = H(ch) - W(ch);
+                for (int64_t a = 0; a < nu; a++) Tat(s, S.rel[S.rel_ptr[ch] + a]) += Tat(ch, H(ch) - nu + a);
+            }
+            std::vector<double> y(64, 0.0);
+            for (int i = 0; i < w; i++) {
+                double a = Tat(s, i);
+                for (int k = 0; k < i; k++) a += Lat(s, (int64_t)k * H(s) + i) * Tat(s, k);
+                y[i] = a;
+            }
+            for (int i = 0; i < w; i++) Xat(fs + i) = y[i] / Lat(s, (int64_t)i * H(s) + i);
+            for (int64_t r = w; r < H(s); r++) {
+                double a = 0.0;
+                for (int j = 0; j < w; j++) a += Lat(s, (int64_t)j * H(s) + r) * y[j];
+                Tat(s, r) -= a;
+            }
+        }
+    }
     for (int l = 0; l < nlev; l++) {
         const SolveLevel& Lv = plan.levels[l];
-        launches++;
-        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {      // k_fwd_gather
-            const int s = S.level_sn[q], fs = S.sn_first[s];
+        if (Lv.gath_cnt) launches++;
+        for (int q = 0; q < Lv.gath_cnt; q++) {                           // k_fwd_gather
+            const int s = items[Lv.gath_off + q], fs = S.sn_first[s];
+            solved_fwd[s]++;
+            if (W(s) > Lv.maxw || H(s) - W(s) > Lv.maxu) nerr++;          // staging sized by the level
             for (int64_t r = 0; r < H(s); r++) Tat(s, r) = r < W(s) ? Xat(fs + r) : 0.0;
             for (int c = S.child_ptr[s]; c < S.child_ptr[s + 1]; c++) {
                 const int ch = S.child_list[c];
@@ -220,6 +255,33 @@ int main(int argc, char** argv) {
             }
         }
     }
+    // k_sub_bwd (one warp per task, supernodes root..first)
+    if (plan.sub_cnt) launches++;
+    for (int it = 0; it < plan.sub_cnt; it++) {
+        const int s0 = item(plan.sub_off, it, 0), s1 = item(plan.sub_off, it, 1);
+        if (s0 > s1 || s0 < 0 || s1 >= ns) continue;
+        for (int s = s1; s >= s0; s--) {
+            const int fs = S.sn_first[s], w = W(s);
+            const int32_t* rows = &S.sn_rows[S.sn_row_ptr[s]];
+            std::vector<double> z(64, 0.0);
+            for (int j = 0; j < w; j++) {
+                double a = 0.0;
+                for (int64_t r = w; r < H(s); r++) a += Lat(s, (int64_t)j * H(s) + r) * Xat(rows[r]);
+                z[j] = Xat(fs + j) - a;
+            }
+            for (int i = 0; i < w; i++) {
+                double a = z[i];
+                for (int k = i + 1; k < w; k++) a += Lat(s, (int64_t)i * H(s) + k) * z[k];
+                Xat(fs + i) = a;
+            }
+        }
+    }
+    for (int it = 0; it < plan.sub_cnt; it++)
+        for (int s = item(plan.sub_off, it, 0); s <= item(plan.sub_off, it, 1) && s < ns; s++) solved_bwd[s]++;
+    for (const SolveLevel& Lv : plan.levels)
+        for (int q = 0; q < Lv.gath_cnt; q++) solved_bwd[items[Lv.gath_off + q]]++;
+    for (int s = 0; s < ns; s++)
+        if (solved_fwd[s] != 1 || solved_bwd[s] != 1) nerr++;
     double err = 0.0, sc = 0.0;
     for (int i = 0; i < n; i++) {
         err = std::max(err, std::fabs(x[i] - xr[i]));
@@ -262,7 +324,7 @@ int main(int argc, char** argv) {
         }
     }
     if (fill != S.nnz_l) struct_errors++;   // the recomputed fill must be the analysis's nnz(L)
-    std::printf("max_rel_err=%.3e bounds_errors=%ld launches=%ld supernodes=%d struct_errors=%ld\n", err / sc, nerr,
-                launches, ns, struct_errors);
+    std::printf("max_rel_err=%.3e bounds_errors=%ld launches=%ld supernodes=%d struct_errors=%ld subtrees=%d "
+                "subtree_fronts=%d\n", err / sc, nerr, launches, ns, struct_errors, plan.sub_cnt, plan.sub_fronts);
     return 0;
 }

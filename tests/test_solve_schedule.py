@@ -1,9 +1,10 @@
 """The triangular-solve schedule on the host: the library's supernodal analysis and solve plan
 (turbomodal_gb300/csrc/sym.cpp) replayed with the device kernels' index arithmetic
-(tests/native/solve_schedule_check.cpp) must stay inside every panel, front vector and solution
-vector and reproduce a plain supernodal solve to roundoff (1e-12 relative), and every column's
-fill must lie inside its supernode's front, for fundamental and for relaxed supernodes
-(amalgamation by analyze(relax > 0), which the solver does not use yet), on the harmonic operator
+(tests/native/solve_schedule_check.cpp: the warp-per-subtree kernels, then the level kernels)
+must stay inside every panel, front vector and solution vector, solve every supernode exactly
+once per direction and reproduce a plain supernodal solve to roundoff (1e-12 relative), and every
+column's fill must lie inside its supernode's front, for fundamental and for relaxed supernodes
+(amalgamation by analyze(relax > 0), one of the autotuner's shapes), on the harmonic operator
 and on the 2n Lancaster operator of the Coriolis QEP."""
 
 import os
@@ -79,3 +80,5 @@ def test_solve_schedule_matches_plain_solve(checker, oracle, case, relax):
     assert int(vals["struct_errors"]) == 0
     assert float(vals["max_rel_err"]) <= 1e-12
     assert int(vals["launches"]) > 0
+    # most fronts of these sectors are narrow leaves: the subtree kernels carry them
+    assert int(vals["subtrees"]) > 0 and 2 * int(vals["subtree_fronts"]) > int(vals["supernodes"])
