@@ -13,6 +13,7 @@
 // simplicial up-looking LDL^T (src/hermitian_lanczos.cpp:12-56); the supernodal form has the
 // same L and D in exact arithmetic.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <map>
@@ -55,24 +56,32 @@ __global__ void k_scatter(int64_t n, const T* __restrict__ vals, const int64_t* 
     L[p * lstride + d] = cj[q] ? conj(v) : v;
 }
 
+// Zero the lower triangle (row >= column: the only part the Schur updates write and the
+// extend-add reads) of every listed front's update block; one warp per column.
 template <typename T>
 __global__ void k_uzero(const int32_t* __restrict__ items, int nitems, SnDev S, T* __restrict__ U, int64_t ustride) {
     const int64_t p = blockIdx.z;
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int it = blockIdx.y; it < nitems; it += gridDim.y) {
         const int s = items[it];
         const int64_t u = (S.row_ptr[s + 1] - S.row_ptr[s]) - (S.first[s + 1] - S.first[s]);
         T* Us = U + p * ustride + S.uoff[s];
-        for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < u * u; q += (int64_t)gridDim.x * blockDim.x)
-            Us[q] = zero_of<T>();
+        for (int64_t b = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); b < u; b += warps)
+            for (int64_t a = b + lane; a < u; a += 32) Us[b * u + a] = zero_of<T>();
     }
 }
 
+// Add each listed child's update block (lower triangle, column by column: one warp per column)
+// into its parent's front, through the child's row map.
 template <typename T>
 __global__ void k_extend_add(const int32_t* __restrict__ items, int nitems, SnDev S, T* __restrict__ L,
                              T* __restrict__ U, int64_t lstride, int64_t ustride) {
     const int64_t p = blockIdx.z;
     T* Lp = L + p * lstride;
     T* Up = U + p * ustride;
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int it = blockIdx.y; it < nitems; it += gridDim.y) {
         const int par = items[2 * it], c = items[2 * it + 1];
         const int64_t mc = S.row_ptr[c + 1] - S.row_ptr[c];
@@ -82,11 +91,9 @@ __global__ void k_extend_add(const int32_t* __restrict__ items, int nitems, SnDe
         const int wp = S.first[par + 1] - S.first[par];
         const int32_t* rl = S.rel + S.rel_ptr[c];
         const T* Uc = Up + S.uoff[c];
-        for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < u * u;
-             idx += (int64_t)gridDim.x * blockDim.x) {
-            const int64_t a = idx % u, b = idx / u;
-            if (a < b) continue;
-            *fent(S, Lp, Up, par, mp, wp, rl[a], rl[b]) += Uc[b * u + a];
+        for (int64_t b = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); b < u; b += warps) {
+            const int32_t jb = rl[b];
+            for (int64_t a = b + lane; a < u; a += 32) *fent(S, Lp, Up, par, mp, wp, rl[a], jb) += Uc[b * u + a];
         }
     }
 }
@@ -1206,15 +1213,17 @@ void mf_factor(cudaStream_t st, const DevSymbolic& S, const Batch<T>& bt, int* s
     const unsigned B = bt.B;
     for (const auto& stp : S.steps) {
         if (stp.uzero_cnt) {
-            const unsigned gx = (unsigned)std::min<int64_t>(std::max<int64_t>(1, ceil_div(stp.uzero_max, 256)), 2048);
+            // one warp per column of the largest update block of the step (8 per CTA; uzero_max
+            // counts its entries)
+            const int64_t ucols = (int64_t)std::ceil(std::sqrt((double)stp.uzero_max));
+            const unsigned gx = (unsigned)std::min<int64_t>(std::max<int64_t>(1, ceil_div(ucols, 8)), 2048);
             const unsigned gy = (unsigned)std::min<int64_t>(stp.uzero_cnt, 65535);
             TMG_LAUNCH(k_uzero<T>, dim3(gx, gy, B), 256, 0, st, S.items + stp.uzero_off, stp.uzero_cnt, sn, bt.U,
                        bt.ustride);
         }
         for (size_t r = 0; r < stp.ext_off.size(); r++) {
             if (stp.ext_cnt[r] == 0) continue;
-            const int64_t ent = (int64_t)stp.ext_max[r] * stp.ext_max[r];
-            const unsigned gx = (unsigned)std::min<int64_t>(std::max<int64_t>(1, ceil_div(ent, 256)), 2048);
+            const unsigned gx = (unsigned)std::min<int64_t>(std::max<int64_t>(1, ceil_div(stp.ext_max[r], 8)), 2048);
             const unsigned gy = (unsigned)std::min<int64_t>(stp.ext_cnt[r], 65535);
             TMG_LAUNCH(k_extend_add<T>, dim3(gx, gy, B), 256, 0, st, S.items + stp.ext_off[r], stp.ext_cnt[r], sn, bt.L,
                        bt.U, bt.lstride, bt.ustride);
