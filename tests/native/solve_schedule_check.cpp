@@ -131,6 +131,11 @@ int main(int argc, char** argv) {
     for (int it = 0; it < plan.sub_cnt; it++) {
         const int s0 = item(plan.sub_off, it, 0), s1 = item(plan.sub_off, it, 1);
         if (s0 > s1 || s0 < 0 || s1 >= ns) { nerr++; continue; }
+        int64_t entries = 0;                                              // the plan's subtree bound
+        for (int s = s0; s <= s1; s++) entries += H(s) * W(s);
+        if (entries > 65536) nerr++;
+        const int top = S.sn_parent[s1];
+        if (top >= s0 && top <= s1) nerr++;                               // the task ends at its root
         for (int s = s0; s <= s1; s++) {
             solved_fwd[s]++;
             const int fs = S.sn_first[s], w = W(s);
